@@ -1,0 +1,392 @@
+"""GB300 (sm_103a) Kirchhoff-Love shell hot path of gsStructuralAnalysis -- Python front-end.
+
+ctypes bindings of the C-ABI in include/klshell_gb300.h.  The classes mirror the reference's
+solver classes and callbacks (gsStaticNewton, gsALMCrisfield/Riks/LoadControl,
+gsBucklingSolver, gsModalSolver, the Jacobian_t / Residual_t / ALResidual_t callbacks) with
+the same option keys.  Everything runs in the CUDA library: there is no CPU code path, and
+loading fails loudly if the library was not built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import problems  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libklshell_gb300.so")
+_lib = None
+
+SUCCESS, NOT_CONVERGED, ASSEMBLY_ERROR, SOLVER_ERROR, NOT_STARTED, OTHER_ERROR = range(6)
+
+_c_int, _c_i64, _c_dbl, _c_vp, _c_char_p = ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p, ctypes.c_char_p
+
+
+class PatchDesc(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_int32), ("n1", ctypes.c_int32), ("n2", ctypes.c_int32), ("nq", ctypes.c_int32),
+                ("knots1", _c_vp), ("knots2", _c_vp), ("ctrl", _c_vp),
+                ("E", _c_dbl), ("nu", _c_dbl), ("thickness", _c_dbl), ("density", _c_dbl),
+                ("fixed", _c_vp), ("surface_load", _c_vp),
+                ("n_point_loads", ctypes.c_int32), ("point_loads", _c_vp),
+                ("n_edge_loads", ctypes.c_int32), ("edge_loads", _c_vp)]
+
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "klsa_last_error": (_c_char_p, []),
+    "klsa_launch_count": (ctypes.c_uint64, []),
+    "klsa_problem_create": (_c_int, [ctypes.POINTER(PatchDesc), ctypes.POINTER(_c_vp)]),
+    "klsa_problem_destroy": (_c_int, [_c_vp]),
+    "klsa_problem_ndof": (_c_i64, [_c_vp]),
+    "klsa_problem_nnz": (_c_i64, [_c_vp]),
+    "klsa_force": (_c_int, [_c_vp, _c_vp]),
+    "klsa_residual": (_c_int, [_c_vp, _c_vp, _c_vp]),
+    "klsa_al_residual": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
+    "klsa_jacobian_csr": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "klsa_mass_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_options_create": (_c_vp, []),
+    "klsa_options_destroy": (None, [_c_vp]),
+    "klsa_options_set_real": (_c_int, [_c_vp, _c_char_p, _c_dbl]),
+    "klsa_options_set_int": (_c_int, [_c_vp, _c_char_p, _c_i64]),
+    "klsa_options_set_string": (_c_int, [_c_vp, _c_char_p, _c_char_p]),
+    "klsa_solver_create": (_c_int, [_c_vp, _c_char_p, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_solver_destroy": (_c_int, [_c_vp]),
+    "klsa_solver_compute_jacobian": (_c_int, [_c_vp, _c_vp]),
+    "klsa_solver_compute_linear": (_c_int, [_c_vp]),
+    "klsa_solver_solve": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int]),
+    "klsa_solver_stability": (_c_int, [_c_vp, _c_vp, _c_vp]),
+    "klsa_static_create": (_c_int, [_c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_static_destroy": (_c_int, [_c_vp]),
+    "klsa_static_solve": (_c_int, [_c_vp]),
+    "klsa_static_solve_linear": (_c_int, [_c_vp]),
+    "klsa_static_set_load_factor": (_c_int, [_c_vp, _c_dbl]),
+    "klsa_static_set_displacement": (_c_int, [_c_vp, _c_vp]),
+    "klsa_static_solution": (_c_int, [_c_vp, _c_vp]),
+    "klsa_static_iterations": (_c_int, [_c_vp]),
+    "klsa_alm_create": (_c_int, [_c_vp, _c_char_p, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_alm_destroy": (_c_int, [_c_vp]),
+    "klsa_alm_initialize": (_c_int, [_c_vp]),
+    "klsa_alm_step": (_c_int, [_c_vp]),
+    "klsa_alm_set_length": (_c_int, [_c_vp, _c_dbl]),
+    "klsa_alm_reduce_length": (_c_int, [_c_vp, _c_dbl]),
+    "klsa_alm_get_length": (_c_dbl, [_c_vp]),
+    "klsa_alm_set_solution": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_alm_set_solution_step": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_alm_set_initial_guess": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_alm_solution": (_c_int, [_c_vp, _c_vp, _c_vp]),
+    "klsa_alm_info": (_c_int, [_c_vp, _c_vp]),
+    "klsa_alm_history": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
+    "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
+    "klsa_nd_stats": (_c_int, [_c_int, _c_int, _c_int, _c_vp, _c_int, _c_vp]),
+    "klsa_nd_export": (_c_int, [_c_int, _c_int, _c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_i64, _c_i64]),
+}
+
+
+class KLSAError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"status {code}: {msg}")
+        self.code = code
+
+
+def load_library(path: str | None = None):
+    """Load the CUDA library (raises if it was not built -- there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"CUDA library not built: {p} (run gsstructuralanalysis_gb300/build.py)")
+    L = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_c_vp)
+
+
+def _check(code):
+    if code < 0:
+        raise KLSAError(code, _lib.klsa_last_error().decode())
+    return code
+
+
+def launch_count() -> int:
+    return int(load_library().klsa_launch_count())
+
+
+class Options:
+    """gsOptionList-like key/value store handed to the solvers."""
+
+    def __init__(self, values: dict | None = None):
+        L = load_library()
+        self.h = L.klsa_options_create()
+        for k, v in (values or {}).items():
+            self[k] = v
+
+    def __setitem__(self, key, value):
+        L = load_library()
+        k = key.encode()
+        if isinstance(value, str):
+            L.klsa_options_set_string(self.h, k, value.encode())
+        elif isinstance(value, (bool, int, np.integer)):
+            L.klsa_options_set_int(self.h, k, int(value))
+        else:
+            L.klsa_options_set_real(self.h, k, float(value))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_options_destroy(self.h)
+            self.h = None
+
+
+class Problem:
+    """Device-resident patch problem: the Jacobian_t / Residual_t / ALResidual_t / Mass_t /
+    Force_t callbacks of the reference (gsStructuralAnalysisTypes.h:58-93)."""
+
+    def __init__(self, prob):
+        L = load_library()
+        self.prob = prob
+        self._keep = dict(
+            k1=np.ascontiguousarray(prob.knots1, dtype=np.float64),
+            k2=np.ascontiguousarray(prob.knots2, dtype=np.float64),
+            X=np.ascontiguousarray(prob.ctrl, dtype=np.float64),
+            fx=np.ascontiguousarray(prob.fixed, dtype=np.uint8),
+            qs=np.ascontiguousarray(prob.surface_load, dtype=np.float64),
+            pl=np.ascontiguousarray(prob.point_loads, dtype=np.float64).reshape(-1, 5),
+            ed=np.ascontiguousarray(prob.edge_loads, dtype=np.float64).reshape(-1, 4),
+        )
+        k = self._keep
+        d = PatchDesc(prob.p, prob.n1, prob.n2, prob.nq, _ptr(k["k1"]), _ptr(k["k2"]), _ptr(k["X"]),
+                      prob.E, prob.nu, prob.t, prob.rho, _ptr(k["fx"]), _ptr(k["qs"]),
+                      len(k["pl"]), _ptr(k["pl"]), len(k["ed"]), _ptr(k["ed"]))
+        h = _c_vp()
+        _check(L.klsa_problem_create(ctypes.byref(d), ctypes.byref(h)))
+        self.h = h
+        self.ndof = int(L.klsa_problem_ndof(h))
+        self.nnz = int(L.klsa_problem_nnz(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.klsa_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def force(self):
+        F = np.zeros(self.ndof)
+        _check(_lib.klsa_force(self.h, _ptr(F)))
+        return F
+
+    def residual(self, x):
+        """Residual_t: R = Fext - Fint(x)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        R = np.zeros(self.ndof)
+        _check(_lib.klsa_residual(self.h, _ptr(x), _ptr(R)))
+        return R
+
+    def al_residual(self, x, lam):
+        """ALResidual_t: R = Fint(x) - lam F."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        R = np.zeros(self.ndof)
+        _check(_lib.klsa_al_residual(self.h, _ptr(x), float(lam), _ptr(R)))
+        return R
+
+    def _csr(self, fn, *args):
+        import scipy.sparse as sp
+        rp = np.zeros(self.ndof + 1, dtype=np.int64)
+        cols = np.zeros(self.nnz, dtype=np.int32)
+        vals = np.zeros(self.nnz)
+        _check(fn(self.h, *args, _ptr(rp), _ptr(cols), _ptr(vals)))
+        return sp.csr_matrix((vals, cols, rp), shape=(self.ndof, self.ndof))
+
+    def jacobian(self, x, precision: int = 1):
+        """Jacobian_t: K(x); precision 0 = FP32 element integration, 1 = FP64."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        return self._csr(_lib.klsa_jacobian_csr, _ptr(x), int(precision))
+
+    def mass(self):
+        return self._csr(_lib.klsa_mass_csr)
+
+
+class SparseSolver:
+    """Named solver plug-in (gsSparseSolver<T>::get(name)): 'SimplicialLDLT' (multifrontal
+    LDL^T) or 'CGDiagonal' (Jacobi PCG)."""
+
+    def __init__(self, problem: Problem, name: str = "SimplicialLDLT", options: dict | None = None):
+        self.problem = problem
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_solver_create(problem.h, name.encode(), self.opts.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_solver_destroy(self.h)
+            self.h = None
+
+    def compute_jacobian(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        return _check(_lib.klsa_solver_compute_jacobian(self.h, _ptr(x)))
+
+    def compute_linear(self):
+        return _check(_lib.klsa_solver_compute_linear(self.h))
+
+    def solve(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        x = np.zeros_like(b)
+        _check(_lib.klsa_solver_solve(self.h, _ptr(b), _ptr(x), nrhs))
+        return x
+
+    def stability(self):
+        mn = np.zeros(1)
+        ng = np.zeros(1, dtype=np.int64)
+        _check(_lib.klsa_solver_stability(self.h, _ptr(mn), _ptr(ng)))
+        return float(mn[0]), int(ng[0])
+
+
+class StaticNewton:
+    """gsStaticNewton (gsStaticSolvers/gsStaticNewton.hpp) on the device."""
+
+    def __init__(self, problem: Problem, options: dict | None = None):
+        self.problem = problem
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_static_create(problem.h, self.opts.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_static_destroy(self.h)
+            self.h = None
+
+    def solve(self):
+        return _check(_lib.klsa_static_solve(self.h))
+
+    def solveLinear(self):
+        return _check(_lib.klsa_static_solve_linear(self.h))
+
+    def setLoad(self, lam):
+        _check(_lib.klsa_static_set_load_factor(self.h, float(lam)))
+
+    def setDisplacement(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(_lib.klsa_static_set_displacement(self.h, _ptr(U)))
+
+    def solution(self):
+        U = np.zeros(self.problem.ndof)
+        _check(_lib.klsa_static_solution(self.h, _ptr(U)))
+        return U
+
+    def iterations(self):
+        return int(_lib.klsa_static_iterations(self.h))
+
+
+class _ALM:
+    method = ""
+
+    def __init__(self, problem: Problem, options: dict | None = None):
+        self.problem = problem
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_alm_create(problem.h, self.method.encode(), self.opts.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_alm_destroy(self.h)
+            self.h = None
+
+    def initialize(self):
+        _check(_lib.klsa_alm_initialize(self.h))
+
+    def step(self):
+        return _check(_lib.klsa_alm_step(self.h))
+
+    def setLength(self, length):
+        _check(_lib.klsa_alm_set_length(self.h, float(length)))
+
+    def reduceLength(self, fac=0.5):
+        _check(_lib.klsa_alm_reduce_length(self.h, float(fac)))
+
+    def getLength(self):
+        return float(_lib.klsa_alm_get_length(self.h))
+
+    def setSolution(self, U, L):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(_lib.klsa_alm_set_solution(self.h, _ptr(U), float(L)))
+
+    def setSolutionStep(self, DU, DL):
+        DU = np.ascontiguousarray(DU, dtype=np.float64)
+        _check(_lib.klsa_alm_set_solution_step(self.h, _ptr(DU), float(DL)))
+
+    def setInitialGuess(self, U, L):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(_lib.klsa_alm_set_initial_guess(self.h, _ptr(U), float(L)))
+
+    def solutionU(self):
+        U = np.zeros(self.problem.ndof)
+        _check(_lib.klsa_alm_solution(self.h, _ptr(U), None))
+        return U
+
+    def solutionL(self):
+        L = np.zeros(1)
+        _check(_lib.klsa_alm_solution(self.h, None, _ptr(L)))
+        return float(L[0])
+
+    def info(self):
+        out = np.zeros(10)
+        _check(_lib.klsa_alm_info(self.h, _ptr(out)))
+        keys = ["iterations", "residueF", "residueU", "phi", "converged", "Lprev", "DLold", "n_jac", "n_res",
+                "n_solve"]
+        return dict(zip(keys, out.tolist()))
+
+    def history(self):
+        n = self.problem.ndof
+        Up, DUo = np.zeros(n), np.zeros(n)
+        Lp, DLo = np.zeros(1), np.zeros(1)
+        _check(_lib.klsa_alm_history(self.h, _ptr(Up), _ptr(Lp), _ptr(DUo), _ptr(DLo)))
+        return Up, float(Lp[0]), DUo, float(DLo[0])
+
+
+class ALMCrisfield(_ALM):
+    """gsALMCrisfield (gsALMSolvers/gsALMCrisfield.hpp)."""
+    method = "Crisfield"
+
+
+class ALMRiks(_ALM):
+    """gsALMRiks (gsALMSolvers/gsALMRiks.hpp)."""
+    method = "Riks"
+
+
+class ALMLoadControl(_ALM):
+    """gsALMLoadControl (gsALMSolvers/gsALMLoadControl.hpp)."""
+    method = "LoadControl"
+
+
+def buckling(problem: Problem, nev: int, shift: float, scaling: float = 1.0, options: dict | None = None,
+             vectors: bool = True):
+    """gsBucklingSolver + Buckling-mode shift-invert Lanczos: K_L v = lambda (K(u_L) - K_L) v."""
+    o = Options(options)
+    vals = np.zeros(nev)
+    vecs = np.zeros((nev, problem.ndof)) if vectors else None
+    st = _check(_lib.klsa_buckling(problem.h, o.h, int(nev), float(shift), float(scaling), _ptr(vals), _ptr(vecs)))
+    return st, vals, vecs
+
+
+def modal(problem: Problem, nev: int, shift: float = 0.0, options: dict | None = None, vectors: bool = True):
+    """gsModalSolver + ShiftInvert-mode Lanczos: K v = lambda M v."""
+    o = Options(options)
+    vals = np.zeros(nev)
+    vecs = np.zeros((nev, problem.ndof)) if vectors else None
+    st = _check(_lib.klsa_modal(problem.h, o.h, int(nev), float(shift), _ptr(vals), _ptr(vecs)))
+    return st, vals, vecs

@@ -1,0 +1,568 @@
+// assemble.cu -- Kirchhoff-Love shell tangent K(u), internal force Fint(u) and mass M on sm_103a.
+//
+// One warp per element.  Lane a (< (p+1)^2) owns control point a of the element: it loads the
+// displacement once, forms its basis derivatives at each Gauss point, and the warp reduces the
+// deformed base vectors / second derivatives with butterfly shuffles.  Every lane then
+// evaluates the point's strains and stress resultants redundantly (scalar work), writes its
+// control point's first-variation blocks to shared memory, and accumulates the 3x3 blocks of
+// its assigned control-point pairs (A <= B) in registers across all Gauss points.
+//
+// Second variation of the bending strain (per dof pair r=(A,i), s=(B,j)), with ~a3 = a1 x a2,
+// l = |~a3|, P_r = d~a3/du_r, q_r = a3.P_r, v = m^11 x,11 + m^22 x,22 + 2 m^12 x,12,
+// c = v.a3, w = v - c a3, g_r = v.P_r, M_A = m^11 N_A,11 + m^22 N_A,22 + 2 m^12 N_A,12:
+//   sum_ab w_ab d2b_ab = M_A (da3/du_s)_i + M_B (da3/du_r)_j
+//                      + (N_A,1 N_B,2 - N_A,2 N_B,1) e_ijk w_k / l
+//                      + (3c q_r q_s - g_r q_s - g_s q_r - c P_r.P_s) / l^2
+// (the CPU oracle evaluates the same quantity from explicit vector derivatives instead).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <utility>
+
+#include "problem.h"
+
+namespace klsa {
+
+namespace {
+
+template <class T> struct V3T { T x, y, z; };
+template <class T> __device__ __forceinline__ V3T<T> mk(T a, T b, T c) { return {a, b, c}; }
+template <class T> __device__ __forceinline__ T dot3(V3T<T> a, V3T<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> __device__ __forceinline__ V3T<T> cross3(V3T<T> a, V3T<T> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class T> __device__ __forceinline__ T comp(V3T<T> a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+template <class T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-control-point first-variation data in shared memory.
+template <class T> struct CPData {
+    T Bm[3][3];    // Bm[a][i]  = d eps_a / du_{A,i}
+    T DBm[3][3];   // (t C Bm)[a][i]
+    T Bb[3][3];    // Bb[a][i]  = d kappa_a / du_{A,i}
+    T DBb[3][3];   // (t^3/12 C Bb)[a][i]
+    T Da3[3][3];   // Da3[i][k] = (d a3 / du_{A,i})_k
+    T Pv[3][3];    // Pv[i][k]  = (d ~a3 / du_{A,i})_k
+    T q[3], g[3], h[3];
+    T M, N1, N2;
+};
+
+template <int P> struct PairTable {
+    static constexpr int NB = (P + 1) * (P + 1);
+    static constexpr int NPAIR = NB * (NB + 1) / 2;
+    static constexpr int NPS = (NPAIR + 31) / 32;
+};
+
+__constant__ unsigned char c_pairA[4][325];
+__constant__ unsigned char c_pairB[4][325];
+
+// Gauss-point state shared by all lanes (computed redundantly per lane).
+template <class T> struct QPState {
+    V3T<T> a1, a2, x11, x22, x12, a3, v, w;
+    T l, il, il2, c;
+    T n[3], m[3];
+    T Cm[3][3], Cb[3][3];
+    T dV;
+};
+
+template <int P, class T>
+__device__ __forceinline__ void qp_state(const double* __restrict__ geo, const T du[15], T tm, T tb, QPState<T>& s) {
+    V3T<T> A1 = mk<T>(geo[0], geo[1], geo[2]), A2 = mk<T>(geo[3], geo[4], geo[5]);
+    V3T<T> X11 = mk<T>(geo[6], geo[7], geo[8]), X22 = mk<T>(geo[9], geo[10], geo[11]), X12 = mk<T>(geo[12], geo[13], geo[14]);
+    s.a1 = mk<T>(A1.x + du[0], A1.y + du[1], A1.z + du[2]);
+    s.a2 = mk<T>(A2.x + du[3], A2.y + du[4], A2.z + du[5]);
+    s.x11 = mk<T>(X11.x + du[6], X11.y + du[7], X11.z + du[8]);
+    s.x22 = mk<T>(X22.x + du[9], X22.y + du[10], X22.z + du[11]);
+    s.x12 = mk<T>(X12.x + du[12], X12.y + du[13], X12.z + du[14]);
+    V3T<T> At = cross3(A1, A2);
+    T J0 = sqrt(dot3(At, At));
+    V3T<T> A3 = mk<T>(At.x / J0, At.y / J0, At.z / J0);
+    V3T<T> at = cross3(s.a1, s.a2);
+    s.l = sqrt(dot3(at, at));
+    s.il = T(1) / s.l;
+    s.il2 = s.il * s.il;
+    s.a3 = mk<T>(at.x * s.il, at.y * s.il, at.z * s.il);
+    // membrane strain from displacement-gradient terms (avoids cancellation a.a - A.A)
+    V3T<T> d1 = mk<T>(du[0], du[1], du[2]), d2 = mk<T>(du[3], du[4], du[5]);
+    T e0 = dot3(A1, d1) + T(0.5) * dot3(d1, d1);
+    T e1 = dot3(A2, d2) + T(0.5) * dot3(d2, d2);
+    T e2 = dot3(A1, d2) + dot3(d1, A2) + dot3(d1, d2);
+    T k0 = dot3(X11, A3) - dot3(s.x11, s.a3);
+    T k1 = dot3(X22, A3) - dot3(s.x22, s.a3);
+    T k2 = T(2) * (dot3(X12, A3) - dot3(s.x12, s.a3));
+    T C00 = geo[15], C01 = geo[16], C02 = geo[17], C11 = geo[18], C12 = geo[19], C22 = geo[20];
+    T C[3][3] = {{C00, C01, C02}, {C01, C11, C12}, {C02, C12, C22}};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) { s.Cm[a][b] = tm * C[a][b]; s.Cb[a][b] = tb * C[a][b]; }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        s.n[a] = s.Cm[a][0] * e0 + s.Cm[a][1] * e1 + s.Cm[a][2] * e2;
+        s.m[a] = s.Cb[a][0] * k0 + s.Cb[a][1] * k1 + s.Cb[a][2] * k2;
+    }
+    s.v = mk<T>(s.m[0] * s.x11.x + s.m[1] * s.x22.x + T(2) * s.m[2] * s.x12.x,
+                s.m[0] * s.x11.y + s.m[1] * s.x22.y + T(2) * s.m[2] * s.x12.y,
+                s.m[0] * s.x11.z + s.m[1] * s.x22.z + T(2) * s.m[2] * s.x12.z);
+    s.c = dot3(s.v, s.a3);
+    s.w = mk<T>(s.v.x - s.c * s.a3.x, s.v.y - s.c * s.a3.y, s.v.z - s.c * s.a3.z);
+    s.dV = geo[21];
+}
+
+// First-variation data of one control point (basis derivatives N1,N2,N11,N22,N12).
+template <class T>
+__device__ __forceinline__ void cp_data(const QPState<T>& s, T N1, T N2, T N11, T N22, T N12, CPData<T>& o,
+                                        bool stiffness) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        V3T<T> ei = mk<T>(i == 0, i == 1, i == 2);
+        o.Bm[0][i] = N1 * comp(s.a1, i);
+        o.Bm[1][i] = N2 * comp(s.a2, i);
+        o.Bm[2][i] = N1 * comp(s.a2, i) + N2 * comp(s.a1, i);
+        V3T<T> c1 = cross3(ei, s.a2), c2 = cross3(s.a1, ei);
+        V3T<T> Pi = mk<T>(N1 * c1.x + N2 * c2.x, N1 * c1.y + N2 * c2.y, N1 * c1.z + N2 * c2.z);
+        T qi = dot3(s.a3, Pi);
+        V3T<T> Di = mk<T>((Pi.x - qi * s.a3.x) * s.il, (Pi.y - qi * s.a3.y) * s.il, (Pi.z - qi * s.a3.z) * s.il);
+        T a3i = comp(s.a3, i);
+        T db11 = N11 * a3i + dot3(s.x11, Di);
+        T db22 = N22 * a3i + dot3(s.x22, Di);
+        T db12 = N12 * a3i + dot3(s.x12, Di);
+        o.Bb[0][i] = -db11;
+        o.Bb[1][i] = -db22;
+        o.Bb[2][i] = T(-2) * db12;
+        if (stiffness) {
+            o.Pv[i][0] = Pi.x; o.Pv[i][1] = Pi.y; o.Pv[i][2] = Pi.z;
+            o.Da3[i][0] = Di.x; o.Da3[i][1] = Di.y; o.Da3[i][2] = Di.z;
+            o.q[i] = qi;
+            o.g[i] = dot3(s.v, Pi);
+            o.h[i] = T(3) * s.c * qi - o.g[i];
+        }
+    }
+    if (stiffness) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                o.DBm[a][i] = s.Cm[a][0] * o.Bm[0][i] + s.Cm[a][1] * o.Bm[1][i] + s.Cm[a][2] * o.Bm[2][i];
+                o.DBb[a][i] = s.Cb[a][0] * o.Bb[0][i] + s.Cb[a][1] * o.Bb[1][i] + s.Cb[a][2] * o.Bb[2][i];
+            }
+        o.M = s.m[0] * N11 + s.m[1] * N22 + T(2) * s.m[2] * N12;
+        o.N1 = N1;
+        o.N2 = N2;
+    }
+}
+
+template <int P, class T>
+__global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1, int ncp, int nq,
+                                                         const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                         const double* __restrict__ qpgeo,
+                                                         const double* __restrict__ ufull, double tmd, double tbd,
+                                                         T* __restrict__ elemK) {
+    constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
+    constexpr int NPS = PairTable<P>::NPS, NPAIR = PairTable<P>::NPAIR;
+    __shared__ CPData<T> sm[4][NB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    if (e >= nel) return;
+    const int e1 = e % m1, e2 = e / m1;
+    const int la = lane % NB1, lb = lane / NB1;
+    const bool own = lane < NB;
+    T ux = 0, uy = 0, uz = 0;
+    if (own) {
+        int A = (e2 + lb) * n1 + (e1 + la);
+        ux = (T)ufull[A]; uy = (T)ufull[ncp + A]; uz = (T)ufull[2 * ncp + A];
+    }
+    const T tm = (T)tmd, tb = (T)tbd;
+    T acc[NPS][9];
+#pragma unroll
+    for (int s = 0; s < NPS; ++s)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[s][k] = 0;
+    for (int q2 = 0; q2 < nq; ++q2)
+        for (int q1 = 0; q1 < nq; ++q1) {
+            T N1 = 0, N2 = 0, N11 = 0, N22 = 0, N12 = 0;
+            if (own) {
+                const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
+                const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
+                T f0 = (T)t1[la], f1 = (T)t1[NB1 + la], f2 = (T)t1[2 * NB1 + la];
+                T g0 = (T)t2[lb], g1 = (T)t2[NB1 + lb], g2 = (T)t2[2 * NB1 + lb];
+                N1 = f1 * g0; N2 = f0 * g1; N11 = f2 * g0; N22 = f0 * g2; N12 = f1 * g1;
+            }
+            T du[15] = {N1 * ux, N1 * uy, N1 * uz, N2 * ux, N2 * uy, N2 * uz, N11 * ux, N11 * uy, N11 * uz,
+                        N22 * ux, N22 * uy, N22 * uz, N12 * ux, N12 * uy, N12 * uz};
+#pragma unroll
+            for (int k = 0; k < 15; ++k) du[k] = warp_sum(du[k]);
+            const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * 22;
+            QPState<T> st;
+            qp_state<P, T>(geo, du, tm, tb, st);
+            if (own) cp_data<T>(st, N1, N2, N11, N22, N12, sm[warp][lane], true);
+            __syncwarp();
+            const T dV = st.dV;
+#pragma unroll
+            for (int s = 0; s < NPS; ++s) {
+                int pi = lane + 32 * s;
+                if (pi >= NPAIR) break;
+                const CPData<T>& A = sm[warp][c_pairA[P - 1][pi]];
+                const CPData<T>& B = sm[warp][c_pairB[P - 1][pi]];
+                T Sm = st.n[0] * A.N1 * B.N1 + st.n[1] * A.N2 * B.N2 + st.n[2] * (A.N1 * B.N2 + A.N2 * B.N1);
+                T cr = (A.N1 * B.N2 - A.N2 * B.N1) * st.il;
+                T wv[3] = {st.w.x, st.w.y, st.w.z};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        T k = A.DBm[0][i] * B.Bm[0][j] + A.DBm[1][i] * B.Bm[1][j] + A.DBm[2][i] * B.Bm[2][j] +
+                              A.DBb[0][i] * B.Bb[0][j] + A.DBb[1][i] * B.Bb[1][j] + A.DBb[2][i] * B.Bb[2][j];
+                        if (i == j) k += Sm;
+                        T pp = A.Pv[i][0] * B.Pv[j][0] + A.Pv[i][1] * B.Pv[j][1] + A.Pv[i][2] * B.Pv[j][2];
+                        T gb = A.M * B.Da3[j][i] + B.M * A.Da3[i][j] +
+                               st.il2 * (A.q[i] * B.h[j] - A.g[i] * B.q[j] - st.c * pp);
+                        // e_ijk w_k
+                        if (i != j) {
+                            int kk = 3 - i - j;
+                            T sgn = ((j - i + 3) % 3 == 1) ? T(1) : T(-1);
+                            gb += cr * sgn * wv[kk];
+                        }
+                        acc[s][3 * i + j] += (k - gb) * dV;
+                    }
+            }
+            __syncwarp();
+        }
+    T* Ke = elemK + (size_t)e * D * D;
+#pragma unroll
+    for (int s = 0; s < NPS; ++s) {
+        int pi = lane + 32 * s;
+        if (pi >= NPAIR) break;
+        int a = c_pairA[P - 1][pi], b = c_pairB[P - 1][pi];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                Ke[(size_t)(3 * a + i) * D + 3 * b + j] = acc[s][3 * i + j];
+                if (a != b) Ke[(size_t)(3 * b + j) * D + 3 * a + i] = acc[s][3 * i + j];
+            }
+    }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, int ncp, int nq,
+                                                      const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                      const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                                      double tm, double tb, double* __restrict__ elemR) {
+    constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    if (e >= nel) return;
+    const int e1 = e % m1, e2 = e / m1;
+    const int la = lane % NB1, lb = lane / NB1;
+    const bool own = lane < NB;
+    double ux = 0, uy = 0, uz = 0;
+    if (own) {
+        int A = (e2 + lb) * n1 + (e1 + la);
+        ux = ufull[A]; uy = ufull[ncp + A]; uz = ufull[2 * ncp + A];
+    }
+    double f[3] = {0, 0, 0};
+    for (int q2 = 0; q2 < nq; ++q2)
+        for (int q1 = 0; q1 < nq; ++q1) {
+            double N1 = 0, N2 = 0, N11 = 0, N22 = 0, N12 = 0;
+            if (own) {
+                const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
+                const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
+                N1 = t1[NB1 + la] * t2[lb]; N2 = t1[la] * t2[NB1 + lb];
+                N11 = t1[2 * NB1 + la] * t2[lb]; N22 = t1[la] * t2[2 * NB1 + lb]; N12 = t1[NB1 + la] * t2[NB1 + lb];
+            }
+            double du[15] = {N1 * ux, N1 * uy, N1 * uz, N2 * ux, N2 * uy, N2 * uz, N11 * ux, N11 * uy, N11 * uz,
+                             N22 * ux, N22 * uy, N22 * uz, N12 * ux, N12 * uy, N12 * uz};
+#pragma unroll
+            for (int k = 0; k < 15; ++k) du[k] = warp_sum(du[k]);
+            const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * 22;
+            QPState<double> st;
+            qp_state<P, double>(geo, du, tm, tb, st);
+            if (own) {
+                CPData<double> o;
+                cp_data<double>(st, N1, N2, N11, N22, N12, o, false);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    f[i] += (st.n[0] * o.Bm[0][i] + st.n[1] * o.Bm[1][i] + st.n[2] * o.Bm[2][i] +
+                             st.m[0] * o.Bb[0][i] + st.m[1] * o.Bb[1][i] + st.m[2] * o.Bb[2][i]) * st.dV;
+            }
+        }
+    if (own)
+        for (int i = 0; i < 3; ++i) elemR[(size_t)e * D + 3 * lane + i] = f[i];
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) kl_mass_kernel(int nel, int m1, int nq, const double* __restrict__ tab1,
+                                                      const double* __restrict__ tab2, const double* __restrict__ qpgeo,
+                                                      double rhot, double* __restrict__ elemK) {
+    constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
+    constexpr int NPS = PairTable<P>::NPS, NPAIR = PairTable<P>::NPAIR;
+    __shared__ double Ns[4][NB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    if (e >= nel) return;
+    const int e1 = e % m1, e2 = e / m1;
+    double acc[NPS];
+    for (int s = 0; s < NPS; ++s) acc[s] = 0;
+    for (int q2 = 0; q2 < nq; ++q2)
+        for (int q1 = 0; q1 < nq; ++q1) {
+            if (lane < NB) {
+                const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
+                const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
+                Ns[warp][lane] = t1[lane % NB1] * t2[lane / NB1];
+            }
+            __syncwarp();
+            double dV = qpgeo[((size_t)e * nq * nq + q2 * nq + q1) * 22 + 21];
+            for (int s = 0; s < NPS; ++s) {
+                int pi = lane + 32 * s;
+                if (pi < NPAIR) acc[s] += rhot * Ns[warp][c_pairA[P - 1][pi]] * Ns[warp][c_pairB[P - 1][pi]] * dV;
+            }
+            __syncwarp();
+        }
+    double* Ke = elemK + (size_t)e * D * D;
+    for (int s = 0; s < NPS; ++s) {
+        int pi = lane + 32 * s;
+        if (pi >= NPAIR) break;
+        int a = c_pairA[P - 1][pi], b = c_pairB[P - 1][pi];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double v = (i == j) ? acc[s] : 0.0;
+                Ke[(size_t)(3 * a + i) * D + 3 * b + j] = v;
+                Ke[(size_t)(3 * b + j) * D + 3 * a + i] = v;
+            }
+    }
+}
+
+// CSR gather: every nonzero (row R, col C) sums the element entries of the elements that
+// contain both control points (tensor-product structure: element e covers points e..e+p).
+template <class TE, class TV>
+__global__ void csr_gather_kernel(int nfree, int64_t nnz, int p, int n1, int m1, int m2, int ncp,
+                                  const int* __restrict__ rowptr, const int* __restrict__ cols,
+                                  const int* __restrict__ int2full, const TE* __restrict__ elemK, TV* __restrict__ vals) {
+    int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (z >= nnz) return;
+    // row by binary search
+    int lo = 0, hi = nfree;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (rowptr[mid] <= z) lo = mid; else hi = mid;
+    }
+    int R = lo, C = cols[z];
+    int fr = int2full[R], fc = int2full[C];
+    int ci = fr / ncp, Ar = fr - ci * ncp, cj = fc / ncp, Ac = fc - cj * ncp;
+    int ir = Ar % n1, jr = Ar / n1, ic = Ac % n1, jc = Ac / n1;
+    int NB1 = p + 1, D = 3 * NB1 * NB1;
+    int e1lo = max(max(ir, ic) - p, 0), e1hi = min(min(ir, ic), m1 - 1);
+    int e2lo = max(max(jr, jc) - p, 0), e2hi = min(min(jr, jc), m2 - 1);
+    double s = 0.0;
+    for (int e2 = e2lo; e2 <= e2hi; ++e2)
+        for (int e1 = e1lo; e1 <= e1hi; ++e1) {
+            int la = (jr - e2) * NB1 + (ir - e1), lb = (jc - e2) * NB1 + (ic - e1);
+            s += (double)elemK[((size_t)(e2 * m1 + e1) * D + 3 * la + ci) * D + 3 * lb + cj];
+        }
+    vals[z] = (TV)s;
+}
+
+__global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int ncp, const int* __restrict__ int2full,
+                                  const double* __restrict__ elemR, double* __restrict__ out) {
+    int R = blockIdx.x * blockDim.x + threadIdx.x;
+    if (R >= nfree) return;
+    int fr = int2full[R];
+    int ci = fr / ncp, A = fr - ci * ncp;
+    int i = A % n1, j = A / n1;
+    int NB1 = p + 1, D = 3 * NB1 * NB1;
+    double s = 0.0;
+    for (int e2 = max(j - p, 0); e2 <= min(j, m2 - 1); ++e2)
+        for (int e1 = max(i - p, 0); e1 <= min(i, m1 - 1); ++e1) {
+            int la = (j - e2) * NB1 + (i - e1);
+            s += elemR[(size_t)(e2 * m1 + e1) * D + 3 * la + ci];
+        }
+    out[R] = s;
+}
+
+__global__ void scatter_free_kernel(int nfree, const int* __restrict__ int2full, const double* __restrict__ x,
+                                    double* __restrict__ ufull) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nfree) ufull[int2full[r]] = x[r];
+}
+
+__global__ void permute_kernel(int n, int nv, const int* __restrict__ map, const double* __restrict__ src,
+                               double* __restrict__ dst) {
+    // dst[map[i]] = src[i]
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int v = 0; v < nv; ++v) dst[(size_t)v * n + map[i]] = src[(size_t)v * n + i];
+}
+
+template <class TV>
+__global__ void spmv_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ cols,
+                            const TV* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
+    // one warp per row
+    int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0.0;
+    for (int k = rowptr[row] + lane; k < rowptr[row + 1]; k += 32) s += (double)vals[k] * x[cols[k]];
+    s = warp_sum(s);
+    if (lane == 0) y[row] = s;
+}
+
+bool g_pairs_ready = false;
+
+void init_pairs() {
+    if (g_pairs_ready) return;
+    unsigned char A[4][325] = {}, B[4][325] = {};
+    for (int P = 1; P <= 4; ++P) {
+        int nb = (P + 1) * (P + 1), k = 0;
+        for (int a = 0; a < nb; ++a)
+            for (int b = a; b < nb; ++b) { A[P - 1][k] = (unsigned char)a; B[P - 1][k] = (unsigned char)b; ++k; }
+    }
+    KL_CUDA(cudaMemcpyToSymbol(c_pairA, A, sizeof(A)));
+    KL_CUDA(cudaMemcpyToSymbol(c_pairB, B, sizeof(B)));
+    g_pairs_ready = true;
+}
+
+template <class T>
+void launch_tangent(Problem& P, T* elemK) {
+    init_pairs();
+    int grid = ceil_div(P.nel, 4);
+    double tm = P.t, tb = P.t * P.t * P.t / 12.0;
+    switch (P.p) {
+        case 2: kl_tangent_kernel<2, T><<<grid, 128, 0, P.stream>>>(P.nel, P.m1, P.n1, P.ncp, P.nq, P.d_tab1.get(), P.d_tab2.get(), P.d_qpgeo.get(), P.d_ufull.get(), tm, tb, elemK); break;
+        case 3: kl_tangent_kernel<3, T><<<grid, 128, 0, P.stream>>>(P.nel, P.m1, P.n1, P.ncp, P.nq, P.d_tab1.get(), P.d_tab2.get(), P.d_qpgeo.get(), P.d_ufull.get(), tm, tb, elemK); break;
+        default: throw std::invalid_argument("unsupported degree");
+    }
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void Problem::set_displacement(const double* d_x) {
+    scatter_free_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, d_int2full.get(), d_x, d_ufull.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::tangent_f32() {
+    int D = 3 * (p + 1) * (p + 1);
+    if (d_elemKf.size() < (size_t)nel * D * D) d_elemKf.alloc((size_t)nel * D * D);
+    if (d_vals32.size() < (size_t)nnz) d_vals32.alloc(nnz);
+    launch_tangent<float>(*this, d_elemKf.get());
+    csr_gather_kernel<float, float><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKf.get(), d_vals32.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::tangent_f64() {
+    int D = 3 * (p + 1) * (p + 1);
+    if (d_elemKd.size() < (size_t)nel * D * D) d_elemKd.alloc((size_t)nel * D * D);
+    if (d_vals64.size() < (size_t)nnz) d_vals64.alloc(nnz);
+    launch_tangent<double>(*this, d_elemKd.get());
+    csr_gather_kernel<double, double><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::mass_f64() {
+    init_pairs();
+    int D = 3 * (p + 1) * (p + 1);
+    if (d_elemKd.size() < (size_t)nel * D * D) d_elemKd.alloc((size_t)nel * D * D);
+    if (d_vals64.size() < (size_t)nnz) d_vals64.alloc(nnz);
+    int grid = ceil_div(nel, 4);
+    double rt = rho * t;
+    switch (p) {
+        case 2: kl_mass_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), rt, d_elemKd.get()); break;
+        case 3: kl_mass_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), rt, d_elemKd.get()); break;
+        default: throw std::invalid_argument("unsupported degree");
+    }
+    count_launch();
+    csr_gather_kernel<double, double><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::internal_force(double* d_out) {
+    int D = 3 * (p + 1) * (p + 1);
+    if (d_elemR.size() < (size_t)nel * D) d_elemR.alloc((size_t)nel * D);
+    int grid = ceil_div(nel, 4);
+    double tm = t, tb = t * t * t / 12.0;
+    switch (p) {
+        case 2: kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get()); break;
+        case 3: kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get()); break;
+        default: throw std::invalid_argument("unsupported degree");
+    }
+    count_launch();
+    vec_gather_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, p, n1, m1, m2, ncp, d_int2full.get(), d_elemR.get(), d_out);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::pub_to_int(const double* d_pub, double* d_int, int nv) {
+    permute_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, nv, d_pub2int.get(), d_pub, d_int);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::int_to_pub(const double* d_int, double* d_pub, int nv) {
+    permute_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, nv, d_int2pub.get(), d_int, d_pub);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void Problem::upload_pub(const double* h_pub, double* d_int, int nv) {
+    if (d_tmp_pub.size() < (size_t)nfree * nv) d_tmp_pub.alloc((size_t)nfree * nv);
+    KL_CUDA(cudaMemcpyAsync(d_tmp_pub.get(), h_pub, sizeof(double) * nfree * nv, cudaMemcpyHostToDevice, stream));
+    pub_to_int(d_tmp_pub.get(), d_int, nv);
+}
+
+void Problem::download_pub(const double* d_int, double* h_pub, int nv) {
+    if (d_tmp_pub.size() < (size_t)nfree * nv) d_tmp_pub.alloc((size_t)nfree * nv);
+    int_to_pub(d_int, d_tmp_pub.get(), nv);
+    KL_CUDA(cudaMemcpyAsync(h_pub, d_tmp_pub.get(), sizeof(double) * nfree * nv, cudaMemcpyDeviceToHost, stream));
+    KL_CUDA(cudaStreamSynchronize(stream));
+}
+
+void Problem::csr_to_host_pub(bool f64, int64_t* rowptr_out, int32_t* cols_out, double* vals_out) {
+    // download internal-order values, then re-index rows/cols to the public order on the host
+    std::vector<double> v(nnz);
+    if (f64) {
+        KL_CUDA(cudaMemcpyAsync(v.data(), d_vals64.get(), sizeof(double) * nnz, cudaMemcpyDeviceToHost, stream));
+        KL_CUDA(cudaStreamSynchronize(stream));
+    } else {
+        std::vector<float> vf(nnz);
+        KL_CUDA(cudaMemcpyAsync(vf.data(), d_vals32.get(), sizeof(float) * nnz, cudaMemcpyDeviceToHost, stream));
+        KL_CUDA(cudaStreamSynchronize(stream));
+        for (int64_t z = 0; z < nnz; ++z) v[z] = vf[z];
+    }
+    rowptr_out[0] = 0;
+    for (int pr = 0; pr < nfree; ++pr) {
+        int R = pub2int[pr];
+        rowptr_out[pr + 1] = rowptr_out[pr] + (rowptr[R + 1] - rowptr[R]);
+    }
+    std::vector<std::pair<int, double>> row;
+    for (int pr = 0; pr < nfree; ++pr) {
+        int R = pub2int[pr];
+        row.clear();
+        for (int z = rowptr[R]; z < rowptr[R + 1]; ++z) row.emplace_back(int2pub[cols[z]], v[z]);
+        std::sort(row.begin(), row.end());
+        int64_t o = rowptr_out[pr];
+        for (size_t k = 0; k < row.size(); ++k) { cols_out[o + k] = row[k].first; vals_out[o + k] = row[k].second; }
+    }
+}
+
+void spmv(const Problem& P, bool f64, const double* x, double* y) {
+    if ((f64 ? P.d_vals64.size() : P.d_vals32.size()) < (size_t)P.nnz)
+        throw std::logic_error("spmv: matrix values not assembled");
+    int grid = ceil_div((int64_t)P.nfree * 32, 256);
+    if (f64) spmv_kernel<double><<<grid, 256, 0, P.stream>>>(P.nfree, P.d_rowptr.get(), P.d_cols.get(), P.d_vals64.get(), x, y);
+    else spmv_kernel<float><<<grid, 256, 0, P.stream>>>(P.nfree, P.d_rowptr.get(), P.d_cols.get(), P.d_vals32.get(), x, y);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+}  // namespace klsa

@@ -1,0 +1,424 @@
+// capi.cu -- extern "C" entry points (include/klshell_gb300.h).  No exception crosses the ABI.
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+#include "../../include/klshell_gb300.h"
+#include "eigen.h"
+#include "linalg.h"
+#include "problem.h"
+#include "solvers.h"
+
+using namespace klsa;
+
+struct klsa_problem {
+    std::unique_ptr<Problem> P;
+    DevBuf<double> x, r, f;   // staging (internal order)
+};
+struct klsa_options {
+    Options o;
+};
+struct klsa_solver {
+    klsa_problem* prob;
+    std::unique_ptr<LinearSolver> S;
+    DevBuf<double> b, x;
+};
+struct klsa_static {
+    klsa_problem* prob;
+    std::unique_ptr<StaticNewtonGPU> N;
+};
+struct klsa_alm {
+    klsa_problem* prob;
+    std::unique_ptr<ALMGPU> A;
+    DevBuf<double> v;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const CudaError& e) {
+        g_err = e.what();
+        return KLSA_CUDA_ERROR;
+    } catch (const std::invalid_argument& e) {
+        g_err = e.what();
+        return KLSA_INVALID_ARGUMENT;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return KLSA_OTHER_ERROR;
+    } catch (...) {
+        g_err = "unknown error";
+        return KLSA_OTHER_ERROR;
+    }
+}
+
+void ensure(DevBuf<double>& b, size_t n) {
+    if (b.size() < n) b.alloc(n);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* klsa_last_error(void) { return g_err.c_str(); }
+uint64_t klsa_launch_count(void) { return (uint64_t)g_launch_count; }
+
+int klsa_problem_create(const klsa_patch_desc* desc, klsa_problem** out) {
+    if (!desc || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        auto h = new klsa_problem();
+        try {
+            h->P.reset(new Problem(*desc));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_problem_destroy(klsa_problem* prob) {
+    return guarded([&] {
+        delete prob;
+        return KLSA_SUCCESS;
+    });
+}
+
+int64_t klsa_problem_ndof(const klsa_problem* prob) { return prob ? prob->P->nfree : -1; }
+int64_t klsa_problem_nnz(const klsa_problem* prob) { return prob ? prob->P->nnz : -1; }
+
+int klsa_force(klsa_problem* prob, double* F) {
+    if (!prob || !F) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        prob->P->download_pub(prob->P->d_F.get(), F);
+        return KLSA_SUCCESS;
+    });
+}
+
+static int residual_impl(klsa_problem* prob, const double* x, double lambda, bool al, double* R) {
+    if (!prob || !x || !R) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *prob->P;
+        ensure(prob->x, P.nfree); ensure(prob->r, P.nfree); ensure(prob->f, P.nfree);
+        P.upload_pub(x, prob->x.get());
+        P.set_displacement(prob->x.get());
+        P.internal_force(prob->f.get());
+        if (al) vec::lincomb(1.0, prob->f.get(), -lambda, P.d_F.get(), prob->r.get(), P.nfree, P.stream);
+        else vec::lincomb(1.0, P.d_F.get(), -1.0, prob->f.get(), prob->r.get(), P.nfree, P.stream);
+        P.download_pub(prob->r.get(), R);
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_residual(klsa_problem* prob, const double* x, double* R) { return residual_impl(prob, x, 0.0, false, R); }
+int klsa_al_residual(klsa_problem* prob, const double* x, double lambda, double* R) {
+    return residual_impl(prob, x, lambda, true, R);
+}
+
+int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_t* rowptr, int32_t* cols,
+                      double* vals) {
+    if (!prob || !x || !rowptr || !cols || !vals) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *prob->P;
+        ensure(prob->x, P.nfree);
+        P.upload_pub(x, prob->x.get());
+        P.set_displacement(prob->x.get());
+        if (precision) P.tangent_f64(); else P.tangent_f32();
+        P.csr_to_host_pub(precision != 0, rowptr, cols, vals);
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals) {
+    if (!prob || !rowptr || !cols || !vals) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        prob->P->mass_f64();
+        prob->P->csr_to_host_pub(true, rowptr, cols, vals);
+        return KLSA_SUCCESS;
+    });
+}
+
+klsa_options* klsa_options_create(void) { return new klsa_options(); }
+void klsa_options_destroy(klsa_options* opt) { delete opt; }
+int klsa_options_set_real(klsa_options* opt, const char* key, double value) {
+    if (!opt || !key) return KLSA_INVALID_ARGUMENT;
+    opt->o.reals[key] = value;
+    opt->o.ints.erase(key);
+    return KLSA_SUCCESS;
+}
+int klsa_options_set_int(klsa_options* opt, const char* key, int64_t value) {
+    if (!opt || !key) return KLSA_INVALID_ARGUMENT;
+    opt->o.ints[key] = value;
+    opt->o.reals.erase(key);
+    return KLSA_SUCCESS;
+}
+int klsa_options_set_string(klsa_options* opt, const char* key, const char* value) {
+    if (!opt || !key || !value) return KLSA_INVALID_ARGUMENT;
+    opt->o.strs[key] = value;
+    return KLSA_SUCCESS;
+}
+
+int klsa_solver_create(klsa_problem* prob, const char* name, const klsa_options* opt, klsa_solver** out) {
+    if (!prob || !name || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Options o = opt ? opt->o : Options();
+        auto s = make_linear_solver(*prob->P, name, (int)o.integer("Refinement", 0), o.real("RefineTol", 1e-12),
+                                    (int)o.integer("CGMaxIterations", 0), o.real("CGTolerance", 1e-10));
+        if (!s) {
+            g_err = std::string("unknown solver name ") + name;
+            return KLSA_INVALID_ARGUMENT;
+        }
+        auto h = new klsa_solver();
+        h->prob = prob;
+        h->S = std::move(s);
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_solver_destroy(klsa_solver* s) {
+    return guarded([&] {
+        delete s;
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_solver_compute_jacobian(klsa_solver* s, const double* x) {
+    if (!s || !x) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *s->prob->P;
+        ensure(s->x, P.nfree);
+        P.upload_pub(x, s->x.get());
+        P.set_displacement(s->x.get());
+        return s->S->compute_tangent();
+    });
+}
+
+int klsa_solver_compute_linear(klsa_solver* s) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *s->prob->P;
+        ensure(s->x, P.nfree);
+        s->x.zero(P.stream);
+        P.set_displacement(s->x.get());
+        return s->S->compute_tangent();
+    });
+}
+
+int klsa_solver_solve(klsa_solver* s, const double* b, double* x, int nrhs) {
+    if (!s || !b || !x || nrhs < 1 || nrhs > MF_MAX_RHS) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *s->prob->P;
+        ensure(s->b, (size_t)P.nfree * nrhs);
+        ensure(s->x, (size_t)P.nfree * nrhs);
+        P.upload_pub(b, s->b.get(), nrhs);
+        int st = s->S->solve(s->b.get(), s->x.get(), nrhs);
+        if (st != KLSA_SUCCESS) return st;
+        P.download_pub(s->x.get(), x, nrhs);
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_solver_stability(klsa_solver* s, double* min_d, int64_t* negatives) {
+    if (!s || !min_d || !negatives) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!s->S->has_ldlt()) {
+            g_err = "determinant stability needs the LDL^T solver";
+            return KLSA_SOLVER_ERROR;
+        }
+        s->S->stability(min_d, negatives);
+        return KLSA_SUCCESS;
+    });
+}
+
+// ---- static Newton ------------------------------------------------------------------------
+int klsa_static_create(klsa_problem* prob, const klsa_options* opt, klsa_static** out) {
+    if (!prob || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        auto h = new klsa_static();
+        h->prob = prob;
+        try {
+            h->N.reset(new StaticNewtonGPU(*prob->P, opt ? opt->o : Options()));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_static_destroy(klsa_static* s) {
+    return guarded([&] {
+        delete s;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_static_solve(klsa_static* s) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return s->N->solve(); });
+}
+int klsa_static_solve_linear(klsa_static* s) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return s->N->solve_linear(); });
+}
+int klsa_static_set_load_factor(klsa_static* s, double lambda) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    s->N->set_load(lambda);
+    return KLSA_SUCCESS;
+}
+int klsa_static_set_displacement(klsa_static* s, const double* U) {
+    if (!s || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *s->prob->P;
+        ensure(s->prob->x, P.nfree);
+        P.upload_pub(U, s->prob->x.get());
+        s->N->set_displacement(s->prob->x.get());
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_static_solution(klsa_static* s, double* U) {
+    if (!s || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        s->prob->P->download_pub(s->N->solution(), U);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_static_iterations(klsa_static* s) { return s ? s->N->iterations() : -1; }
+
+// ---- arc-length -----------------------------------------------------------------------------
+int klsa_alm_create(klsa_problem* prob, const char* method, const klsa_options* opt, klsa_alm** out) {
+    if (!prob || !method || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ALMGPU::Method m;
+        std::string s(method);
+        if (s == "Crisfield") m = ALMGPU::Crisfield;
+        else if (s == "Riks") m = ALMGPU::Riks;
+        else if (s == "LoadControl") m = ALMGPU::LoadControl;
+        else {
+            g_err = "unknown arc-length method " + s;
+            return KLSA_INVALID_ARGUMENT;
+        }
+        auto h = new klsa_alm();
+        h->prob = prob;
+        try {
+            h->A.reset(new ALMGPU(*prob->P, m, opt ? opt->o : Options()));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_destroy(klsa_alm* a) {
+    return guarded([&] {
+        delete a;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_initialize(klsa_alm* a) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        a->A->initialize();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_step(klsa_alm* a) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return a->A->step(); });
+}
+int klsa_alm_set_length(klsa_alm* a, double length) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    a->A->set_length(length);
+    return KLSA_SUCCESS;
+}
+int klsa_alm_reduce_length(klsa_alm* a, double factor) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    a->A->reduce_length(factor);
+    return KLSA_SUCCESS;
+}
+double klsa_alm_get_length(klsa_alm* a) { return a ? a->A->length() : -1.0; }
+int klsa_alm_set_solution(klsa_alm* a, const double* U, double L) {
+    if (!a || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->v, P.nfree);
+        P.upload_pub(U, a->v.get());
+        a->A->set_solution(a->v.get(), L);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_set_solution_step(klsa_alm* a, const double* DU, double DL) {
+    if (!a || !DU) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->v, P.nfree);
+        P.upload_pub(DU, a->v.get());
+        a->A->set_solution_step(a->v.get(), DL);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_set_initial_guess(klsa_alm* a, const double* U, double L) {
+    if (!a || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->v, P.nfree);
+        P.upload_pub(U, a->v.get());
+        a->A->set_initial_guess(a->v.get(), L);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_solution(klsa_alm* a, double* U, double* L) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (U) a->prob->P->download_pub(a->A->U(), U);
+        if (L) *L = a->A->L();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_info(klsa_alm* a, double* out) {
+    if (!a || !out) return KLSA_INVALID_ARGUMENT;
+    out[0] = a->A->iterations();
+    out[1] = a->A->residueF();
+    out[2] = a->A->residueU();
+    out[3] = a->A->phi();
+    out[4] = a->A->converged() ? 1.0 : 0.0;
+    out[5] = a->A->Lprev();
+    out[6] = a->A->DLold();
+    out[7] = a->A->n_jac;
+    out[8] = a->A->n_res;
+    out[9] = a->A->n_solve;
+    return KLSA_SUCCESS;
+}
+int klsa_alm_history(klsa_alm* a, double* Uprev, double* Lprev, double* DUold, double* DLold) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (Uprev) a->prob->P->download_pub(a->A->Uprev(), Uprev);
+        if (DUold) a->prob->P->download_pub(a->A->DUold(), DUold);
+        if (Lprev) *Lprev = a->A->Lprev();
+        if (DLold) *DLold = a->A->DLold();
+        return KLSA_SUCCESS;
+    });
+}
+
+// ---- eigen problems ---------------------------------------------------------------------------
+int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double scaling,
+                  double* values, double* vectors) {
+    if (!prob || !values || nev < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        return buckling_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, scaling, values, vectors);
+    });
+}
+
+int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values, double* vectors) {
+    if (!prob || !values || nev < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return modal_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, values, vectors); });
+}
+
+}  // extern "C"

@@ -1,0 +1,64 @@
+// linalg.h -- named linear solvers behind the reference's "Solver" option.
+#pragma once
+
+#include <memory>
+#include <string>
+
+#include "problem.h"
+
+namespace klsa {
+
+// compute()/solve() of gsSparseSolver<T> (gsStaticSolvers/gsStaticNewton.hpp:215-240,
+// gsALMSolvers/gsALMBase.hpp:186-211).  Vectors: FP64, internal order, device pointers.
+class LinearSolver {
+public:
+    virtual ~LinearSolver() = default;
+    // assemble K at the problem's current displacement and factorise / set up
+    virtual int compute_tangent() = 0;
+    virtual int solve(const double* d_b, double* d_x, int nrhs) = 0;
+    virtual bool has_ldlt() const { return false; }
+    virtual void stability(double* min_d, int64_t* neg) { *min_d = 0; *neg = 0; }
+    virtual int last_iterations() const { return 0; }
+};
+
+class MFSolver : public LinearSolver {
+public:
+    MFSolver(Problem& P, int refine, double refine_tol);
+    int compute_tangent() override;
+    int factor_current(bool f64_for_refine);
+    int solve(const double* d_b, double* d_x, int nrhs) override;
+    bool has_ldlt() const override { return true; }
+    void stability(double* min_d, int64_t* neg) override;
+    int last_iterations() const override { return last_refine_its_; }
+    void set_refine(int r) { refine_ = r; }
+
+private:
+    void solve_raw(const double* d_b, double* d_x, int nrhs);
+    Problem& P_;
+    int refine_;
+    double tol_;
+    bool has64_ = false;
+    int last_refine_its_ = 0;
+    DevBuf<float> b32_, x32_;
+    DevBuf<double> r_, dx_;
+};
+
+class PCGSolver : public LinearSolver {
+public:
+    PCGSolver(Problem& P, int max_it, double tol);
+    int compute_tangent() override;
+    int solve(const double* d_b, double* d_x, int nrhs) override;
+    int last_iterations() const override { return iterations_; }
+
+private:
+    Problem& P_;
+    int max_it_;
+    double tol_;
+    int iterations_ = 0;
+    DevBuf<double> dinv_, r_, z_, p_, q_;
+};
+
+std::unique_ptr<LinearSolver> make_linear_solver(Problem& P, const std::string& name, int refine, double refine_tol,
+                                                 int cg_max_it, double cg_tol);
+
+}  // namespace klsa

@@ -1,0 +1,76 @@
+// multifrontal.h -- nested-dissection multifrontal LDL^T on the device (FP32 fronts).
+//
+// Stands in for the sparse factorisation behind the reference's "SimplicialLDLT" solver name
+// (Eigen SimplicialLDLT via gsSparseSolver<T>::get, gsStaticSolvers/gsStaticBase.h:85,
+// gsALMSolvers/gsALMBase.hpp:73-78): an LDL^T without pivoting, so it factorises the
+// indefinite tangents met past limit points, and its D gives the determinant stability
+// indicator (gsStaticBase.h:162-179).
+//
+// Layout in HBM: one pool of dense column-major fronts (f x f, ld = f, lower triangle used),
+// per-node inverse diagonal tiles (64x64), per-node panel workspace W = L*D (f x 64), per-node
+// solve update vectors.  Work lists per (level, tile step, phase) are built once on the host.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+#include "nd_symbolic.h"
+
+namespace klsa {
+
+constexpr int MF_NB = 64;          // tile size
+constexpr int MF_MAX_RHS = 4;
+
+struct MFWork {
+    int4* items = nullptr;   // device pointer into the item pool
+    int count = 0;
+};
+
+class Multifrontal {
+public:
+    // csr (internal order): rowptr/cols on the host, used to build the front scatter map
+    Multifrontal(const NDTree& tree, const std::vector<int>& rowptr, const std::vector<int>& cols,
+                 cudaStream_t stream);
+    ~Multifrontal() = default;
+
+    // Numeric factorisation of the FP32 CSR values (internal order, same pattern).
+    // Returns ST_SUCCESS or ST_SOLVER_ERROR (zero / non-finite pivot).
+    int factorize(const float* d_vals, bool check_status = true);
+    // Enqueue the factorisation without the status read-back (status stays on the device).
+    void factorize_async(const float* d_vals);
+    int read_status();
+    // x = (L D L^T)^-1 b for nrhs columns (ld = n), FP32 in/out, internal order, device pointers.
+    void solve(const float* d_b, float* d_x, int nrhs);
+    // min(D) and #negatives of D (after factorize)
+    void stability(double* min_d, int64_t* negatives);
+
+    int n() const { return n_; }
+    double flops() const { return flops_; }
+    int64_t front_bytes() const { return (int64_t)pool_.size() * 4; }
+    const std::vector<int>& level_nodes(int lvl) const { return level_nodes_[lvl]; }
+
+private:
+    cudaStream_t stream_;
+    int n_ = 0, nnodes_ = 0, nlevels_ = 0;
+    double flops_ = 0;
+    // per-node device metadata
+    DevBuf<int> d_f_, d_k_, d_own_, d_parent_;
+    DevBuf<int64_t> d_front_off_, d_linv_off_, d_ws_off_, d_upd_off_, d_halo_off_, d_map_off_;
+    DevBuf<int> d_child0_, d_child1_;
+    DevBuf<int> d_halo_, d_map_;
+    DevBuf<int64_t> d_fpos_;     // CSR nz -> pool position (lower entries) or -1
+    int64_t nnz_ = 0;
+    DevBuf<float> pool_, linv_, ws_, upd_, D_;
+    DevBuf<float> y_;            // forward-solve intermediate (n x MF_MAX_RHS)
+    DevBuf<int> status_;
+    DevBuf<int4> items_;
+    struct Step { MFWork diag, panel, update; int t; };
+    struct Level { MFWork ea[2]; std::vector<Step> steps; MFWork nodes; int max_f = 0; };
+    std::vector<Level> levels_;
+    std::vector<std::vector<int>> level_nodes_;
+    int max_f_ = 0;
+};
+
+}  // namespace klsa

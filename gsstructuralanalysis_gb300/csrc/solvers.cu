@@ -1,0 +1,553 @@
+// solvers.cu -- gsStaticNewton / gsALMCrisfield / gsALMRiks / gsALMLoadControl on the device.
+#include "solvers.h"
+
+#include <cmath>
+#include <stdexcept>
+
+namespace klsa {
+
+namespace {
+
+struct Fail {
+    int code;
+};
+
+inline double sgn(double x) { return (double)((x > 0) - (x < 0)); }
+
+std::unique_ptr<LinearSolver> solver_from_options(Problem& P, const Options& opt, const std::string& def) {
+    std::string name = opt.str("Solver", def);
+    auto s = make_linear_solver(P, name, (int)opt.integer("Refinement", 0), opt.real("RefineTol", 1e-12),
+                                (int)opt.integer("CGMaxIterations", 0), opt.real("CGTolerance", 1e-10));
+    if (!s) throw std::invalid_argument("unknown Solver '" + name + "'");
+    return s;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// gsStaticNewton
+// ------------------------------------------------------------------------------------------
+StaticNewtonGPU::StaticNewtonGPU(Problem& P, const Options& opt) : P_(P), opt_(opt) {
+    // gsStaticNewton::defaultOptions sets Solver = CGDiagonal (gsStaticNewton.hpp:23)
+    S_ = solver_from_options(P_, opt_, "CGDiagonal");
+    int n = P_.nfree;
+    U_.alloc(n); DU_.alloc(n); dU_.alloc(n); R_.alloc(n); x_.alloc(n); fint_.alloc(n);
+    U_.zero(P_.stream); DU_.zero(P_.stream); dU_.zero(P_.stream);
+}
+
+void StaticNewtonGPU::residual(const double* d_x, double* d_R) {
+    P_.set_displacement(d_x);
+    P_.internal_force(fint_.get());
+    vec::lincomb(L_, P_.d_F.get(), -1.0, fint_.get(), d_R, P_.nfree, P_.stream);
+}
+
+int StaticNewtonGPU::solve_linear() {
+    KL_CUDA(cudaMemsetAsync(x_.get(), 0, sizeof(double) * P_.nfree, P_.stream));
+    P_.set_displacement(x_.get());
+    int st = S_->compute_tangent();
+    if (st != ST_SUCCESS) return ST_SOLVER_ERROR;
+    vec::lincomb(L_, P_.d_F.get(), 0.0, P_.d_F.get(), R_.get(), P_.nfree, P_.stream);
+    return S_->solve(R_.get(), U_.get(), 1) == ST_SUCCESS ? ST_SUCCESS : ST_SOLVER_ERROR;
+}
+
+void StaticNewtonGPU::set_displacement(const double* d_U) {
+    KL_CUDA(cudaMemcpyAsync(U_.get(), d_U, sizeof(double) * P_.nfree, cudaMemcpyDeviceToDevice, P_.stream));
+}
+
+void StaticNewtonGPU::set_update(const double* d_DU) {
+    KL_CUDA(cudaMemcpyAsync(DU_.get(), d_DU, sizeof(double) * P_.nfree, cudaMemcpyDeviceToDevice, P_.stream));
+    headstart_ = true;
+    has_DU_ = true;
+}
+
+int StaticNewtonGPU::solve_nonlinear_impl() {
+    const int n = P_.nfree;
+    cudaStream_t s = P_.stream;
+    double tol = opt_.real("tol", 1e-6);
+    double tolF = opt_.real("tolF", -1) != -1 ? opt_.real("tolF", -1) : tol;
+    double tolU = opt_.real("tolU", -1) != -1 ? opt_.real("tolU", -1) : tol;
+    int maxIt = (int)opt_.integer("maxIt", 25);
+    double relax = opt_.real("Relaxation", 1.0);
+    if (!has_DU_) {
+        // first call: linear solve as head start (gsStaticNewton.hpp:148-153)
+        DevBuf<double> Usave(n);
+        KL_CUDA(cudaMemcpyAsync(Usave.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        if (solve_linear() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        KL_CUDA(cudaMemcpyAsync(DU_.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        KL_CUDA(cudaMemcpyAsync(dU_.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        KL_CUDA(cudaMemsetAsync(U_.get(), 0, sizeof(double) * n, s));
+        headstart_ = true;
+        has_DU_ = true;
+    }
+    // _start (hpp:274-316)
+    if (!headstart_) {
+        KL_CUDA(cudaMemsetAsync(DU_.get(), 0, sizeof(double) * n, s));
+        residual(U_.get(), R_.get());
+        double rr;
+        const double* a[1] = {R_.get()};
+        vec::multidot(1, a, a, n, &rr, s);
+        residual_ = std::sqrt(rr);
+        if (residual_ == 0) residual_ = 1;
+        residualIni_ = residualOld_ = residual_;
+    } else {
+        vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n, s);
+        residual(x_.get(), R_.get());
+        double rr;
+        const double* a[1] = {R_.get()};
+        vec::multidot(1, a, a, n, &rr, s);
+        residual_ = std::sqrt(rr);
+        if (residual_ == 0) residual_ = 1;
+        residualOld_ = residual_;
+        DevBuf<double> R0(n);
+        residual(U_.get(), R0.get());
+        const double* b[1] = {R0.get()};
+        vec::multidot(1, b, b, n, &rr, s);
+        residualIni_ = std::sqrt(rr);
+        if (residualIni_ == 0) residualIni_ = 1;
+        headstart_ = false;
+    }
+    KL_CUDA(cudaMemsetAsync(dU_.get(), 0, sizeof(double) * n, s));
+    for (num_it_ = 0; num_it_ != maxIt; ++num_it_) {
+        vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n, s);
+        P_.set_displacement(x_.get());
+        if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        if (S_->solve(R_.get(), dU_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        vec::axpby(relax, dU_.get(), 1.0, DU_.get(), n, s);
+        vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n, s);
+        residual(x_.get(), R_.get());
+        double d[3];
+        const double* xs[3] = {R_.get(), dU_.get(), DU_.get()};
+        vec::multidot(3, xs, xs, n, d, s);
+        residual_ = std::sqrt(d[0]);
+        residualOld_ = residual_;
+        double ratioU = relax * std::sqrt(d[1]) / std::sqrt(d[2]);
+        if (ratioU < tolU && residual_ / residualIni_ < tolF) {
+            vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n, s);
+            break;
+        } else if (num_it_ + 1 == maxIt) {
+            vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n, s);
+            throw Fail{ST_NOT_CONVERGED};
+        }
+    }
+    return ST_SUCCESS;
+}
+
+int StaticNewtonGPU::solve() {
+    try {
+        return solve_nonlinear_impl();
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// arc-length family
+// ------------------------------------------------------------------------------------------
+ALMGPU::ALMGPU(Problem& P, Method m, const Options& opt) : P_(P), method_(m), opt_(opt) {
+    // gsALMBase::defaultOptions: Solver = SimplicialLDLT (gsALMBase.hpp:48)
+    S_ = solver_from_options(P_, opt_, "SimplicialLDLT");
+    n_ = P_.nfree;
+    for (DevBuf<double>* b : {&U_, &DU_, &dU_, &dUt_, &dUbar_, &DUold_, &Uprev_, &Uguess_, &R_, &x_, &fint_, &tmp_}) {
+        b->alloc(n_);
+        b->zero(P_.stream);
+    }
+    rhs2_.alloc(2 * (size_t)n_);
+    sol2_.alloc(2 * (size_t)n_);
+    apply_options();
+    const double* f[1] = {P_.d_F.get()};
+    vec::multidot(1, f, f, n_, &FF_, P_.stream);
+}
+
+void ALMGPU::apply_options() {
+    maxIt_ = (int)opt_.integer("MaxIter", 100);
+    tolF_ = opt_.real("TolF", 1e-3);
+    tolU_ = opt_.real("TolU", 1e-6);
+    arcLength_ = arcLength_prev_ = arcLength_ori_ = opt_.real("Length", 1e-2);
+    adaptive_ = opt_.integer("AdaptiveLength", 0) != 0;
+    desiredIt_ = (int)opt_.integer("AdaptiveIterations", 10);
+    quasi_ = opt_.integer("Quasi", 0) != 0;
+    quasiInterval_ = (int)opt_.integer("QuasiIterations", -1);
+    relax_ = opt_.real("Relaxation", 1.0);
+    phi_ = opt_.real("Scaling", -1.0);
+    phi_user_ = phi_ != -1.0;
+    angle_ = (int)opt_.integer("AngleMethod", 0);
+}
+
+void ALMGPU::set_length(double l) {
+    opt_.reals["Length"] = l;
+    arcLength_ = arcLength_prev_ = arcLength_ori_ = l;
+}
+
+void ALMGPU::initialize() {
+    for (DevBuf<double>* b : {&U_, &DU_, &DUold_, &Uprev_}) b->zero(P_.stream);
+    L_ = DL_ = DLold_ = Lprev_ = 0.0;
+}
+
+void ALMGPU::set_solution(const double* d_U, double L) {
+    KL_CUDA(cudaMemcpyAsync(U_.get(), d_U, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+    L_ = L;
+}
+
+void ALMGPU::set_solution_step(const double* d_DU, double DL) {
+    KL_CUDA(cudaMemcpyAsync(DUold_.get(), d_DU, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+    DLold_ = DL;
+}
+
+void ALMGPU::set_initial_guess(const double* d_U, double L) {
+    KL_CUDA(cudaMemcpyAsync(Uguess_.get(), d_U, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+    Lguess_ = L;
+    has_guess_ = true;
+}
+
+void ALMGPU::compute_jacobian() {
+    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, P_.stream);
+    P_.set_displacement(x_.get());
+    ++n_jac;
+    if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    ut_valid_ = false;
+}
+
+void ALMGPU::compute_residual() {
+    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, P_.stream);
+    P_.set_displacement(x_.get());
+    P_.internal_force(fint_.get());
+    vec::lincomb(1.0, fint_.get(), -(L_ + DL_), P_.d_F.get(), R_.get(), n_, P_.stream);
+    ++n_res;
+}
+
+void ALMGPU::compute_residual_norms() {
+    double d[3];
+    const double* xs[3] = {R_.get(), dU_.get(), DU_.get()};
+    vec::multidot(3, xs, xs, n_, d, P_.stream);
+    double nR = std::sqrt(d[0]), ndU = std::sqrt(d[1]), nDU = std::sqrt(d[2]);
+    if (num_it_ == 0) {
+        basisF_ = std::fabs(L_ + DL_) * std::sqrt(FF_);
+        basisU_ = nDU;
+        residueF_ = nR / basisF_;
+        residueU_ = ndU / nDU;
+    } else {
+        residueF_ = nR / basisF_;
+        residueU_ = ndU / basisU_;
+    }
+}
+
+// one factorisation, two right-hand sides: [F, -R] -> [dUt, dUbar]
+void ALMGPU::solve_ut_ubar(bool need_ut) {
+    cudaStream_t s = P_.stream;
+    if (need_ut) {
+        KL_CUDA(cudaMemcpyAsync(rhs2_.get(), P_.d_F.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        vec::lincomb(-1.0, R_.get(), 0.0, R_.get(), rhs2_.get() + n_, n_, s);
+        if (S_->solve(rhs2_.get(), sol2_.get(), 2) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        KL_CUDA(cudaMemcpyAsync(dUt_.get(), sol2_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        KL_CUDA(cudaMemcpyAsync(dUbar_.get(), sol2_.get() + n_, sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        n_solve += 2;
+        ut_valid_ = true;
+    } else {
+        vec::lincomb(-1.0, R_.get(), 0.0, R_.get(), rhs2_.get(), n_, s);
+        if (S_->solve(rhs2_.get(), dUbar_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        n_solve += 1;
+    }
+}
+
+void ALMGPU::initiate_step() {
+    DU_.zero(P_.stream);
+    dU_.zero(P_.stream);
+    if (method_ == Crisfield) {
+        dUbar_.zero(P_.stream);
+        dUt_.zero(P_.stream);
+        eta_ = 1.0;
+    }
+    DL_ = dL_ = 0.0;
+}
+
+void ALMGPU::compute_lambda_mu() {
+    // gsALMCrisfield.hpp:384-398
+    double A0 = phi_ * phi_ * FF_;
+    double d[2];
+    const double* xs[2] = {DUold_.get(), dUt_.get()};
+    const double* ys[2] = {dUt_.get(), dUt_.get()};
+    vec::multidot(2, xs, ys, n_, d, P_.stream);
+    double dir = sgn(d[0] + A0 * DLold_);
+    double denum = std::sqrt(d[1] + A0);
+    double mu = denum == 0 ? arcLength_ : arcLength_ / denum;
+    dL_ = dir * mu;
+    vec::lincomb(dL_, dUt_.get(), 0.0, dUt_.get(), dU_.get(), n_, P_.stream);
+}
+
+void ALMGPU::predictor() {
+    cudaStream_t s = P_.stream;
+    compute_jacobian();
+    if (method_ == Crisfield) {
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        ut_valid_ = true;
+        double d[3];
+        const double* xs[3] = {DUold_.get(), dUt_.get(), U_.get()};
+        vec::multidot(3, xs, xs, n_, d, s);
+        if (d[0] == 0 && DLold_ * DLold_ == 0) {
+            dL_ = arcLength_ / std::sqrt(2 * d[1]);
+            vec::lincomb(1.0, dUbar_.get(), dL_, dUt_.get(), dU_.get(), n_, s);
+            if (!phi_user_) phi_ = std::sqrt(d[1] / FF_);
+        } else {
+            if (!phi_user_) phi_ = std::sqrt(d[2] / (L_ * L_ * FF_));
+            compute_lambda_mu();
+        }
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
+        if (angle_ == 1 || angle_ == 2) {
+            KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+            DLold_ = DL_;
+        }
+    } else if (method_ == Riks) {
+        phi_ = n_ == 1 ? 0.99999999999 : 1.0 / n_;
+        double d[1];
+        vec::lincomb(1.0, U_.get(), -1.0, Uprev_.get(), tmp_.get(), n_, s);
+        const double* xs[1] = {tmp_.get()};
+        vec::multidot(1, xs, xs, n_, d, s);
+        const double tol = 1e-10;
+        if (std::sqrt(d[0]) < tol && (L_ - Lprev_) * (L_ - Lprev_) < tol) {
+            double DLs = 1.0;
+            if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+            ++n_solve;
+            ut_valid_ = true;
+            double uu;
+            const double* a[1] = {dUt_.get()};
+            vec::multidot(1, a, a, n_, &uu, s);
+            double den = std::sqrt(uu + DL_ * DLs);
+            vec::lincomb(1.0 / den, dUt_.get(), 0.0, dUt_.get(), dU_.get(), n_, s);
+            dL_ = DLs / den;
+        } else {
+            dL_ = (L_ - Lprev_) / arcLength_prev_;
+            vec::lincomb(1.0 / arcLength_prev_, tmp_.get(), 0.0, tmp_.get(), dU_.get(), n_, s);
+        }
+        dL_ *= arcLength_;
+        vec::axpby(0.0, dU_.get(), arcLength_, dU_.get(), n_, s);
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
+    } else {  // LoadControl
+        DL_ = dL_ = arcLength_;
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        vec::lincomb(dL_, dUt_.get(), 0.0, dUt_.get(), DU_.get(), n_, s);
+    }
+}
+
+void ALMGPU::predictor_guess() {
+    cudaStream_t s = P_.stream;
+    compute_jacobian();
+    if (method_ == Crisfield) {
+        // gsALMCrisfield.hpp:167-191
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        ut_valid_ = true;
+        double uu;
+        const double* a[1] = {dUt_.get()};
+        vec::multidot(1, a, a, n_, &uu, s);
+        if (!phi_user_) phi_ = std::sqrt(uu / FF_);
+        vec::lincomb(-1.0, Uguess_.get(), 1.0, U_.get(), DUold_.get(), n_, s);
+        DLold_ = -(Lguess_ - L_);
+        compute_lambda_mu();
+        KL_CUDA(cudaMemcpyAsync(DU_.get(), dU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        DL_ = dL_;
+    } else if (method_ == Riks) {
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        ut_valid_ = true;
+        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, s);
+        double d;
+        const double* a[1] = {tmp_.get()};
+        vec::multidot(1, a, a, n_, &d, s);
+        const double tol = 1e-10;
+        if (std::sqrt(d) < tol && (Lguess_ - L_) * (Lguess_ - L_) < tol) {
+            double uu;
+            const double* b[1] = {dUt_.get()};
+            vec::multidot(1, b, b, n_, &uu, s);
+            double den = std::sqrt(uu + DL_);
+            vec::lincomb(1.0 / den, dUt_.get(), 0.0, dUt_.get(), dU_.get(), n_, s);
+            dL_ = 1.0 / den;
+        } else {
+            dL_ = (Lguess_ - L_) / arcLength_prev_;
+            vec::lincomb(1.0 / arcLength_prev_, tmp_.get(), 0.0, tmp_.get(), dU_.get(), n_, s);
+        }
+        dL_ *= arcLength_;
+        vec::axpby(0.0, dU_.get(), arcLength_, dU_.get(), n_, s);
+        KL_CUDA(cudaMemcpyAsync(DU_.get(), dU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        DL_ = dL_;
+    } else {
+        DL_ = dL_ = Lguess_ - L_;
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        vec::lincomb(dL_, dUt_.get(), 0.0, dUt_.get(), DU_.get(), n_, s);
+    }
+    has_guess_ = false;
+}
+
+void ALMGPU::quasi_newton_iteration() {
+    compute_jacobian();
+}
+
+void ALMGPU::lambdas_crisfield() {
+    // gsALMCrisfield.hpp:213-427 (computeLambdas, Simple, Modified, Eta, Complex, DOT)
+    cudaStream_t s = P_.stream;
+    double A0 = phi_ * phi_ * FF_;
+    double d[7];
+    const double* xs[7] = {dUt_.get(), dUt_.get(), dUbar_.get(), DU_.get(), DU_.get(), dUbar_.get(), DUold_.get()};
+    const double* ys[7] = {dUt_.get(), DU_.get(), dUt_.get(), DU_.get(), dUbar_.get(), dUbar_.get(), dUt_.get()};
+    vec::multidot(7, xs, ys, n_, d, s);
+    double a0 = d[0] + A0;
+    double b0 = 2 * (d[1] + DL_ * A0);
+    double b1 = 2 * d[2];
+    double c0 = d[3] + DL_ * DL_ * A0 - arcLength_ * arcLength_;
+    double c1 = 2 * d[4];
+    double c2 = d[5];
+    double DOTfac = d[6] + phi_ * phi_ * DLold_;
+    double al1 = a0, al2 = b0 + eta_ * b1, al3 = c0 + eta_ * c1 + eta_ * eta_ * c2;
+    double disc = al2 * al2 - 4 * al1 * al3;
+    auto choose = [&](double r0, double r1) {
+        double d0 = r0 * DOTfac, d1 = r1 * DOTfac;
+        double r = (d0 < d1) ? r1 : r0;
+        dL_ = r;
+        vec::lincomb(eta_, dUbar_.get(), r, dUt_.get(), dU_.get(), n_, s);
+    };
+    if (disc >= 0) {
+        eta_ = 1.0;
+        choose((-al2 + std::sqrt(disc)) / (2 * al1), (-al2 - std::sqrt(disc)) / (2 * al1));
+        return;
+    }
+    // modified (Lam 1992)
+    al1 = b1 * b1 - 4.0 * a0 * c2;
+    al2 = 2.0 * b0 * b1 - 4.0 * a0 * c1;
+    al3 = b0 * b0 - 4.0 * a0 * c0;
+    disc = al2 * al2 - 4.0 * al1 * al3;
+    if (disc >= 0) {
+        double e0 = (-al2 + std::sqrt(disc)) / (2.0 * al1), e1 = (-al2 - std::sqrt(disc)) / (2.0 * al1);
+        double eta1 = std::min(e0, e1), eta2 = std::max(e0, e1);
+        double xi = 0.05 * std::fabs(eta2 - eta1);
+        if (eta2 < 1.0) eta_ = eta2 - xi;
+        else if (eta2 > 1.0 && -al2 / al1 < 1.0) eta_ = eta2 + xi;
+        else if (eta1 < 1.0 && -al2 / al1 > 1.0) eta_ = eta1 - xi;
+        else if (eta1 > 1.0) eta_ = eta1 + xi;
+    }
+    if (disc >= 0 && eta_ > 0.05) {
+        double bl1 = a0, bl2 = b0 + eta_ * b1;
+        double r = -bl2 / (2 * bl1);
+        choose(r, r);
+        return;
+    }
+    // simplified complex-root solve (Lam 1992 eq. 13-17)
+    eta_ = 1.0;
+    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, s);
+    spmv(P_, false, x_.get(), tmp_.get());            // Fint ~ K (U + DU)
+    double fF;
+    const double* fa[1] = {tmp_.get()};
+    const double* fb[1] = {P_.d_F.get()};
+    vec::multidot(1, fa, fb, n_, &fF, s);
+    double Lcr = fF / FF_;
+    double DLcr = Lcr - L_;
+    double DUcr2 = d[3] + 2 * d[4] + d[5];              // (DU + dUbar).(DU + dUbar)
+    double arc_cr = std::sqrt(DUcr2 + A0 * DLcr * DLcr);
+    double mu = arcLength_ / arc_cr;
+    dL_ = mu * DLcr - DL_;
+    // dU = mu (DU + dUbar) - DU
+    vec::lincomb(mu - 1.0, DU_.get(), mu, dUbar_.get(), dU_.get(), n_, s);
+}
+
+void ALMGPU::iteration() {
+    cudaStream_t s = P_.stream;
+    if (method_ == Crisfield) {
+        solve_ut_ubar(!ut_valid_);
+        eta_ = 1.0;
+        double lamold = dL_;
+        lambdas_crisfield();
+        if ((lamold * dL_ < 0 && std::fabs(dL_) <= std::fabs(lamold)) && relax_ != 1.0) {
+            vec::lincomb(relax_ * dL_, dUt_.get(), relax_ * eta_, dUbar_.get(), dU_.get(), n_, s);
+            dL_ = relax_ * dL_;
+        }
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
+        if (angle_ == 1) {
+            KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+            DLold_ = DL_;
+        }
+    } else if (method_ == Riks) {
+        solve_ut_ubar(!ut_valid_);
+        double d[3];
+        const double* xs[3] = {DU_.get(), DU_.get(), DU_.get()};
+        const double* ys[3] = {DU_.get(), dUbar_.get(), dUt_.get()};
+        vec::multidot(3, xs, ys, n_, d, s);
+        double r = phi_ * d[0] + (1 - phi_) * DL_ * DL_ - arcLength_ * arcLength_;
+        dL_ = -(r + 2 * phi_ * d[1]) / (2 * (1 - phi_) * DL_ + 2 * phi_ * d[2]);
+        vec::lincomb(1.0, dUbar_.get(), dL_, dUt_.get(), dU_.get(), n_, s);
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
+    } else {
+        solve_ut_ubar(false);
+        KL_CUDA(cudaMemcpyAsync(dU_.get(), dUbar_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+    }
+}
+
+void ALMGPU::iteration_finish() {
+    cudaStream_t s = P_.stream;
+    converged_ = true;
+    KL_CUDA(cudaMemcpyAsync(Uprev_.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    Lprev_ = L_;
+    vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
+    L_ += DL_;
+    if (method_ == Crisfield && angle_ == 0) {
+        KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        DLold_ = DL_;
+    }
+}
+
+void ALMGPU::step_impl() {
+    converged_ = false;
+    num_it_ = 0;
+    initiate_step();
+    bool use_guess = false;
+    if (has_guess_) {
+        double d;
+        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, P_.stream);
+        const double* a[1] = {tmp_.get()};
+        vec::multidot(1, a, a, n_, &d, P_.stream);
+        use_guess = d != 0 && (Lguess_ - L_) != 0;
+    }
+    if (use_guess) predictor_guess();
+    else predictor();
+    compute_residual();
+    compute_residual_norms();
+    if (quasi_ && !ut_valid_) {
+        // quasiNewtonPredictor: keep the predictor's tangent
+    }
+    for (num_it_ = 1; num_it_ < maxIt_; ++num_it_) {
+        if (!quasi_ || (quasiInterval_ > 0 && num_it_ % quasiInterval_ == 0)) quasi_newton_iteration();
+        iteration();
+        compute_residual();
+        compute_residual_norms();
+        if (residueF_ < tolF_ && residueU_ < tolU_) {
+            iteration_finish();
+            if (adaptive_) {
+                double fac = (double)desiredIt_ / num_it_;
+                fac = std::min(std::max(fac, 0.5), 2.0);
+                arcLength_prev_ = arcLength_;
+                arcLength_ = arcLength_ * fac;
+            } else {
+                arcLength_prev_ = arcLength_;
+            }
+            return;
+        } else if (num_it_ == maxIt_ - 1) {
+            throw Fail{ST_NOT_CONVERGED};
+        }
+    }
+}
+
+int ALMGPU::step() {
+    try {
+        step_impl();
+        return ST_SUCCESS;
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+}  // namespace klsa

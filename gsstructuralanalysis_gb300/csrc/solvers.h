@@ -1,0 +1,142 @@
+// solvers.h -- device-resident mirrors of gsStaticNewton and the gsALM* arc-length family.
+//
+// The solver logic (iteration structure, convergence tests, option keys and defaults, the
+// Crisfield root selection and complex-root fall-backs) follows the reference classes; the
+// vectors live in HBM (FP64, internal order) and the scalars that steer the iteration are
+// reduced to the host once per iteration.  The K(u)/R(u) callbacks are the built-in device
+// assembler of the problem, and the linear solver is chosen by the "Solver" option.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <string>
+
+#include "linalg.h"
+#include "problem.h"
+
+namespace klsa {
+
+struct Options {
+    std::map<std::string, double> reals;
+    std::map<std::string, int64_t> ints;
+    std::map<std::string, std::string> strs;
+    double real(const std::string& k, double def) const {
+        auto it = reals.find(k);
+        if (it != reals.end()) return it->second;
+        auto jt = ints.find(k);
+        return jt != ints.end() ? (double)jt->second : def;
+    }
+    int64_t integer(const std::string& k, int64_t def) const {
+        auto it = ints.find(k);
+        if (it != ints.end()) return it->second;
+        auto jt = reals.find(k);
+        return jt != reals.end() ? (int64_t)jt->second : def;
+    }
+    std::string str(const std::string& k, const std::string& def) const {
+        auto it = strs.find(k);
+        return it != strs.end() ? it->second : def;
+    }
+};
+
+// gsStaticNewton (gsStaticSolvers/gsStaticNewton.hpp:101-316; options gsStaticBase.h:66-75,
+// gsStaticNewton.hpp:20-25).  Residual convention R = L*F - Fint(U).
+class StaticNewtonGPU {
+public:
+    StaticNewtonGPU(Problem& P, const Options& opt);
+    int solve_linear();
+    int solve();                       // nonlinear Newton
+    void set_displacement(const double* d_U);
+    void set_update(const double* d_DU);
+    void set_load(double L) { L_ = L; }
+    const double* solution() const { return U_.get(); }
+    int iterations() const { return num_it_; }
+    double residual_ratio() const { return residual_ / residualIni_; }
+    LinearSolver& lin() { return *S_; }
+
+private:
+    void residual(const double* d_x, double* d_R);
+    int solve_nonlinear_impl();
+    Problem& P_;
+    Options opt_;
+    std::unique_ptr<LinearSolver> S_;
+    DevBuf<double> U_, DU_, dU_, R_, x_, fint_;
+    double L_ = 1.0;
+    bool headstart_ = false, has_DU_ = false;
+    int num_it_ = 0;
+    double residual_ = 0, residualIni_ = 1, residualOld_ = 0;
+};
+
+// gsALMBase + subclasses (gsALMSolvers/gsALMBase.hpp:22-416, gsALMCrisfield.hpp,
+// gsALMRiks.hpp, gsALMLoadControl.hpp).  ALResidual convention R = Fint(U) - L*F.
+class ALMGPU {
+public:
+    enum Method { Crisfield = 0, Riks = 1, LoadControl = 2 };
+    ALMGPU(Problem& P, Method m, const Options& opt);
+    void apply_options();
+    void initialize();
+    int step();
+    void set_length(double l);
+    double reduce_length(double fac) { arcLength_ *= fac; return arcLength_; }
+    double length() const { return arcLength_; }
+    void set_solution(const double* d_U, double L);
+    void set_solution_step(const double* d_DU, double DL);
+    void set_initial_guess(const double* d_U, double L);
+    const double* U() const { return U_.get(); }
+    double L() const { return L_; }
+    const double* Uprev() const { return Uprev_.get(); }
+    double Lprev() const { return Lprev_; }
+    const double* DUold() const { return DUold_.get(); }
+    double DLold() const { return DLold_; }
+    int iterations() const { return num_it_; }
+    double residueF() const { return residueF_; }
+    double residueU() const { return residueU_; }
+    double phi() const { return phi_; }
+    bool converged() const { return converged_; }
+    LinearSolver& lin() { return *S_; }
+    // per-step work counters
+    int n_jac = 0, n_res = 0, n_solve = 0;
+
+private:
+    void step_impl();
+    void initiate_step();
+    void predictor();
+    void predictor_guess();
+    void quasi_newton_iteration();
+    void iteration();
+    void iteration_finish();
+    void compute_jacobian();
+    void compute_residual();
+    void compute_residual_norms();
+    void solve_ut_ubar(bool need_ut);
+    void compute_lambda_mu();
+    void lambdas_crisfield();
+
+    Problem& P_;
+    Method method_;
+    Options opt_;
+    std::unique_ptr<LinearSolver> S_;
+    int n_;
+    DevBuf<double> U_, DU_, dU_, dUt_, dUbar_, DUold_, Uprev_, Uguess_, R_, x_, fint_, rhs2_, sol2_, tmp_;
+    double L_ = 0, DL_ = 0, dL_ = 0, DLold_ = 0, Lprev_ = 0, Lguess_ = 0;
+    bool has_guess_ = false;
+    double FF_ = 0;
+    // options
+    int maxIt_ = 100;
+    double tolF_ = 1e-3, tolU_ = 1e-6, relax_ = 1.0;
+    double arcLength_ = 1e-2, arcLength_prev_ = 1e-2, arcLength_ori_ = 1e-2;
+    bool adaptive_ = false;
+    int desiredIt_ = 10;
+    bool quasi_ = false;
+    int quasiInterval_ = -1;
+    double phi_ = -1;
+    bool phi_user_ = false;
+    int angle_ = 0;
+    // state
+    int num_it_ = 0;
+    bool converged_ = false;
+    double eta_ = 1.0;
+    double residueF_ = 0, residueU_ = 0, basisF_ = 0, basisU_ = 0;
+    bool ut_valid_ = false;
+};
+
+}  // namespace klsa

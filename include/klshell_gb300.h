@@ -1,0 +1,158 @@
+/* klshell_gb300.h -- C-ABI of the GB300 (sm_103a) Kirchhoff-Love shell hot path.
+ *
+ * The reference module (gsStructuralAnalysis) has no FFI: its boundary is the set of C++
+ * callback types in gsStructuralAnalysisTools/gsStructuralAnalysisTypes.h:58-93
+ * (Jacobian_t, dJacobian_t, Residual_t, ALResidual_t, Mass_t, Force_t), the sparse-solver
+ * name resolved by gsSparseSolver<T>::get (gsStaticSolvers/gsStaticBase.h:85,
+ * gsALMSolvers/gsALMBase.hpp:73) and the solver classes' step/solve calls.  Each entry
+ * point below names the reference interface it replaces.  Plain pointers and sizes only;
+ * host buffers are caller-owned; every call returns a status (0..5 = gsStatus, negative =
+ * ABI error) and never throws.
+ *
+ * Vector layout of every host vector: free dofs in the reference's order (component-blocked
+ * x,y,z, Dirichlet dofs removed), i.e. what gsThinShellAssembler's Residual/Jacobian
+ * callbacks exchange with the solvers.
+ */
+#ifndef KLSHELL_GB300_H
+#define KLSHELL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (gsStatus, gsStructuralAnalysisTypes.h:22-30) ---------------------- */
+#define KLSA_SUCCESS 0
+#define KLSA_NOT_CONVERGED 1
+#define KLSA_ASSEMBLY_ERROR 2
+#define KLSA_SOLVER_ERROR 3
+#define KLSA_NOT_STARTED 4
+#define KLSA_OTHER_ERROR 5
+#define KLSA_INVALID_ARGUMENT (-1)
+#define KLSA_CUDA_ERROR (-2)
+#define KLSA_UNSUPPORTED (-3)
+
+/* ---- problem description ------------------------------------------------------------- */
+/* One tensor-product B-spline patch (open knot vectors, simple interior knots), SVK
+ * material, homogeneous Dirichlet mask, dead loads.  Control point A = j*n1 + i. */
+typedef struct klsa_patch_desc {
+    int32_t p;                   /* degree in both directions, 1..4 */
+    int32_t n1, n2;              /* control points per direction */
+    int32_t nq;                  /* Gauss points per direction per element, 0 -> p+1 */
+    const double* knots1;        /* n1+p+1 */
+    const double* knots2;        /* n2+p+1 */
+    const double* ctrl;          /* n1*n2*3 reference control points, (A*3 + c) */
+    double E, nu, thickness, density;
+    const uint8_t* fixed;        /* 3*n1*n2 component-blocked mask, 1 = Dirichlet (u = 0) */
+    const double* surface_load;  /* 3 comps per unit reference area, or NULL */
+    int32_t n_point_loads;       /* rows of [xi1, xi2, Px, Py, Pz] */
+    const double* point_loads;
+    int32_t n_edge_loads;        /* rows of [side(0:xi1=0,1:xi1=1,2:xi2=0,3:xi2=1), qx, qy, qz] */
+    const double* edge_loads;
+} klsa_patch_desc;
+
+typedef struct klsa_problem klsa_problem;
+typedef struct klsa_options klsa_options;
+typedef struct klsa_solver klsa_solver;
+typedef struct klsa_static klsa_static;
+typedef struct klsa_alm klsa_alm;
+
+/* Last error message of the calling thread (static storage). */
+const char* klsa_last_error(void);
+/* Number of CUDA kernels this library launched since load (graph replays count their nodes). */
+uint64_t klsa_launch_count(void);
+
+/* Builds device geometry tables, the dof maps, the CSR pattern and the nested-dissection
+ * analysis.  Replaces constructing gsThinShellAssembler + assemble() (call sites
+ * tutorials/nonlinear_shell_static.cpp:106-139). */
+int klsa_problem_create(const klsa_patch_desc* desc, klsa_problem** out);
+int klsa_problem_destroy(klsa_problem* prob);
+int64_t klsa_problem_ndof(const klsa_problem* prob);   /* free dofs */
+int64_t klsa_problem_nnz(const klsa_problem* prob);    /* CSR nonzeros of K over free dofs */
+
+/* Force_t (gsStructuralAnalysisTypes.h:61): external load vector F. */
+int klsa_force(klsa_problem* prob, double* F);
+/* Residual_t (Types.h:66): R = Fext - Fint(x), assembled in FP64 on the device. */
+int klsa_residual(klsa_problem* prob, const double* x, double* R);
+/* ALResidual_t (Types.h:68): R = Fint(x) - lambda*F (tutorials/nonlinear_shell_arcLength.cpp:135-142). */
+int klsa_al_residual(klsa_problem* prob, const double* x, double lambda, double* R);
+/* Jacobian_t (Types.h:85): K(x) as CSR over free dofs (reference order, rows sorted).
+ * precision 0: FP32 element integration, 1: FP64.  rowptr has ndof+1 entries. */
+int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_t* rowptr, int32_t* cols,
+                      double* vals);
+/* Mass_t (Types.h:71): consistent mass matrix int rho t N_A N_B dA, same CSR pattern. */
+int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals);
+
+/* ---- options (gsOptionList keys and defaults of the mirrored classes) ------------------ */
+klsa_options* klsa_options_create(void);
+void klsa_options_destroy(klsa_options* opt);
+int klsa_options_set_real(klsa_options* opt, const char* key, double value);
+int klsa_options_set_int(klsa_options* opt, const char* key, int64_t value);
+int klsa_options_set_string(klsa_options* opt, const char* key, const char* value);
+
+/* ---- named sparse solver (gsSparseSolver<T>::get(name), gsStaticBase.h:85) --------------
+ * "SimplicialLDLT" / "GPUMultifrontalLDLT": nested-dissection multifrontal LDL^T, FP32
+ * fronts, optional FP64 iterative refinement ("Refinement" steps, tolerance "RefineTol").
+ * "CGDiagonal" / "GPUPCG": Jacobi (3x3 nodal block) preconditioned CG on the CSR matrix. */
+int klsa_solver_create(klsa_problem* prob, const char* name, const klsa_options* opt, klsa_solver** out);
+int klsa_solver_destroy(klsa_solver* s);
+/* compute(K(x)) of the named solver: assemble the tangent at x on the device and factorise. */
+int klsa_solver_compute_jacobian(klsa_solver* s, const double* x);
+/* compute(K_L) */
+int klsa_solver_compute_linear(klsa_solver* s);
+/* solve(b) for nrhs right-hand sides stored one after the other (ndof each). */
+int klsa_solver_solve(klsa_solver* s, const double* b, double* x, int nrhs);
+/* LDL^T pivots: minimum of D and number of negative entries (determinant stability
+ * indicator, gsStaticBase.h:162-179). */
+int klsa_solver_stability(klsa_solver* s, double* min_d, int64_t* negatives);
+
+/* ---- gsStaticNewton (gsStaticSolvers/gsStaticNewton.hpp:101-316) ----------------------- */
+int klsa_static_create(klsa_problem* prob, const klsa_options* opt, klsa_static** out);
+int klsa_static_destroy(klsa_static* s);
+int klsa_static_solve(klsa_static* s);                    /* solve(): nonlinear Newton */
+int klsa_static_solve_linear(klsa_static* s);             /* solveLinear() */
+int klsa_static_set_load_factor(klsa_static* s, double lambda);   /* Residual = lambda*F - Fint */
+int klsa_static_set_displacement(klsa_static* s, const double* U);   /* setDisplacement */
+int klsa_static_solution(klsa_static* s, double* U);
+int klsa_static_iterations(klsa_static* s);
+
+/* ---- arc-length family (gsALMSolvers/gsALMBase.hpp:354-416 and subclasses) ------------
+ * method: "Crisfield" (gsALMCrisfield.hpp), "Riks" (gsALMRiks.hpp), "LoadControl"
+ * (gsALMLoadControl.hpp). */
+int klsa_alm_create(klsa_problem* prob, const char* method, const klsa_options* opt, klsa_alm** out);
+int klsa_alm_destroy(klsa_alm* a);
+int klsa_alm_initialize(klsa_alm* a);                     /* initialize(false) */
+int klsa_alm_step(klsa_alm* a);                           /* step() -> gsStatus */
+int klsa_alm_set_length(klsa_alm* a, double length);      /* setLength */
+int klsa_alm_reduce_length(klsa_alm* a, double factor);   /* reduceLength */
+double klsa_alm_get_length(klsa_alm* a);
+int klsa_alm_set_solution(klsa_alm* a, const double* U, double L);      /* setSolution */
+int klsa_alm_set_solution_step(klsa_alm* a, const double* DU, double DL); /* setSolutionStep */
+int klsa_alm_set_initial_guess(klsa_alm* a, const double* U, double L);  /* setInitialGuess */
+int klsa_alm_solution(klsa_alm* a, double* U, double* L);  /* solutionU / solutionL */
+/* out: [iterations, residueF, residueU, phi, converged, Lprev, DeltaL_old] */
+int klsa_alm_info(klsa_alm* a, double* out);
+/* Copies the previous converged point (Uprev, Lprev) and the last step (DeltaUold, DeltaLold). */
+int klsa_alm_history(klsa_alm* a, double* Uprev, double* Lprev, double* DUold, double* DLold);
+
+/* ---- eigen problems (gsEigenSolvers/gsEigenProblemBase.hpp:152-215) ------------------- */
+/* Buckling (gsBucklingSolver.h:127-149): u_L = K_L^-1 (scaling F), B = K(u_L) - K_L,
+ * eigenpairs of K_L v = lambda B v by shift-invert Lanczos about ``shift``.
+ * values: nev, vectors: nev*ndof (may be NULL). */
+int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double scaling,
+                  double* values, double* vectors);
+/* Modal (gsModalSolver.h:46-51): eigenpairs of K v = omega^2 M v about ``shift``. */
+int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
+               double* vectors);
+
+/* ---- host-only symbolic queries (no device call) -------------------------------------- */
+int klsa_nd_stats(int n1, int n2, int p, const uint8_t* fixed, int leaf_max, double* out);
+int klsa_nd_export(int n1, int n2, int p, const uint8_t* fixed, int leaf_max, int32_t* full2int,
+                   int32_t* node_info, int32_t* halo_ids, int64_t capacity_nodes, int64_t capacity_halo);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KLSHELL_GB300_H */
