@@ -80,6 +80,13 @@ SIGNATURES = {
     "klsa_alm_history": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
+    "klsa_profile_enable": (_c_int, [_c_int]),
+    "klsa_profile_read": (_c_int, [_c_vp, _c_vp]),
+    "klsa_profile_reset": (_c_int, []),
+    "klsa_event_record": (_c_int, [_c_vp, _c_int]),
+    "klsa_event_elapsed": (_c_int, [_c_vp, _c_int, _c_int, _c_vp]),
+    "klsa_problem_sync": (_c_int, [_c_vp]),
+    "klsa_problem_stats": (_c_int, [_c_vp, _c_vp]),
     "klsa_nd_stats": (_c_int, [_c_int, _c_int, _c_int, _c_vp, _c_int, _c_vp]),
     "klsa_nd_export": (_c_int, [_c_int, _c_int, _c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_i64, _c_i64]),
 }
@@ -120,6 +127,24 @@ def _check(code):
 
 def launch_count() -> int:
     return int(load_library().klsa_launch_count())
+
+
+PHASES = ["assembly", "factorization", "solve", "residual", "mf_update", "mf_diag", "mf_panel", "other"]
+
+
+def profile_enable(on: bool = True):
+    load_library().klsa_profile_enable(1 if on else 0)
+
+
+def profile_reset():
+    load_library().klsa_profile_reset()
+
+
+def profile_read():
+    ms = np.zeros(8)
+    cnt = np.zeros(8, dtype=np.uint64)
+    _check(load_library().klsa_profile_read(_ptr(ms), _ptr(cnt)))
+    return {k: (float(m), int(c)) for k, m, c in zip(PHASES, ms, cnt)}
 
 
 class Options:
@@ -180,6 +205,23 @@ class Problem:
 
     def __del__(self):
         self.close()
+
+    def stats(self):
+        out = np.zeros(8)
+        _check(_lib.klsa_problem_stats(self.h, _ptr(out)))
+        keys = ["ndof", "nnz", "elements", "gauss_points", "front_bytes", "factor_flops", "tangent_flops", "nodes"]
+        return dict(zip(keys, out.tolist()))
+
+    def record(self, slot):
+        _check(_lib.klsa_event_record(self.h, int(slot)))
+
+    def elapsed_ms(self, a, b):
+        ms = np.zeros(1, dtype=np.float32)
+        _check(_lib.klsa_event_elapsed(self.h, int(a), int(b), _ptr(ms)))
+        return float(ms[0])
+
+    def sync(self):
+        _check(_lib.klsa_problem_sync(self.h))
 
     def force(self):
         F = np.zeros(self.ndof)

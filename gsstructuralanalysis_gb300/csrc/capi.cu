@@ -15,6 +15,11 @@ using namespace klsa;
 struct klsa_problem {
     std::unique_ptr<Problem> P;
     DevBuf<double> x, r, f;   // staging (internal order)
+    cudaEvent_t ev[16] = {};
+    ~klsa_problem() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
 };
 struct klsa_options {
     Options o;
@@ -403,6 +408,69 @@ int klsa_alm_history(klsa_alm* a, double* Uprev, double* Lprev, double* DUold, d
         if (DUold) a->prob->P->download_pub(a->A->DUold(), DUold);
         if (Lprev) *Lprev = a->A->Lprev();
         if (DLold) *DLold = a->A->DLold();
+        return KLSA_SUCCESS;
+    });
+}
+
+// ---- measurement helpers ----------------------------------------------------------------------
+int klsa_profile_enable(int on) {
+    g_timer.collect();
+    g_timer.enabled = on != 0;
+    return KLSA_SUCCESS;
+}
+int klsa_profile_read(double* ms, uint64_t* counts) {
+    return guarded([&] {
+        g_timer.collect();
+        for (int i = 0; i < PhaseTimer::NPH; ++i) {
+            if (ms) ms[i] = g_timer.ms[i];
+            if (counts) counts[i] = g_timer.count[i];
+        }
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_profile_reset(void) {
+    return guarded([&] {
+        g_timer.reset();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_event_record(klsa_problem* prob, int slot) {
+    if (!prob || slot < 0 || slot >= 16) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!prob->ev[slot]) KL_CUDA(cudaEventCreate(&prob->ev[slot]));
+        KL_CUDA(cudaEventRecord(prob->ev[slot], prob->P->stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_event_elapsed(klsa_problem* prob, int slot_a, int slot_b, float* ms) {
+    if (!prob || !ms || slot_a < 0 || slot_a >= 16 || slot_b < 0 || slot_b >= 16) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!prob->ev[slot_a] || !prob->ev[slot_b]) return KLSA_INVALID_ARGUMENT;
+        KL_CUDA(cudaEventSynchronize(prob->ev[slot_b]));
+        KL_CUDA(cudaEventElapsedTime(ms, prob->ev[slot_a], prob->ev[slot_b]));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_problem_sync(klsa_problem* prob) {
+    if (!prob) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        KL_CUDA(cudaStreamSynchronize(prob->P->stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_problem_stats(klsa_problem* prob, double* out) {
+    if (!prob || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *prob->P;
+        Multifrontal& mf = P.solver();
+        out[0] = P.nfree;
+        out[1] = (double)P.nnz;
+        out[2] = P.nel;
+        out[3] = P.nqp;
+        out[4] = (double)mf.front_bytes();
+        out[5] = mf.flops();
+        out[6] = P.flops_tangent();
+        out[7] = (double)P.tree.nodes.size();
         return KLSA_SUCCESS;
     });
 }

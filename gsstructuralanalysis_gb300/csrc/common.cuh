@@ -84,3 +84,61 @@ extern unsigned long long g_launch_count;
 inline void count_launch(unsigned long long k = 1) { g_launch_count += k; }
 
 }  // namespace klsa
+
+namespace klsa {
+
+// Optional per-phase device timing with CUDA events on the launching stream.
+// Phases: 0 tangent assembly, 1 factorisation, 2 triangular solves, 3 residual (Fint),
+//         4 multifrontal trailing-update launches, 5 multifrontal diagonal launches,
+//         6 multifrontal panel launches, 7 eigen / other.
+struct PhaseTimer {
+    static constexpr int NPH = 8;
+    bool enabled = false;
+    double ms[NPH] = {0};
+    unsigned long long count[NPH] = {0};
+    std::vector<cudaEvent_t> pool;
+    struct Pending { int ph; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    cudaEvent_t get() {
+        if (pool.empty()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t begin(cudaStream_t s) {
+        if (!enabled) return nullptr;
+        cudaEvent_t a = get();
+        cudaEventRecord(a, s);
+        return a;
+    }
+    void end(cudaStream_t s, int ph, cudaEvent_t a) {
+        if (!enabled || !a) return;
+        cudaEvent_t b = get();
+        cudaEventRecord(b, s);
+        pending.push_back({ph, a, b});
+        if (pending.size() > 4096) collect();
+    }
+    void collect() {
+        for (auto& p : pending) {
+            float t = 0;
+            cudaEventSynchronize(p.b);
+            cudaEventElapsedTime(&t, p.a, p.b);
+            ms[p.ph] += t;
+            count[p.ph] += 1;
+            pool.push_back(p.a);
+            pool.push_back(p.b);
+        }
+        pending.clear();
+    }
+    void reset() {
+        collect();
+        for (int i = 0; i < NPH; ++i) { ms[i] = 0; count[i] = 0; }
+    }
+};
+extern PhaseTimer g_timer;
+
+}  // namespace klsa

@@ -150,23 +150,27 @@ int MFSolver::factor_current(bool f64_for_refine) {
         throw std::logic_error("FP32 matrix values missing");
     }
     has64_ = f64_for_refine;
-    return P_.solver().factorize(P_.d_vals32.get(), true);
+    cudaEvent_t ev = g_timer.begin(P_.stream);
+    P_.solver().factorize_async(P_.d_vals32.get());
+    g_timer.end(P_.stream, 1, ev);
+    return P_.solver().read_status();
 }
 
 int MFSolver::compute_tangent() {
-    if (refine_ > 0) {
-        P_.tangent_f64();
-        return factor_current(true);
-    }
-    P_.tangent_f32();
-    return factor_current(false);
+    cudaEvent_t ev = g_timer.begin(P_.stream);
+    if (refine_ > 0) P_.tangent_f64();
+    else P_.tangent_f32();
+    g_timer.end(P_.stream, 0, ev);
+    return factor_current(refine_ > 0);
 }
 
 void MFSolver::solve_raw(const double* d_b, double* d_x, int nrhs) {
     int n = P_.nfree;
+    cudaEvent_t ev = g_timer.begin(P_.stream);
     vec::to_f32(d_b, b32_.get(), (int64_t)n * nrhs, P_.stream);
     P_.solver().solve(b32_.get(), x32_.get(), nrhs);
     vec::to_f64(x32_.get(), d_x, (int64_t)n * nrhs, P_.stream);
+    g_timer.end(P_.stream, 2, ev);
 }
 
 int MFSolver::solve(const double* d_b, double* d_x, int nrhs) {

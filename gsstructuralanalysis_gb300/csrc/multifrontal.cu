@@ -499,21 +499,27 @@ void Multifrontal::factorize_async(const float* d_vals) {
             }
         for (Step& st : lv.steps) {
             if (st.diag.count) {
+                cudaEvent_t evk = g_timer.begin(stream_);
                 mf_diag_kernel<<<st.diag.count, 256, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
                                                                    d_own_.get(), d_front_off_.get(), d_linv_off_.get(),
                                                                    pool_.get(), linv_.get(), D_.get(), status_.get());
+                g_timer.end(stream_, 5, evk);
                 count_launch();
             }
             if (st.panel.count) {
+                cudaEvent_t evk = g_timer.begin(stream_);
                 mf_panel_kernel<<<st.panel.count, 256, 0, stream_>>>(st.panel.items, st.t, d_f_.get(), d_k_.get(),
                                                                      d_front_off_.get(), d_linv_off_.get(),
                                                                      d_ws_off_.get(), pool_.get(), linv_.get(), ws_.get());
+                g_timer.end(stream_, 6, evk);
                 count_launch();
             }
             if (st.update.count) {
+                cudaEvent_t evk = g_timer.begin(stream_);
                 mf_update_kernel<<<st.update.count, 256, 0, stream_>>>(st.update.items, st.t, d_f_.get(), d_k_.get(),
                                                                        d_front_off_.get(), d_ws_off_.get(), pool_.get(),
                                                                        ws_.get());
+                g_timer.end(stream_, 4, evk);
                 count_launch();
             }
         }

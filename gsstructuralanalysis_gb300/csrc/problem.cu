@@ -13,6 +13,7 @@
 namespace klsa {
 
 unsigned long long g_launch_count = 0;
+PhaseTimer g_timer;
 
 namespace {
 

@@ -208,10 +208,12 @@ void ALMGPU::compute_jacobian() {
 }
 
 void ALMGPU::compute_residual() {
+    cudaEvent_t ev = g_timer.begin(P_.stream);
     vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, P_.stream);
     P_.set_displacement(x_.get());
     P_.internal_force(fint_.get());
     vec::lincomb(1.0, fint_.get(), -(L_ + DL_), P_.d_F.get(), R_.get(), n_, P_.stream);
+    g_timer.end(P_.stream, 3, ev);
     ++n_res;
 }
 

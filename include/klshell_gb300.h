@@ -146,6 +146,21 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
                double* vectors);
 
+/* ---- measurement helpers (no counterpart in the reference, which has no device) -------- */
+/* Per-phase device times from CUDA events on the problem streams: ms[8], counts[8] for
+ * 0 tangent assembly, 1 factorisation, 2 solves, 3 residual, 4/5/6 multifrontal update /
+ * diagonal / panel launches, 7 other. */
+int klsa_profile_enable(int on);
+int klsa_profile_read(double* ms, uint64_t* counts);
+int klsa_profile_reset(void);
+/* Records CUDA event `slot` (0..15) on the problem's stream; elapsed time between two slots. */
+int klsa_event_record(klsa_problem* prob, int slot);
+int klsa_event_elapsed(klsa_problem* prob, int slot_a, int slot_b, float* ms);
+int klsa_problem_sync(klsa_problem* prob);
+/* out[8]: ndof, nnz, elements, Gauss points, front pool bytes, factorisation flops,
+ * tangent-assembly flops, multifrontal tree nodes */
+int klsa_problem_stats(klsa_problem* prob, double* out);
+
 /* ---- host-only symbolic queries (no device call) -------------------------------------- */
 int klsa_nd_stats(int n1, int n2, int p, const uint8_t* fixed, int leaf_max, double* out);
 int klsa_nd_export(int n1, int n2, int p, const uint8_t* fixed, int leaf_max, int32_t* full2int,
