@@ -172,6 +172,12 @@ def run_ours(args):
     value = world * pts / (ms / 1e3)
     U_end, L_end = alm.solutionU(), alm.solutionL()
 
+    if args.lean:
+        # timed leg only (used for ncu launch lists)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "points/s", "steps": args.steps,
+                              "ms_per_step": ms / max(pts, 1), "gpu_launches": int(launches), "lean": True}))
+        return
     # e2e: the same steps again through the C-ABI with host vectors in and out every step
     alm2 = G.ALMCrisfield(gp, ALM_OPTS)
     alm2.initialize()
@@ -375,6 +381,7 @@ def main():
     ap.add_argument("--imperfection", type=int, default=0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

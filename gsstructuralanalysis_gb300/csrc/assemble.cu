@@ -248,51 +248,97 @@ __global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1
     }
 }
 
+// Internal force in FP64.  A warp holds ES = 32 / max((p+1)^2, nq^2) elements: lanes first act
+// as Gauss points (one lane evaluates one point's deformed geometry and stress resultants, no
+// redundant per-lane work), then as control points (one lane accumulates one control point's
+// three force components over the element's Gauss points, reading the point states from
+// shared memory).
+constexpr int QSTATE = 16;   // G1, G2, S11, S22, S12 of one Gauss point
+
 template <int P>
 __global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, int ncp, int nq,
                                                       const double* __restrict__ tab1, const double* __restrict__ tab2,
                                                       const double* __restrict__ qpgeo, const double* __restrict__ ufull,
                                                       double tm, double tb, double* __restrict__ elemR) {
     constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
+    __shared__ double us[4][32][3];
+    __shared__ double qs[4][32][QSTATE];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int e = blockIdx.x * 4 + warp;
-    if (e >= nel) return;
-    const int e1 = e % m1, e2 = e / m1;
-    const int la = lane % NB1, lb = lane / NB1;
-    const bool own = lane < NB;
-    double ux = 0, uy = 0, uz = 0;
-    if (own) {
-        int A = (e2 + lb) * n1 + (e1 + la);
-        ux = ufull[A]; uy = ufull[ncp + A]; uz = ufull[2 * ncp + A];
+    const int nqp = nq * nq;
+    const int lpe = NB > nqp ? NB : nqp;
+    const int es = 32 / lpe;
+    const int slot = lane / lpe, idx = lane % lpe;
+    const int e = (blockIdx.x * 4 + warp) * es + slot;
+    const bool live = slot < es && e < nel;
+    const int e1 = live ? e % m1 : 0, e2 = live ? e / m1 : 0;
+    // phase 0: displacements of the element's control points
+    if (live && idx < NB) {
+        int A = (e2 + idx / NB1) * n1 + (e1 + idx % NB1);
+        us[warp][slot * NB + idx][0] = ufull[A];
+        us[warp][slot * NB + idx][1] = ufull[ncp + A];
+        us[warp][slot * NB + idx][2] = ufull[2 * ncp + A];
     }
-    double f[3] = {0, 0, 0};
-    for (int q2 = 0; q2 < nq; ++q2)
-        for (int q1 = 0; q1 < nq; ++q1) {
-            double N1 = 0, N2 = 0, N11 = 0, N22 = 0, N12 = 0;
-            if (own) {
-                const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
-                const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
-                N1 = t1[NB1 + la] * t2[lb]; N2 = t1[la] * t2[NB1 + lb];
-                N11 = t1[2 * NB1 + la] * t2[lb]; N22 = t1[la] * t2[2 * NB1 + lb]; N12 = t1[NB1 + la] * t2[NB1 + lb];
-            }
-            double du[15] = {N1 * ux, N1 * uy, N1 * uz, N2 * ux, N2 * uy, N2 * uz, N11 * ux, N11 * uy, N11 * uz,
-                             N22 * ux, N22 * uy, N22 * uz, N12 * ux, N12 * uy, N12 * uz};
+    __syncwarp();
+    // phase 1: one lane per Gauss point
+    if (live && idx < nqp) {
+        int q1 = idx % nq, q2 = idx / nq;
+        const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
+        const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
+        double du[15];
 #pragma unroll
-            for (int k = 0; k < 15; ++k) du[k] = warp_sum(du[k]);
-            const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * 22;
-            QPState<double> st;
-            qp_state<P, double>(geo, du, tm, tb, st);
-            if (own) {
-                CPData<double> o;
-                cp_data<double>(st, N1, N2, N11, N22, N12, o, false);
+        for (int k = 0; k < 15; ++k) du[k] = 0.0;
 #pragma unroll
-                for (int i = 0; i < 3; ++i)
-                    f[i] += (st.n[0] * o.Bm[0][i] + st.n[1] * o.Bm[1][i] + st.n[2] * o.Bm[2][i] +
-                             st.m[0] * o.Bb[0][i] + st.m[1] * o.Bb[1][i] + st.m[2] * o.Bb[2][i]) * st.dV;
+        for (int c = 0; c < NB; ++c) {
+            int a = c % NB1, b = c / NB1;
+            double N1 = t1[NB1 + a] * t2[b], N2 = t1[a] * t2[NB1 + b];
+            double N11 = t1[2 * NB1 + a] * t2[b], N22 = t1[a] * t2[2 * NB1 + b], N12 = t1[NB1 + a] * t2[NB1 + b];
+            const double* u = us[warp][slot * NB + c];
+            double Ns[5] = {N1, N2, N11, N22, N12};
+#pragma unroll
+            for (int g = 0; g < 5; ++g) {
+                du[3 * g] += Ns[g] * u[0];
+                du[3 * g + 1] += Ns[g] * u[1];
+                du[3 * g + 2] += Ns[g] * u[2];
             }
         }
-    if (own)
-        for (int i = 0; i < 3; ++i) elemR[(size_t)e * D + 3 * lane + i] = f[i];
+        const double* geo = qpgeo + ((size_t)e * nqp + idx) * 22;
+        QPState<double> st;
+        qp_state<P, double>(geo, du, tm, tb, st);
+        // f_{A,i} = sum_qp [N1 G1 + N2 G2 - N11 S11 - N22 S22 - N12 S12]_i with
+        //   G1 = dV (n0 a1 + n2 a2 - (a2 x w)/l),  G2 = dV (n1 a2 + n2 a1 - (w x a1)/l),
+        //   S11 = dV m0 a3, S22 = dV m1 a3, S12 = 2 dV m2 a3   (w = v - (v.a3) a3)
+        const double dV = st.dV;
+        V3T<double> u1 = cross3(st.a2, st.w), u2 = cross3(st.w, st.a1);
+        double* o = qs[warp][slot * nqp + idx];
+        o[0] = dV * (st.n[0] * st.a1.x + st.n[2] * st.a2.x - u1.x * st.il);
+        o[1] = dV * (st.n[0] * st.a1.y + st.n[2] * st.a2.y - u1.y * st.il);
+        o[2] = dV * (st.n[0] * st.a1.z + st.n[2] * st.a2.z - u1.z * st.il);
+        o[3] = dV * (st.n[1] * st.a2.x + st.n[2] * st.a1.x - u2.x * st.il);
+        o[4] = dV * (st.n[1] * st.a2.y + st.n[2] * st.a1.y - u2.y * st.il);
+        o[5] = dV * (st.n[1] * st.a2.z + st.n[2] * st.a1.z - u2.z * st.il);
+        const double s11 = dV * st.m[0], s22 = dV * st.m[1], s12 = 2.0 * dV * st.m[2];
+        o[6] = s11 * st.a3.x; o[7] = s11 * st.a3.y; o[8] = s11 * st.a3.z;
+        o[9] = s22 * st.a3.x; o[10] = s22 * st.a3.y; o[11] = s22 * st.a3.z;
+        o[12] = s12 * st.a3.x; o[13] = s12 * st.a3.y; o[14] = s12 * st.a3.z;
+    }
+    __syncwarp();
+    // phase 2: one lane per control point, 15 FMAs per Gauss point
+    if (live && idx < NB) {
+        int a = idx % NB1, b = idx / NB1;
+        double f[3] = {0.0, 0.0, 0.0};
+        for (int qq = 0; qq < nqp; ++qq) {
+            int q1 = qq % nq, q2 = qq / nq;
+            const double* t1 = tab1 + (((size_t)e1 * nq + q1) * 3) * NB1;
+            const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
+            double N1 = t1[NB1 + a] * t2[b], N2 = t1[a] * t2[NB1 + b];
+            double N11 = t1[2 * NB1 + a] * t2[b], N22 = t1[a] * t2[2 * NB1 + b], N12 = t1[NB1 + a] * t2[NB1 + b];
+            const double* o = qs[warp][slot * nqp + qq];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                f[i] += N1 * o[i] + N2 * o[3 + i] - N11 * o[6 + i] - N22 * o[9 + i] - N12 * o[12 + i];
+        }
+        for (int i = 0; i < 3; ++i) elemR[(size_t)e * D + 3 * idx + i] = f[i];
+    }
 }
 
 template <int P>
@@ -339,32 +385,32 @@ __global__ void __launch_bounds__(128) kl_mass_kernel(int nel, int m1, int nq, c
 
 // CSR gather: every nonzero (row R, col C) sums the element entries of the elements that
 // contain both control points (tensor-product structure: element e covers points e..e+p).
+// One warp per row; lanes over the row's columns.
 template <class TE, class TV>
 __global__ void csr_gather_kernel(int nfree, int64_t nnz, int p, int n1, int m1, int m2, int ncp,
                                   const int* __restrict__ rowptr, const int* __restrict__ cols,
                                   const int* __restrict__ int2full, const TE* __restrict__ elemK, TV* __restrict__ vals) {
-    int64_t z = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (z >= nnz) return;
-    // row by binary search
-    int lo = 0, hi = nfree;
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (rowptr[mid] <= z) lo = mid; else hi = mid;
-    }
-    int R = lo, C = cols[z];
-    int fr = int2full[R], fc = int2full[C];
-    int ci = fr / ncp, Ar = fr - ci * ncp, cj = fc / ncp, Ac = fc - cj * ncp;
-    int ir = Ar % n1, jr = Ar / n1, ic = Ac % n1, jc = Ac / n1;
+    int R = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (R >= nfree) return;
+    int fr = int2full[R];
+    int ci = fr / ncp, Ar = fr - ci * ncp;
+    int ir = Ar % n1, jr = Ar / n1;
     int NB1 = p + 1, D = 3 * NB1 * NB1;
-    int e1lo = max(max(ir, ic) - p, 0), e1hi = min(min(ir, ic), m1 - 1);
-    int e2lo = max(max(jr, jc) - p, 0), e2hi = min(min(jr, jc), m2 - 1);
-    double s = 0.0;
-    for (int e2 = e2lo; e2 <= e2hi; ++e2)
-        for (int e1 = e1lo; e1 <= e1hi; ++e1) {
-            int la = (jr - e2) * NB1 + (ir - e1), lb = (jc - e2) * NB1 + (ic - e1);
-            s += (double)elemK[((size_t)(e2 * m1 + e1) * D + 3 * la + ci) * D + 3 * lb + cj];
-        }
-    vals[z] = (TV)s;
+    for (int z = rowptr[R] + lane; z < rowptr[R + 1]; z += 32) {
+        int fc = int2full[cols[z]];
+        int cj = fc / ncp, Ac = fc - cj * ncp;
+        int ic = Ac % n1, jc = Ac / n1;
+        int e1lo = max(max(ir, ic) - p, 0), e1hi = min(min(ir, ic), m1 - 1);
+        int e2lo = max(max(jr, jc) - p, 0), e2hi = min(min(jr, jc), m2 - 1);
+        double s = 0.0;
+        for (int e2 = e2lo; e2 <= e2hi; ++e2)
+            for (int e1 = e1lo; e1 <= e1hi; ++e1) {
+                int la = (jr - e2) * NB1 + (ir - e1), lb = (jc - e2) * NB1 + (ic - e1);
+                s += (double)elemK[((size_t)(e2 * m1 + e1) * D + 3 * la + ci) * D + 3 * lb + cj];
+            }
+        vals[z] = (TV)s;
+    }
 }
 
 __global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int ncp, const int* __restrict__ int2full,
@@ -453,7 +499,7 @@ void Problem::tangent_f32() {
     if (d_elemKf.size() < (size_t)nel * D * D) d_elemKf.alloc((size_t)nel * D * D);
     if (d_vals32.size() < (size_t)nnz) d_vals32.alloc(nnz);
     launch_tangent<float>(*this, d_elemKf.get());
-    csr_gather_kernel<float, float><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKf.get(), d_vals32.get());
+    csr_gather_kernel<float, float><<<ceil_div((int64_t)nfree * 32, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKf.get(), d_vals32.get());
     count_launch();
     KL_CHECK_LAUNCH();
 }
@@ -463,7 +509,7 @@ void Problem::tangent_f64() {
     if (d_elemKd.size() < (size_t)nel * D * D) d_elemKd.alloc((size_t)nel * D * D);
     if (d_vals64.size() < (size_t)nnz) d_vals64.alloc(nnz);
     launch_tangent<double>(*this, d_elemKd.get());
-    csr_gather_kernel<double, double><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
+    csr_gather_kernel<double, double><<<ceil_div((int64_t)nfree * 32, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
     count_launch();
     KL_CHECK_LAUNCH();
 }
@@ -481,7 +527,7 @@ void Problem::mass_f64() {
         default: throw std::invalid_argument("unsupported degree");
     }
     count_launch();
-    csr_gather_kernel<double, double><<<ceil_div(nnz, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
+    csr_gather_kernel<double, double><<<ceil_div((int64_t)nfree * 32, 256), 256, 0, stream>>>(nfree, nnz, p, n1, m1, m2, ncp, d_rowptr.get(), d_cols.get(), d_int2full.get(), d_elemKd.get(), d_vals64.get());
     count_launch();
     KL_CHECK_LAUNCH();
 }
@@ -489,7 +535,10 @@ void Problem::mass_f64() {
 void Problem::internal_force(double* d_out) {
     int D = 3 * (p + 1) * (p + 1);
     if (d_elemR.size() < (size_t)nel * D) d_elemR.alloc((size_t)nel * D);
-    int grid = ceil_div(nel, 4);
+    int lpe = std::max((p + 1) * (p + 1), nq * nq);
+    if (lpe > 32) throw std::invalid_argument("internal force kernel: (p+1)^2 and nq^2 must be <= 32");
+    int es = 32 / lpe;
+    int grid = ceil_div(nel, 4 * es);
     double tm = t, tb = t * t * t / 12.0;
     switch (p) {
         case 2: kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get()); break;

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 namespace klsa {
 
@@ -27,80 +28,202 @@ __global__ void mf_scatter_kernel(int64_t nnz, const int64_t* __restrict__ fpos,
     }
 }
 
-__global__ void mf_extend_add_kernel(const int4* __restrict__ items, const int* __restrict__ f, const int* __restrict__ k,
-                                     const int* __restrict__ parent, const int64_t* __restrict__ front_off,
-                                     const int64_t* __restrict__ map_off, const int* __restrict__ map, float* pool) {
+// Extend-add of 8 columns of a child's Schur complement into its parent's front: one warp per
+// column, lanes stride over the rows (4 independent read-modify-writes in flight per lane).
+constexpr int EA_COLS = 8;
+__global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restrict__ items, const int* __restrict__ f,
+                                                            const int* __restrict__ k, const int* __restrict__ parent,
+                                                            const int64_t* __restrict__ front_off,
+                                                            const int64_t* __restrict__ map_off,
+                                                            const int* __restrict__ map, float* pool) {
     int4 it = items[blockIdx.x];
-    int c = it.x, a0 = it.y;
+    int c = it.x;
+    int a = it.y + (threadIdx.x >> 5);
+    int lane = threadIdx.x & 31;
     int fc = f[c], kc = k[c], hc = fc - kc;
+    if (a >= hc) return;
     int par = parent[c];
     int fp = f[par];
     const int* mp = map + map_off[c];
-    const float* src = pool + front_off[c];
-    float* dst = pool + front_off[par];
-    int a1 = min(a0 + 32, hc);
-    for (int a = a0; a < a1; ++a) {
-        int pa = mp[a];
-        const float* scol = src + (int64_t)(kc + a) * fc + kc;
-        float* dcol = dst + (int64_t)pa * fp;
-        for (int b = a + threadIdx.x; b < hc; b += blockDim.x) dcol[mp[b]] += scol[b];
+    const float* scol = pool + front_off[c] + (int64_t)(kc + a) * fc + kc;
+    float* dcol = pool + front_off[par] + (int64_t)mp[a] * fp;
+    int b = a + lane;
+    for (; b + 96 < hc; b += 128) {
+        float v0 = scol[b], v1 = scol[b + 32], v2 = scol[b + 64], v3 = scol[b + 96];
+        int m0 = mp[b], m1 = mp[b + 32], m2 = mp[b + 64], m3 = mp[b + 96];
+        dcol[m0] += v0;
+        dcol[m1] += v1;
+        dcol[m2] += v2;
+        dcol[m3] += v3;
     }
+    for (; b < hc; b += 32) dcol[mp[b]] += scol[b];
 }
 
-// Diagonal tile: LDL^T in shared memory, then the inverse of the unit lower factor.
+// One warp factors an n x n (n <= 32) symmetric block held in shared memory (lower triangle,
+// row-major, leading dimension ld): L D L^T in registers with shuffles (lane i owns row i), then
+// the inverse of the unit lower factor by forward elimination.  L (strict lower) and D (diagonal)
+// overwrite the block; the inverse is written to X (row-major, ld 33).  No block-level barrier.
+__device__ __noinline__ void warp_ldlt32(float* A, int ld, int n, float* X, bool* bad) {
+    const int i = threadIdx.x & 31;
+    float a[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) a[c] = (i < n && c <= i) ? A[i * ld + c] : 0.f;
+    bool b = false;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        if (j < n) {
+            float d = __shfl_sync(0xffffffffu, a[j], j);
+            if (!(fabsf(d) > 0.f) || !isfinite(d)) { b = true; d = 1.f; }
+            const float lij = (i > j && i < n) ? a[j] / d : 0.f;
+#pragma unroll
+            for (int c = j + 1; c < 32; ++c) {
+                float v = __shfl_sync(0xffffffffu, a[j], c);   // A(c, j) before scaling
+                if (c <= i) a[c] -= lij * v;
+            }
+            if (i > j) a[j] = lij;
+        }
+    }
+    if (b && i == 0) *bad = true;
+#pragma unroll
+    for (int c = 0; c < 32; ++c)
+        if (i < n && c <= i) A[i * ld + c] = a[c];
+    // X = L^-1: row j of X is final at step j; rows i > j subtract L(i, j) * X(j, :)
+    float x[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) x[c] = (c == i) ? 1.f : 0.f;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        if (j < n) {
+            const float l = (i > j && i < n) ? a[j] : 0.f;
+#pragma unroll
+            for (int c = 0; c <= j; ++c) {
+                float v = __shfl_sync(0xffffffffu, x[c], j);
+                x[c] -= l * v;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 32; ++c) X[i * 33 + c] = (i < n && c < n) ? x[c] : 0.f;
+}
+
+// Diagonal tile (kk <= 64 pivots): blocks of 32.  A11 = L11 D1 L11^T and X11 = L11^-1 (warp 0);
+// W21 = A21 X11^T, L21 = W21 D1^-1; A22 -= W21 L21^T; A22 = L22 D2 L22^T and X22 (warp 0);
+// X21 = -X22 L21 X11.  Writes L, D back to the front, D to Dvec and the 64x64 inverse to linv.
 __global__ void __launch_bounds__(256) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                       const int* __restrict__ k, const int* __restrict__ own,
                                                       const int64_t* __restrict__ front_off,
                                                       const int64_t* __restrict__ linv_off, float* pool, float* linv,
                                                       float* Dvec, int* status) {
     __shared__ float A[NB][NB + 1];
-    __shared__ float X[NB][NB + 1];
-    __shared__ float red[4][NB];
+    __shared__ float X11[32][33], X22[32][33], W[32][33], T[32][33];
+    __shared__ bool bad;
     int nd = items[blockIdx.x].x;
     int fN = f[nd], kN = k[nd];
     int c0 = t * NB;
     int kk = min(NB, kN - c0);
+    const int n1 = min(32, kk), n2 = kk - n1;
     float* F = pool + front_off[nd];
-    int tx = threadIdx.x & (NB - 1), ty = threadIdx.x >> 6;
-    for (int c = ty; c < NB; c += 4) {
-        float v = 0.f;
-        if (tx < kk && c < kk && tx >= c) v = F[(int64_t)(c0 + c) * fN + c0 + tx];
-        A[tx][c] = v;
-    }
-    const int r = tx;
-    bool bad = false;
-    for (int j = 0; j < kk; ++j) {
-        __syncthreads();
-        float d = A[j][j];
-        if (!(fabsf(d) > 0.f) || !isfinite(d)) { bad = true; d = 1.f; }
-        float dinv = 1.f / d;
-        float lrj = (r > j && r < kk) ? A[r][j] : 0.f;
-        if (r < kk)
-            for (int c = j + 1 + ty; c <= r; c += 4) A[r][c] -= lrj * A[c][j] * dinv;
-        __syncthreads();
-        if (ty == 0 && r > j && r < kk) A[r][j] = lrj * dinv;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (tid == 0) bad = false;
+    {
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int e = tid + 256 * q, c = e / NB, r = e % NB;   // column-major walk: coalesced
+            v[q] = (r < kk && c <= r) ? F[(int64_t)(c0 + c) * fN + c0 + r] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int e = tid + 256 * q;
+            A[e % NB][e / NB] = v[q];
+        }
     }
     __syncthreads();
-    if (bad && threadIdx.x == 0) atomicExch(status, 1);
-    // write back L (strict lower) and D (diagonal)
-    for (int c = ty; c < kk; c += 4)
-        if (tx < kk && tx >= c) F[(int64_t)(c0 + c) * fN + c0 + tx] = A[tx][c];
-    if (ty == 0 && tx < kk) Dvec[own[nd] + c0 + tx] = A[tx][tx];
-    // X = L^-1 (unit lower), row by row: X[r][c] = -sum_{m=c}^{r-1} L[r][m] X[m][c]
-    for (int c = ty; c < NB; c += 4) X[tx][c] = (tx == c && tx < kk) ? 1.f : 0.f;
-    for (int rr = 1; rr < kk; ++rr) {
-        __syncthreads();
-        int c = tx;
-        float s = 0.f;
-        if (c < rr)
-            for (int m = c + ty; m < rr; m += 4) s += A[rr][m] * X[m][c];
-        red[ty][c] = s;
-        __syncthreads();
-        if (ty == 0 && c < rr) X[rr][c] = -(red[0][c] + red[1][c] + red[2][c] + red[3][c]);
-    }
+    if (warp == 0) warp_ldlt32(&A[0][0], NB + 1, n1, &X11[0][0], &bad);
     __syncthreads();
+    if (n2 > 0) {
+        // W = A21 X11^T ; L21 = W D1^-1.  Thread: row r = tid >> 3, columns j = (tid & 7) + 8 q.
+        const int rr = tid >> 3, jj = tid & 7;
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (rr < n2)
+                for (int m = 0; m < 32; ++m) {
+                    float av = A[32 + rr][m];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] += av * X11[jj + 8 * q][m];   // X11 lower: zero above
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) W[rr][jj + 8 * q] = acc[q];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int j = jj + 8 * q;
+            if (rr < n2 && j < n1) A[32 + rr][j] = W[rr][j] / A[j][j];
+        }
+        __syncthreads();
+        // A22 -= W L21^T (lower; upper entries of the block are never read)
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (rr < n2)
+                for (int j = 0; j < n1; ++j) {
+                    float wv = W[rr][j];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] += wv * A[32 + jj + 8 * q][j];
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int c = jj + 8 * q;
+                if (rr < n2 && c <= rr) A[32 + rr][32 + c] -= acc[q];
+            }
+        }
+        __syncthreads();
+        if (warp == 0) warp_ldlt32(&A[32][32], NB + 1, n2, &X22[0][0], &bad);
+        __syncthreads();
+        // T = L21 X11 ; X21 = -X22 T
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (rr < n2)
+                for (int m = 0; m < n1; ++m) {
+                    float lv = A[32 + rr][m];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] += lv * X11[m][jj + 8 * q];   // X11[m][c] = 0 for c > m
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) T[rr][jj + 8 * q] = acc[q];
+        }
+        __syncthreads();
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (rr < n2)
+                for (int m = 0; m <= rr; ++m) {
+                    float xv = X22[rr][m];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] += xv * T[m][jj + 8 * q];
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) W[rr][jj + 8 * q] = -acc[q];   // X21
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && bad) atomicExch(status, 1);
+    // write back L / D (lower part of the tile), D, and the inverse
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        int e = tid + 256 * q, c = e / NB, r = e % NB;
+        if (r < kk && c <= r) F[(int64_t)(c0 + c) * fN + c0 + r] = A[r][c];
+    }
+    if (tid < kk) Dvec[own[nd] + c0 + tid] = A[tid][tid];
     float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-    for (int rr = ty; rr < NB; rr += 4) Li[rr * NB + tx] = X[rr][tx];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        int e = tid + 256 * q, r = e / NB, c = e % NB;
+        float v = 0.f;
+        if (r < 32 && c < 32) v = X11[r][c];
+        else if (r >= 32 && c < 32) v = (r - 32 < n2) ? W[r - 32][c] : 0.f;
+        else if (r >= 32 && c >= 32) v = X22[r - 32][c - 32];
+        Li[e] = (r < kk && c < kk) ? v : 0.f;
+    }
 }
 
 // Panel: W = A21 * Linv^T (rows r0..r0+63), L21 = W D^-1 written in place, W kept for the update.
@@ -121,10 +244,19 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
     const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
     int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
-    for (int m = lg; m < NB; m += 4) {
-        int rr = lt;
-        As[m][rr] = (m < kk && r0 + rr < fN) ? F[(int64_t)(c0 + m) * fN + r0 + rr] : 0.f;
-        Ls[m][rr] = (m < kk && rr < kk) ? Li[rr * NB + m] : 0.f;
+    {
+        float va[16], vl[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int m = lg + 4 * q;
+            va[q] = (m < kk && r0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + r0 + lt] : 0.f;
+            vl[q] = (m < kk && lt < kk) ? Li[lt * NB + m] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            As[lg + 4 * q][lt] = va[q];
+            Ls[lg + 4 * q][lt] = vl[q];
+        }
     }
     if (threadIdx.x < NB) {
         int j = threadIdx.x;
@@ -180,9 +312,19 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
     const float* W = ws + ws_off[nd];
     int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
-    for (int m = lg; m < NB; m += 4) {
-        Ws[m][lt] = (m < kk && R0 + lt < fN) ? W[(int64_t)m * fN + R0 + lt] : 0.f;
-        Ls[m][lt] = (m < kk && C0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + C0 + lt] : 0.f;
+    {
+        float vw[16], vl[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int m = lg + 4 * q;
+            vw[q] = (m < kk && R0 + lt < fN) ? W[(int64_t)m * fN + R0 + lt] : 0.f;
+            vl[q] = (m < kk && C0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + C0 + lt] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            Ws[lg + 4 * q][lt] = vw[q];
+            Ls[lg + 4 * q][lt] = vl[q];
+        }
     }
     __syncthreads();
     float acc[4][4];
@@ -201,22 +343,34 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(a[i], b[q], acc[i][q]);
     }
+    float old[4][4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         int C = C0 + ty + 16 * q;
-        if (C >= fN) continue;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             int R = R0 + tx + 16 * i;
-            if (R >= fN || R < C) continue;
-            F[(int64_t)C * fN + R] -= acc[i][q];
+            old[i][q] = (C < fN && R < fN && R >= C) ? F[(int64_t)C * fN + R] : 0.f;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        int C = C0 + ty + 16 * q;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            int R = R0 + tx + 16 * i;
+            if (C < fN && R < fN && R >= C) F[(int64_t)C * fN + R] = old[i][q] - acc[i][q];
         }
     }
 }
 
 // Forward substitution of one node: children's update vectors, unit-lower solve of the own
-// block, update vector of the halo.  y holds the result in internal order.
-__global__ void __launch_bounds__(256) mf_fwd_kernel(const int4* __restrict__ items, int n, int nrhs,
+// block (inverse diagonal tiles staged in shared memory), update vector of the halo.  Row loops
+// are unrolled so that every thread keeps 16 independent loads of L in flight.
+constexpr int SOLVE_THREADS = 512;
+
+template <int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_kernel(const int4* __restrict__ items, int n,
                                                      const int* __restrict__ f, const int* __restrict__ k,
                                                      const int* __restrict__ own, const int* __restrict__ child0,
                                                      const int* __restrict__ child1,
@@ -226,12 +380,14 @@ __global__ void __launch_bounds__(256) mf_fwd_kernel(const int4* __restrict__ it
                                                      const int64_t* __restrict__ map_off, const int* __restrict__ map,
                                                      const float* __restrict__ pool, const float* __restrict__ linv,
                                                      float* upd, const float* __restrict__ b, float* y) {
-    extern __shared__ float rhs[];   // fN * nrhs
-    __shared__ float yt[NB * MF_MAX_RHS];
+    extern __shared__ float rhs[];   // fN * NR
+    __shared__ float Ls[NB][NB + 1];
+    __shared__ float yt[NR][NB];
     int nd = items[blockIdx.x].x;
     int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
     const float* F = pool + front_off[nd];
-    for (int q = 0; q < nrhs; ++q)
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
         for (int r = threadIdx.x; r < fN; r += blockDim.x) rhs[r + fN * q] = (r < kN) ? b[o + r + (int64_t)n * q] : 0.f;
     __syncthreads();
     int chs[2] = {child0[nd], child1[nd]};
@@ -241,7 +397,8 @@ __global__ void __launch_bounds__(256) mf_fwd_kernel(const int4* __restrict__ it
             int hc = f[c] - k[c];
             const int* mp = map + map_off[c];
             const float* u = upd + upd_off[c];
-            for (int q = 0; q < nrhs; ++q)
+#pragma unroll
+            for (int q = 0; q < NR; ++q)
                 for (int a = threadIdx.x; a < hc; a += blockDim.x) rhs[mp[a] + fN * q] += u[a + hc * q];
         }
         __syncthreads();
@@ -250,37 +407,72 @@ __global__ void __launch_bounds__(256) mf_fwd_kernel(const int4* __restrict__ it
     for (int t = 0; t < ntiles; ++t) {
         int c0 = t * NB, kk = min(NB, kN - c0);
         const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-        for (int e = threadIdx.x; e < kk * nrhs; e += blockDim.x) {
-            int j = e % kk, q = e / kk;
-            float s = 0.f;
-            for (int m = 0; m <= j; ++m) s += Li[j * NB + m] * rhs[c0 + m + fN * q];
-            yt[j + NB * q] = s;
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < kk * nrhs; e += blockDim.x) {
-            int j = e % kk, q = e / kk;
-            rhs[c0 + j + fN * q] = yt[j + NB * q];
-        }
-        __syncthreads();
-        for (int r = c0 + kk + threadIdx.x; r < fN; r += blockDim.x) {
-            float s[MF_MAX_RHS] = {0.f, 0.f, 0.f, 0.f};
-            for (int j = 0; j < kk; ++j) {
-                float l = F[(int64_t)(c0 + j) * fN + r];
-                for (int q = 0; q < nrhs; ++q) s[q] += l * yt[j + NB * q];
+        {
+            float v[NB * NB / SOLVE_THREADS];
+#pragma unroll
+            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) v[q] = Li[threadIdx.x + SOLVE_THREADS * q];
+#pragma unroll
+            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) {
+                int e = threadIdx.x + SOLVE_THREADS * q;
+                Ls[e / NB][e % NB] = v[q];
             }
-            for (int q = 0; q < nrhs; ++q) rhs[r + fN * q] -= s[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < NB * NR) {
+            int j = threadIdx.x % NB, q = threadIdx.x / NB;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;   // Ls is zero above the diagonal
+            if (j < kk)
+                for (int m = 0; m < kk; m += 4) {
+                    a0 += Ls[j][m] * rhs[c0 + m + fN * q];
+                    if (m + 1 < kk) a1 += Ls[j][m + 1] * rhs[c0 + m + 1 + fN * q];
+                    if (m + 2 < kk) a2 += Ls[j][m + 2] * rhs[c0 + m + 2 + fN * q];
+                    if (m + 3 < kk) a3 += Ls[j][m + 3] * rhs[c0 + m + 3 + fN * q];
+                }
+            yt[q][j] = (a0 + a1) + (a2 + a3);
+        }
+        __syncthreads();
+        if (threadIdx.x < NB * NR) {
+            int j = threadIdx.x % NB, q = threadIdx.x / NB;
+            if (j < kk) rhs[c0 + j + fN * q] = yt[q][j];
+        }
+        // rows below the tile: rhs[r] -= L[r, c0:c0+kk] y_t
+        for (int r = c0 + kk + threadIdx.x; r < fN; r += blockDim.x) {
+            float acc[NR];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) acc[q] = 0.f;
+            const float* col = F + (int64_t)c0 * fN + r;
+            int j = 0;
+            for (; j + 16 <= kk; j += 16) {
+                float l[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) l[u] = col[(int64_t)(j + u) * fN];
+#pragma unroll
+                for (int u = 0; u < 16; ++u)
+#pragma unroll
+                    for (int q = 0; q < NR; ++q) acc[q] += l[u] * yt[q][j + u];
+            }
+            for (; j < kk; ++j) {
+                float l = col[(int64_t)j * fN];
+#pragma unroll
+                for (int q = 0; q < NR; ++q) acc[q] += l * yt[q][j];
+            }
+#pragma unroll
+            for (int q = 0; q < NR; ++q) rhs[r + fN * q] -= acc[q];
         }
         __syncthreads();
     }
     float* u = upd + upd_off[nd];
-    for (int q = 0; q < nrhs; ++q) {
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
         for (int r = threadIdx.x; r < kN; r += blockDim.x) y[o + r + (int64_t)n * q] = rhs[r + fN * q];
         for (int a = threadIdx.x; a < hN; a += blockDim.x) u[a + hN * q] = rhs[kN + a + fN * q];
     }
 }
 
-// Backward substitution of one node: x_own = L11^-T (D^-1 y_own - L21^T x_halo).
-__global__ void __launch_bounds__(256) mf_bwd_kernel(const int4* __restrict__ items, int n, int nrhs,
+// Backward substitution of one node: x_own = L11^-T (D^-1 y_own - L21^T x_halo), tile by tile
+// from the last; one warp per column of the tile, lanes stride over the rows below it.
+template <int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_kernel(const int4* __restrict__ items, int n,
                                                      const int* __restrict__ f, const int* __restrict__ k,
                                                      const int* __restrict__ own,
                                                      const int64_t* __restrict__ front_off,
@@ -289,13 +481,15 @@ __global__ void __launch_bounds__(256) mf_bwd_kernel(const int4* __restrict__ it
                                                      const float* __restrict__ pool, const float* __restrict__ linv,
                                                      const float* __restrict__ Dvec, const float* __restrict__ y,
                                                      float* x) {
-    extern __shared__ float xs[];   // fN * nrhs
-    __shared__ float zt[NB * MF_MAX_RHS];
+    extern __shared__ float xs[];   // fN * NR
+    __shared__ float Ls[NB][NB + 1];
+    __shared__ float zt[NR][NB];
     int nd = items[blockIdx.x].x;
     int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
     const float* F = pool + front_off[nd];
     const int* hl = halo + halo_off[nd];
-    for (int q = 0; q < nrhs; ++q) {
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
         for (int a = threadIdx.x; a < hN; a += blockDim.x) xs[kN + a + fN * q] = x[hl[a] + (int64_t)n * q];
         for (int r = threadIdx.x; r < kN; r += blockDim.x) xs[r + fN * q] = y[o + r + (int64_t)n * q] / Dvec[o + r];
     }
@@ -304,30 +498,60 @@ __global__ void __launch_bounds__(256) mf_bwd_kernel(const int4* __restrict__ it
     int ntiles = (kN + NB - 1) / NB;
     for (int t = ntiles - 1; t >= 0; --t) {
         int c0 = t * NB, kk = min(NB, kN - c0), c1 = c0 + kk;
+        const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
+        {
+            float v[NB * NB / SOLVE_THREADS];
+#pragma unroll
+            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) v[q] = Li[threadIdx.x + SOLVE_THREADS * q];
+#pragma unroll
+            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) {
+                int e = threadIdx.x + SOLVE_THREADS * q;
+                Ls[e / NB][e % NB] = v[q];
+            }
+        }
         for (int j = warp; j < kk; j += nwarp) {
             const float* col = F + (int64_t)(c0 + j) * fN;
-            float s[MF_MAX_RHS] = {0.f, 0.f, 0.f, 0.f};
-            for (int r = c1 + lane; r < fN; r += 32) {
-                float l = col[r];
-                for (int q = 0; q < nrhs; ++q) s[q] += l * xs[r + fN * q];
+            float s[NR];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) s[q] = 0.f;
+            int r = c1 + lane;
+            for (; r + 96 < fN; r += 128) {
+                float l0 = col[r], l1 = col[r + 32], l2 = col[r + 64], l3 = col[r + 96];
+#pragma unroll
+                for (int q = 0; q < NR; ++q)
+                    s[q] += l0 * xs[r + fN * q] + l1 * xs[r + 32 + fN * q] + l2 * xs[r + 64 + fN * q] +
+                            l3 * xs[r + 96 + fN * q];
             }
-            for (int q = 0; q < nrhs; ++q) {
+            for (; r < fN; r += 32) {
+                float l = col[r];
+#pragma unroll
+                for (int q = 0; q < NR; ++q) s[q] += l * xs[r + fN * q];
+            }
+#pragma unroll
+            for (int q = 0; q < NR; ++q) {
                 float v = s[q];
                 for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-                if (lane == 0) zt[j + NB * q] = xs[c0 + j + fN * q] - v;
+                if (lane == 0) zt[q][j] = xs[c0 + j + fN * q] - v;
             }
         }
         __syncthreads();
-        const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-        for (int e = threadIdx.x; e < kk * nrhs; e += blockDim.x) {
-            int j = e % kk, q = e / kk;
-            float s = 0.f;
-            for (int m = j; m < kk; ++m) s += Li[m * NB + j] * zt[m + NB * q];
-            xs[c0 + j + fN * q] = s;
+        if (threadIdx.x < NB * NR) {
+            int j = threadIdx.x % NB, q = threadIdx.x / NB;
+            if (j < kk) {
+                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;   // Ls[m][j] = 0 for m < j
+                for (int m = 0; m < kk; m += 4) {
+                    a0 += Ls[m][j] * zt[q][m];
+                    if (m + 1 < kk) a1 += Ls[m + 1][j] * zt[q][m + 1];
+                    if (m + 2 < kk) a2 += Ls[m + 2][j] * zt[q][m + 2];
+                    if (m + 3 < kk) a3 += Ls[m + 3][j] * zt[q][m + 3];
+                }
+                xs[c0 + j + fN * q] = (a0 + a1) + (a2 + a3);
+            }
         }
         __syncthreads();
     }
-    for (int q = 0; q < nrhs; ++q)
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
         for (int r = threadIdx.x; r < kN; r += blockDim.x) x[o + r + (int64_t)n * q] = xs[r + fN * q];
 }
 
@@ -413,7 +637,7 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
                 int c = slot == 0 ? c0[nd] : c1[nd];
                 if (c < 0) continue;
                 int hc = f[c] - k[c];
-                for (int a0 = 0; a0 < hc; a0 += 32) items.push_back(make_int4(c, a0, 0, 0));
+                for (int a0 = 0; a0 < hc; a0 += EA_COLS) items.push_back(make_int4(c, a0, 0, 0));
             }
             marks.push_back({L, 0, slot, 0, b, items.size()});
         }
@@ -475,13 +699,71 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
     status_.alloc(1);
     status_.zero(stream_);
     size_t smem = (size_t)max_f_ * MF_MAX_RHS * sizeof(float);
-    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 48 * 1024)));
-    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 48 * 1024)));
+    int smax = (int)std::max<size_t>(smem, 48 * 1024);
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
     KL_CUDA(cudaStreamSynchronize(stream_));
+}
+
+namespace {
+bool graphs_enabled() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = std::getenv("KLSA_NO_GRAPHS");
+        on = (e && e[0] == '1') ? 0 : 1;
+    }
+    return on == 1;
+}
+}  // namespace
+
+// Captures `launches` (a fixed launch sequence on stream_) into a graph once and replays it.
+template <class Fn>
+void Multifrontal::replay(GraphSlot& slot, const void* key0, const void* key1, Fn&& launches) {
+    if (g_timer.enabled || !graphs_enabled()) {
+        launches();
+        return;
+    }
+    if (!slot.exec || slot.key0 != key0 || slot.key1 != key1) {
+        if (slot.exec) cudaGraphExecDestroy(slot.exec);
+        slot.exec = nullptr;
+        unsigned long long before = g_launch_count;
+        KL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            launches();
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraph_t g;
+        KL_CUDA(cudaStreamEndCapture(stream_, &g));
+        KL_CUDA(cudaGraphInstantiate(&slot.exec, g, 0));
+        cudaGraphDestroy(g);
+        slot.kernels = g_launch_count - before;
+        g_launch_count = before;
+        slot.key0 = key0;
+        slot.key1 = key1;
+    }
+    KL_CUDA(cudaGraphLaunch(slot.exec, stream_));
+    count_launch(slot.kernels);
+}
+
+Multifrontal::~Multifrontal() {
+    for (GraphSlot* s : {&fact_graph_, &solve_graph_[0], &solve_graph_[1], &solve_graph_[2]})
+        if (s->exec) cudaGraphExecDestroy(s->exec);
 }
 
 void Multifrontal::factorize_async(const float* d_vals) {
     if (!d_vals && nnz_ > 0) throw std::logic_error("multifrontal: no matrix values");
+    replay(fact_graph_, d_vals, nullptr, [&] { factorize_launches(d_vals); });
+}
+
+void Multifrontal::factorize_launches(const float* d_vals) {
     KL_CUDA(cudaMemsetAsync(pool_.get(), 0, pool_.size() * sizeof(float), stream_));
     KL_CUDA(cudaMemsetAsync(status_.get(), 0, sizeof(int), stream_));
     if (nnz_ > 0) {
@@ -492,7 +774,7 @@ void Multifrontal::factorize_async(const float* d_vals) {
         Level& lv = levels_[L];
         for (int s = 0; s < 2; ++s)
             if (lv.ea[s].count) {
-                mf_extend_add_kernel<<<lv.ea[s].count, 128, 0, stream_>>>(lv.ea[s].items, d_f_.get(), d_k_.get(),
+                mf_extend_add_kernel<<<lv.ea[s].count, 256, 0, stream_>>>(lv.ea[s].items, d_f_.get(), d_k_.get(),
                                                                           d_parent_.get(), d_front_off_.get(),
                                                                           d_map_off_.get(), d_map_.get(), pool_.get());
                 count_launch();
@@ -539,27 +821,42 @@ int Multifrontal::factorize(const float* d_vals, bool check_status) {
     return check_status ? read_status() : ST_SUCCESS;
 }
 
-void Multifrontal::solve(const float* d_b, float* d_x, int nrhs) {
-    if (nrhs < 1 || nrhs > MF_MAX_RHS) throw std::invalid_argument("multifrontal solve: nrhs out of range");
+template <int NR>
+void Multifrontal::solve_impl(const float* d_b, float* d_x) {
     for (int L = 0; L < nlevels_; ++L) {
         Level& lv = levels_[L];
-        size_t smem = (size_t)lv.max_f * nrhs * sizeof(float);
-        mf_fwd_kernel<<<lv.nodes.count, 256, smem, stream_>>>(
-            lv.nodes.items, n_, nrhs, d_f_.get(), d_k_.get(), d_own_.get(), d_child0_.get(), d_child1_.get(),
+        size_t smem = (size_t)lv.max_f * NR * sizeof(float);
+        mf_fwd_kernel<NR><<<lv.nodes.count, SOLVE_THREADS, smem, stream_>>>(
+            lv.nodes.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_child0_.get(), d_child1_.get(),
             d_front_off_.get(), d_linv_off_.get(), d_upd_off_.get(), d_map_off_.get(), d_map_.get(), pool_.get(),
             linv_.get(), upd_.get(), d_b, y_.get());
         count_launch();
     }
     for (int L = nlevels_ - 1; L >= 0; --L) {
         Level& lv = levels_[L];
-        size_t smem = (size_t)lv.max_f * nrhs * sizeof(float);
-        mf_bwd_kernel<<<lv.nodes.count, 256, smem, stream_>>>(lv.nodes.items, n_, nrhs, d_f_.get(), d_k_.get(),
-                                                              d_own_.get(), d_front_off_.get(), d_linv_off_.get(),
-                                                              d_halo_off_.get(), d_halo_.get(), pool_.get(),
-                                                              linv_.get(), D_.get(), y_.get(), d_x);
+        size_t smem = (size_t)lv.max_f * NR * sizeof(float);
+        mf_bwd_kernel<NR><<<lv.nodes.count, SOLVE_THREADS, smem, stream_>>>(
+            lv.nodes.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_front_off_.get(), d_linv_off_.get(),
+            d_halo_off_.get(), d_halo_.get(), pool_.get(), linv_.get(), D_.get(), y_.get(), d_x);
         count_launch();
     }
     KL_CHECK_LAUNCH();
+}
+
+void Multifrontal::solve(const float* d_b, float* d_x, int nrhs) {
+    switch (nrhs) {
+        case 1: replay(solve_graph_[0], d_b, d_x, [&] { solve_impl<1>(d_b, d_x); }); break;
+        case 2: replay(solve_graph_[1], d_b, d_x, [&] { solve_impl<2>(d_b, d_x); }); break;
+        case 3:
+        case 4: {
+            // pad to 4 columns: the kernels read/write exactly nrhs columns of ld n
+            if (nrhs == 4) { replay(solve_graph_[2], d_b, d_x, [&] { solve_impl<4>(d_b, d_x); }); break; }
+            solve_impl<2>(d_b, d_x);
+            solve_impl<1>(d_b + 2 * (size_t)n_, d_x + 2 * (size_t)n_);
+            break;
+        }
+        default: throw std::invalid_argument("multifrontal solve: nrhs out of range");
+    }
 }
 
 void Multifrontal::stability(double* min_d, int64_t* negatives) {

@@ -33,7 +33,7 @@ public:
     // csr (internal order): rowptr/cols on the host, used to build the front scatter map
     Multifrontal(const NDTree& tree, const std::vector<int>& rowptr, const std::vector<int>& cols,
                  cudaStream_t stream);
-    ~Multifrontal() = default;
+    ~Multifrontal();
 
     // Numeric factorisation of the FP32 CSR values (internal order, same pattern).
     // Returns ST_SUCCESS or ST_SOLVER_ERROR (zero / non-finite pivot).
@@ -52,6 +52,16 @@ public:
     const std::vector<int>& level_nodes(int lvl) const { return level_nodes_[lvl]; }
 
 private:
+    struct GraphSlot {
+        cudaGraphExec_t exec = nullptr;
+        const void* key0 = nullptr;
+        const void* key1 = nullptr;
+        unsigned long long kernels = 0;
+    };
+    template <class Fn> void replay(GraphSlot& slot, const void* key0, const void* key1, Fn&& launches);
+    void factorize_launches(const float* d_vals);
+    template <int NR> void solve_impl(const float* d_b, float* d_x);
+    GraphSlot fact_graph_, solve_graph_[3];
     cudaStream_t stream_;
     int n_ = 0, nnodes_ = 0, nlevels_ = 0;
     double flops_ = 0;
