@@ -44,6 +44,7 @@ SIGNATURES = {
     "klsa_force": (_c_int, [_c_vp, _c_vp]),
     "klsa_residual": (_c_int, [_c_vp, _c_vp, _c_vp]),
     "klsa_al_residual": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
+    "klsa_al_residual_noalloc": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
     "klsa_jacobian_csr": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
     "klsa_mass_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_options_create": (_c_vp, []),

@@ -551,6 +551,19 @@ void Problem::internal_force(double* d_out) {
     KL_CHECK_LAUNCH();
 }
 
+void Problem::internal_force_elements(double* elemR) {
+    int lpe = std::max((p + 1) * (p + 1), nq * nq);
+    if (lpe > 32) throw std::invalid_argument("internal force kernel: (p+1)^2 and nq^2 must be <= 32");
+    int grid = ceil_div(nel, 4 * (32 / lpe));
+    double tm = t, tb = t * t * t / 12.0;
+    switch (p) {
+        case 2: kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR); break;
+        case 3: kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR); break;
+        default: throw std::invalid_argument("unsupported degree");
+    }
+    count_launch();
+}
+
 void Problem::pub_to_int(const double* d_pub, double* d_int, int nv) {
     permute_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, nv, d_pub2int.get(), d_pub, d_int);
     count_launch();

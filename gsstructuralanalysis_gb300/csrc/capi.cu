@@ -68,6 +68,9 @@ void ensure(DevBuf<double>& b, size_t n) {
 
 }  // namespace
 
+void klsa_set_error(const std::string& msg) { g_err = msg; }
+klsa::Problem* klsa_problem_impl(klsa_problem* prob) { return prob->P.get(); }
+
 extern "C" {
 
 const char* klsa_last_error(void) { return g_err.c_str(); }

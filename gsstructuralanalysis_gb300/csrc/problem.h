@@ -63,6 +63,7 @@ struct Problem {
     void tangent_f32();                                 // d_vals32 = K(u) (FP32 element integration)
     void tangent_f64();                                 // d_vals64 = K(u) (FP64)
     void internal_force(double* d_out);                 // Fint(u), internal order, FP64
+    void internal_force_elements(double* elemR);        // element forces of u into elemR (nel*d), no allocation
     void mass_f64();                                    // d_vals64 = M
     Multifrontal& solver();                             // lazily built
 

@@ -84,6 +84,17 @@ int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_
 /* Mass_t (Types.h:71): consistent mass matrix int rho t N_A N_B dA, same CSR pattern. */
 int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals);
 
+/* ALResidual_t without device allocation -- no counterpart in the reference.  For callers that
+ * cannot call cudaMalloc where they need a residual (inside a captured CUDA-graph region, or
+ * under a framework that owns the device memory pool).  x and R are caller-owned DEVICE
+ * vectors in the public free-dof order.  The element-force scratch is a fixed file-scope device
+ * array of 2^20 doubles (8 MiB per GPU, held until exit); problems with more than 2^20
+ * element-force entries (elements x 3(p+1)^2) are rejected with KLSA_INVALID_ARGUMENT.  Calls
+ * share that array: calls that overlap on the GPU race.  The first call on a device resolves
+ * the array's address once; make it before any stream capture.  Synchronises the problem's
+ * stream before returning. */
+int klsa_al_residual_noalloc(klsa_problem* prob, const double* d_x, double lambda, double* d_R);
+
 /* ---- options (gsOptionList keys and defaults of the mirrored classes) ------------------ */
 klsa_options* klsa_options_create(void);
 void klsa_options_destroy(klsa_options* opt);
