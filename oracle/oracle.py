@@ -689,13 +689,16 @@ def buckling(K_lin, F, jacobian, nev=10, shift=0.0, scaling=1.0, tol=1e-10):
     lu.compute(K_lin)
     uL = lu.solve(scaling * F)
     B = (jacobian(uL) - K_lin).tocsc()
-    vals, vecs = spla.eigsh(sp.csc_matrix(K_lin), k=nev, M=B, sigma=shift, mode="buckling", which="LM", tol=tol)
+    v0 = np.ones(K_lin.shape[0])
+    vals, vecs = spla.eigsh(sp.csc_matrix(K_lin), k=nev, M=B, sigma=shift, mode="buckling", which="LM", tol=tol,
+                            v0=v0)
     order = np.argsort(np.abs(vals))
     return vals[order], vecs[:, order], uL
 
 
 def modal(K, M, nev=10, shift=0.0, tol=1e-10):
     """gsModalSolver pencil (K, M) in shift-invert mode (gsModalSolver.h:46-51)."""
-    vals, vecs = spla.eigsh(sp.csc_matrix(K), k=nev, M=sp.csc_matrix(M), sigma=shift, which="LM", tol=tol)
+    v0 = np.ones(K.shape[0])
+    vals, vecs = spla.eigsh(sp.csc_matrix(K), k=nev, M=sp.csc_matrix(M), sigma=shift, which="LM", tol=tol, v0=v0)
     order = np.argsort(np.abs(vals - shift))
     return vals[order], vecs[:, order]
