@@ -59,69 +59,51 @@ __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restri
     for (; b < hc; b += 32) dcol[mp[b]] += scol[b];
 }
 
-// One warp factors an n x n (n <= 32) symmetric block held in shared memory (lower triangle,
-// row-major, leading dimension ld): L D L^T in registers with shuffles (lane i owns row i), then
-// the inverse of the unit lower factor by forward elimination.  L (strict lower) and D (diagonal)
-// overwrite the block; the inverse is written to X (row-major, ld 33).  No block-level barrier.
-__device__ __noinline__ void warp_ldlt32(float* A, int ld, int n, float* X, bool* bad) {
+// One warp factors an n x n (n <= 16) symmetric block in shared memory (row-major, leading
+// dimension ld, lower triangle): lane i < 16 holds row i in registers; each pivot step is one
+// shuffle broadcast per column.  L (strict lower) and D (diagonal) overwrite the block.
+__device__ __noinline__ void warp_ldlt16(float* A, int ld, int n, bool* bad) {
     const int i = threadIdx.x & 31;
-    float a[32];
+    float a[16];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) a[c] = (i < n && c <= i) ? A[i * ld + c] : 0.f;
+    for (int c = 0; c < 16; ++c) a[c] = (i < n && c <= i) ? A[i * ld + c] : 0.f;
     bool b = false;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < 16; ++j) {
         if (j < n) {
             float d = __shfl_sync(0xffffffffu, a[j], j);
             if (!(fabsf(d) > 0.f) || !isfinite(d)) { b = true; d = 1.f; }
             const float lij = (i > j && i < n) ? a[j] / d : 0.f;
 #pragma unroll
-            for (int c = j + 1; c < 32; ++c) {
+            for (int c = j + 1; c < 16; ++c) {
                 float v = __shfl_sync(0xffffffffu, a[j], c);   // A(c, j) before scaling
                 if (c <= i) a[c] -= lij * v;
             }
-            if (i > j) a[j] = lij;
+            if (i > j && i < n) a[j] = lij;
         }
     }
     if (b && i == 0) *bad = true;
 #pragma unroll
-    for (int c = 0; c < 32; ++c)
+    for (int c = 0; c < 16; ++c)
         if (i < n && c <= i) A[i * ld + c] = a[c];
-    // X = L^-1: row j of X is final at step j; rows i > j subtract L(i, j) * X(j, :)
-    float x[32];
-#pragma unroll
-    for (int c = 0; c < 32; ++c) x[c] = (c == i) ? 1.f : 0.f;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        if (j < n) {
-            const float l = (i > j && i < n) ? a[j] : 0.f;
-#pragma unroll
-            for (int c = 0; c <= j; ++c) {
-                float v = __shfl_sync(0xffffffffu, x[c], j);
-                x[c] -= l * v;
-            }
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < 32; ++c) X[i * 33 + c] = (i < n && c < n) ? x[c] : 0.f;
 }
 
-// Diagonal tile (kk <= 64 pivots): blocks of 32.  A11 = L11 D1 L11^T and X11 = L11^-1 (warp 0);
-// W21 = A21 X11^T, L21 = W21 D1^-1; A22 -= W21 L21^T; A22 = L22 D2 L22^T and X22 (warp 0);
-// X21 = -X22 L21 X11.  Writes L, D back to the front, D to Dvec and the 64x64 inverse to linv.
+// Diagonal tile (kk <= 64 pivots): right-looking LDL^T in 16-column panels -- warp 0 factors the
+// 16x16 diagonal block, one thread per row solves the panel below it, all threads apply the
+// rank-16 update of the rest of the tile.  Writes L (strict lower) and D back to the front and D
+// to Dvec.  The inverse of the unit lower factor is not needed here (the panel kernel solves by
+// substitution) and is formed later, off the critical path, by mf_inverse_kernel.
 __global__ void __launch_bounds__(256) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                       const int* __restrict__ k, const int* __restrict__ own,
-                                                      const int64_t* __restrict__ front_off,
-                                                      const int64_t* __restrict__ linv_off, float* pool, float* linv,
-                                                      float* Dvec, int* status) {
-    __shared__ float A[NB][NB + 1];
-    __shared__ float X11[32][33], X22[32][33], W[32][33], T[32][33];
+                                                      const int64_t* __restrict__ front_off, float* pool, float* Dvec,
+                                                      int* status) {
+    __shared__ float A[NB][NB + 1];      // row-major tile
+    __shared__ float Wp[NB][17];         // W = L D of the current panel
     __shared__ bool bad;
     int nd = items[blockIdx.x].x;
     int fN = f[nd], kN = k[nd];
     int c0 = t * NB;
     int kk = min(NB, kN - c0);
-    const int n1 = min(32, kk), n2 = kk - n1;
     float* F = pool + front_off[nd];
     const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) bad = false;
@@ -139,157 +121,156 @@ __global__ void __launch_bounds__(256) mf_diag_kernel(const int4* __restrict__ i
         }
     }
     __syncthreads();
-    if (warp == 0) warp_ldlt32(&A[0][0], NB + 1, n1, &X11[0][0], &bad);
-    __syncthreads();
-    if (n2 > 0) {
-        // W = A21 X11^T ; L21 = W D1^-1.  Thread: row r = tid >> 3, columns j = (tid & 7) + 8 q.
-        const int rr = tid >> 3, jj = tid & 7;
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            if (rr < n2)
-                for (int m = 0; m < 32; ++m) {
-                    float av = A[32 + rr][m];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] += av * X11[jj + 8 * q][m];   // X11 lower: zero above
-                }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) W[rr][jj + 8 * q] = acc[q];
-        }
+    for (int p0 = 0; p0 < kk; p0 += 16) {
+        const int np = min(16, kk - p0);
+        if (warp == 0) warp_ldlt16(&A[p0][p0], NB + 1, np, &bad);
         __syncthreads();
+        // panel: rows r >= p0+np solve  w L_pp^T = a  (w = L D), L(r, p0+j) = w_j / D_j
+        const int r = p0 + np + tid;
+        if (r < kk) {
+            float w[16];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int j = jj + 8 * q;
-            if (rr < n2 && j < n1) A[32 + rr][j] = W[rr][j] / A[j][j];
-        }
-        __syncthreads();
-        // A22 -= W L21^T (lower; upper entries of the block are never read)
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            if (rr < n2)
-                for (int j = 0; j < n1; ++j) {
-                    float wv = W[rr][j];
+            for (int j = 0; j < 16; ++j) {
+                float s = (j < np) ? A[r][p0 + j] : 0.f;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] += wv * A[32 + jj + 8 * q][j];
-                }
+                for (int m = 0; m < j; ++m) s -= w[m] * A[p0 + j][p0 + m];
+                w[j] = s;
+            }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int c = jj + 8 * q;
-                if (rr < n2 && c <= rr) A[32 + rr][32 + c] -= acc[q];
+            for (int j = 0; j < 16; ++j) {
+                Wp[r][j] = w[j];
+                if (j < np) A[r][p0 + j] = w[j] / A[p0 + j][p0 + j];
             }
         }
         __syncthreads();
-        if (warp == 0) warp_ldlt32(&A[32][32], NB + 1, n2, &X22[0][0], &bad);
-        __syncthreads();
-        // T = L21 X11 ; X21 = -X22 T
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            if (rr < n2)
-                for (int m = 0; m < n1; ++m) {
-                    float lv = A[32 + rr][m];
+        // rank-np update of the trailing lower part of the tile
+        const int t0 = p0 + np, nt = kk - t0;
+        for (int e = tid; e < nt * nt; e += 256) {
+            int rr = t0 + e / nt, cc = t0 + e % nt;
+            if (cc > rr) continue;
+            float s = 0.f;
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] += lv * X11[m][jj + 8 * q];   // X11[m][c] = 0 for c > m
-                }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) T[rr][jj + 8 * q] = acc[q];
-        }
-        __syncthreads();
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            if (rr < n2)
-                for (int m = 0; m <= rr; ++m) {
-                    float xv = X22[rr][m];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] += xv * T[m][jj + 8 * q];
-                }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) W[rr][jj + 8 * q] = -acc[q];   // X21
+            for (int j = 0; j < 16; ++j)
+                if (j < np) s += Wp[rr][j] * A[cc][p0 + j];
+            A[rr][cc] -= s;
         }
         __syncthreads();
     }
     if (tid == 0 && bad) atomicExch(status, 1);
-    // write back L / D (lower part of the tile), D, and the inverse
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
         int e = tid + 256 * q, c = e / NB, r = e % NB;
         if (r < kk && c <= r) F[(int64_t)(c0 + c) * fN + c0 + r] = A[r][c];
     }
     if (tid < kk) Dvec[own[nd] + c0 + tid] = A[tid][tid];
-    float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        int e = tid + 256 * q, r = e / NB, c = e % NB;
-        float v = 0.f;
-        if (r < 32 && c < 32) v = X11[r][c];
-        else if (r >= 32 && c < 32) v = (r - 32 < n2) ? W[r - 32][c] : 0.f;
-        else if (r >= 32 && c >= 32) v = X22[r - 32][c - 32];
-        Li[e] = (r < kk && c < kk) ? v : 0.f;
-    }
 }
 
-// Panel: W = A21 * Linv^T (rows r0..r0+63), L21 = W D^-1 written in place, W kept for the update.
-__global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
-                                                       const int* __restrict__ k, const int64_t* __restrict__ front_off,
-                                                       const int64_t* __restrict__ linv_off,
-                                                       const int64_t* __restrict__ ws_off, float* pool,
-                                                       const float* __restrict__ linv, float* ws) {
-    __shared__ float As[NB][NB + 1];   // As[m][rr] = A21[r0+rr][c0+m]
-    __shared__ float Ls[NB][NB + 1];   // Ls[m][j]  = Linv[j][m]
-    __shared__ float Dinv[NB];
+// Inverse of the unit lower factor of one diagonal tile (used only by the triangular solves):
+// launched once for every tile of every node after the factorisation.  Thread (ty, r) keeps row r
+// of X, columns ty + 4q, in registers; row j of X is final at step j and rows r > j subtract
+// L(r, j) X(j, :).
+__global__ void __launch_bounds__(256) mf_inverse_kernel(const int4* __restrict__ items, const int* __restrict__ f,
+                                                         const int* __restrict__ k,
+                                                         const int64_t* __restrict__ front_off,
+                                                         const int64_t* __restrict__ linv_off,
+                                                         const float* __restrict__ pool, float* linv) {
+    __shared__ float L[NB][NB + 1];
+    __shared__ float rowb[2][NB];
+    int4 it = items[blockIdx.x];
+    int nd = it.x, t = it.y;
+    int fN = f[nd], kN = k[nd];
+    int c0 = t * NB;
+    int kk = min(NB, kN - c0);
+    const float* F = pool + front_off[nd];
+    const int tid = threadIdx.x, r = tid & (NB - 1), ty = tid >> 6;
+    {
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int e = tid + 256 * q, c = e / NB, rr = e % NB;
+            v[q] = (rr < kk && c < rr) ? F[(int64_t)(c0 + c) * fN + c0 + rr] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            int e = tid + 256 * q;
+            L[e % NB][e / NB] = v[q];
+        }
+    }
+    float x[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) x[q] = (ty + 4 * q == r && r < kk) ? 1.f : 0.f;
+    __syncthreads();
+    for (int j = 0; j < kk; ++j) {
+        const int buf = j & 1;
+        if (r == j) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) rowb[buf][ty + 4 * q] = x[q];
+        }
+        __syncthreads();
+        if (r > j && r < kk) {
+            const float l = L[r][j];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                int c = ty + 4 * q;
+                if (c <= j) x[q] -= l * rowb[buf][c];
+            }
+        }
+    }
+    float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) Li[r * NB + ty + 4 * q] = (r < kk) ? x[q] : 0.f;
+}
+
+// Panel: one thread per row r of the block below the diagonal tile solves w L11^T = a by
+// substitution (L11 staged in shared memory), writes L21 = w D^-1 in place and keeps W = w for
+// the trailing update.
+constexpr int PANEL_THREADS = 64;
+__global__ void __launch_bounds__(PANEL_THREADS) mf_panel_kernel(const int4* __restrict__ items, int t,
+                                                                 const int* __restrict__ f, const int* __restrict__ k,
+                                                                 const int64_t* __restrict__ front_off,
+                                                                 const int64_t* __restrict__ ws_off, float* pool,
+                                                                 float* ws) {
+    __shared__ float Ls[NB][NB + 1];   // Ls[j][m] = L11(j, m), Ls[j][j] = D_j
     int4 it = items[blockIdx.x];
     int nd = it.x, r0 = it.y;
     int fN = f[nd], kN = k[nd];
     int c0 = t * NB;
     int kk = min(NB, kN - c0);
     float* F = pool + front_off[nd];
-    const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-    int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
+    const int tid = threadIdx.x;
     {
-        float va[16], vl[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            int m = lg + 4 * q;
-            va[q] = (m < kk && r0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + r0 + lt] : 0.f;
-            vl[q] = (m < kk && lt < kk) ? Li[lt * NB + m] : 0.f;
+        // stage L11 (64 x 64) with 64 threads: column-major walk, 64 loads per thread
+#pragma unroll 8
+        for (int q = 0; q < NB; ++q) {
+            int c = q, rr = tid;
+            Ls[rr][c] = (rr < kk && c <= rr) ? F[(int64_t)(c0 + c) * fN + c0 + rr] : 0.f;
         }
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            As[lg + 4 * q][lt] = va[q];
-            Ls[lg + 4 * q][lt] = vl[q];
-        }
-    }
-    if (threadIdx.x < NB) {
-        int j = threadIdx.x;
-        Dinv[j] = (j < kk) ? 1.f / F[(int64_t)(c0 + j) * fN + c0 + j] : 0.f;
     }
     __syncthreads();
-    float acc[4][4];
+    const int r = r0 + tid;
+    if (r >= fN) return;
+    float w[NB];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < NB; ++j) w[j] = (j < kk) ? F[(int64_t)(c0 + j) * fN + r] : 0.f;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[i][q] = 0.f;
-    for (int m = 0; m < kk; ++m) {
-        float a[4], b[4];
+    for (int j = 1; j < NB; ++j) {
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;   // four independent chains
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[m][tx + 16 * i];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) b[q] = Ls[m][ty + 16 * q];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(a[i], b[q], acc[i][q]);
+        for (int m = 0; m < j; ++m) {
+            const float v = w[m] * Ls[j][m];
+            if ((m & 3) == 0) s0 += v;
+            else if ((m & 3) == 1) s1 += v;
+            else if ((m & 3) == 2) s2 += v;
+            else s3 += v;
+        }
+        w[j] -= (s0 + s1) + (s2 + s3);
     }
     float* W = ws + ws_off[nd];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        int j = ty + 16 * q;
-        if (j >= kk) continue;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            int r = r0 + tx + 16 * i;
-            if (r >= fN) continue;
-            W[(int64_t)j * fN + r] = acc[i][q];
-            F[(int64_t)(c0 + j) * fN + r] = acc[i][q] * Dinv[j];
+    for (int j = 0; j < NB; ++j) {
+        if (j < kk) {
+            W[(int64_t)j * fN + r] = w[j];
+            F[(int64_t)(c0 + j) * fN + r] = w[j] / Ls[j][j];
         }
     }
 }
@@ -672,7 +653,12 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
         marks.push_back({L, 4, 0, 0, b, items.size()});
         for (int nd : ln) levels_[L].max_f = std::max(levels_[L].max_f, f[nd]);
     }
+    size_t inv_begin = items.size();
+    for (int i = 0; i < nnodes_; ++i)
+        for (int t = 0; t * NB < k[i]; ++t) items.push_back(make_int4(i, t, 0, 0));
+    size_t inv_end = items.size();
     items_.upload(items, stream_);
+    inv_items_ = MFWork{items_.get() + inv_begin, (int)(inv_end - inv_begin)};
     for (const Pending& m : marks) {
         MFWork w{items_.get() + m.begin, (int)(m.end - m.begin)};
         Level& lv = levels_[m.level];
@@ -783,16 +769,16 @@ void Multifrontal::factorize_launches(const float* d_vals) {
             if (st.diag.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
                 mf_diag_kernel<<<st.diag.count, 256, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
-                                                                   d_own_.get(), d_front_off_.get(), d_linv_off_.get(),
-                                                                   pool_.get(), linv_.get(), D_.get(), status_.get());
+                                                                   d_own_.get(), d_front_off_.get(), pool_.get(),
+                                                                   D_.get(), status_.get());
                 g_timer.end(stream_, 5, evk);
                 count_launch();
             }
             if (st.panel.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_panel_kernel<<<st.panel.count, 256, 0, stream_>>>(st.panel.items, st.t, d_f_.get(), d_k_.get(),
-                                                                     d_front_off_.get(), d_linv_off_.get(),
-                                                                     d_ws_off_.get(), pool_.get(), linv_.get(), ws_.get());
+                mf_panel_kernel<<<st.panel.count, PANEL_THREADS, 0, stream_>>>(st.panel.items, st.t, d_f_.get(),
+                                                                               d_k_.get(), d_front_off_.get(),
+                                                                               d_ws_off_.get(), pool_.get(), ws_.get());
                 g_timer.end(stream_, 6, evk);
                 count_launch();
             }
@@ -805,6 +791,12 @@ void Multifrontal::factorize_launches(const float* d_vals) {
                 count_launch();
             }
         }
+    }
+    if (inv_items_.count) {
+        mf_inverse_kernel<<<inv_items_.count, 256, 0, stream_>>>(inv_items_.items, d_f_.get(), d_k_.get(),
+                                                                 d_front_off_.get(), d_linv_off_.get(), pool_.get(),
+                                                                 linv_.get());
+        count_launch();
     }
     KL_CHECK_LAUNCH();
 }

@@ -79,6 +79,7 @@ private:
     struct Step { MFWork diag, panel, update; int t; };
     struct Level { MFWork ea[2]; std::vector<Step> steps; MFWork nodes; int max_f = 0; };
     std::vector<Level> levels_;
+    MFWork inv_items_;
     std::vector<std::vector<int>> level_nodes_;
     int max_f_ = 0;
 };
