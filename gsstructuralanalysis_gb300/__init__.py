@@ -79,6 +79,18 @@ SIGNATURES = {
     "klsa_alm_solution": (_c_int, [_c_vp, _c_vp, _c_vp]),
     "klsa_alm_info": (_c_int, [_c_vp, _c_vp]),
     "klsa_alm_history": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_mlp_create": (_c_int, [_c_int, _c_int, _c_int, _c_int, ctypes.c_uint64, ctypes.POINTER(_c_vp)]),
+    "klsa_mlp_destroy": (_c_int, [_c_vp]),
+    "klsa_mlp_num_params": (_c_i64, [_c_vp]),
+    "klsa_mlp_get_params": (_c_int, [_c_vp, _c_vp]),
+    "klsa_mlp_set_params": (_c_int, [_c_vp, _c_vp]),
+    "klsa_mlp_forward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
+    "klsa_mlp_loss_grad": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp]),
+    "klsa_mlp_train": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_int, ctypes.c_float, ctypes.c_uint64, _c_vp]),
+    "klsa_predictor_create": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_predictor_destroy": (_c_int, [_c_vp]),
+    "klsa_predictor_reset": (_c_int, [_c_vp]),
+    "klsa_alm_step_learned": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
     "klsa_profile_enable": (_c_int, [_c_int]),
@@ -433,3 +445,80 @@ def modal(problem: Problem, nev: int, shift: float = 0.0, options: dict | None =
     vecs = np.zeros((nev, problem.ndof)) if vectors else None
     st = _check(_lib.klsa_modal(problem.h, o.h, int(nev), float(shift), _ptr(vals), _ptr(vecs)))
     return st, vals, vecs
+
+
+class MLP:
+    """Device MLP (in -> h1 -> h2 -> out, GELU) with hand-written FP32 forward/backward/Adam."""
+
+    def __init__(self, n_in, n_h1, n_h2, n_out, seed=0):
+        L = load_library()
+        h = _c_vp()
+        _check(L.klsa_mlp_create(n_in, n_h1, n_h2, n_out, seed, ctypes.byref(h)))
+        self.h = h
+        self.shape = (n_in, n_h1, n_h2, n_out)
+        self.nparams = int(L.klsa_mlp_num_params(h))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_mlp_destroy(self.h)
+            self.h = None
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        _check(_lib.klsa_mlp_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(_lib.klsa_mlp_set_params(self.h, _ptr(p)))
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.shape[3]), dtype=np.float32)
+        _check(_lib.klsa_mlp_forward(self.h, _ptr(X), X.shape[0], _ptr(Y)))
+        return Y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        g = np.zeros(self.nparams, dtype=np.float32)
+        _check(_lib.klsa_mlp_loss_grad(self.h, _ptr(X), _ptr(T), X.shape[0], _ptr(loss), _ptr(g)))
+        return float(loss[0]), g
+
+    def train(self, X, T, epochs=200, batch=256, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        _check(_lib.klsa_mlp_train(self.h, _ptr(X), _ptr(T), X.shape[0], int(epochs), int(batch), float(lr), int(seed),
+                                   _ptr(loss)))
+        return float(loss[0])
+
+
+class Predictor:
+    """Learned arc-length predictor bound to one problem (modes: nmodes x ndof, public order)."""
+
+    def __init__(self, problem: Problem, net: MLP | None, modes, in_mean=None, in_std=None, out_mean=None,
+                 out_std=None):
+        self.problem = problem
+        self.net = net
+        modes = np.ascontiguousarray(modes, dtype=np.float64).reshape(-1, problem.ndof)
+        self._keep = [modes] + [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                                for a in (in_mean, in_std, out_mean, out_std)]
+        h = _c_vp()
+        _check(_lib.klsa_predictor_create(problem.h, net.h if net is not None else None, _ptr(modes), modes.shape[0],
+                                          *[_ptr(a) for a in self._keep[1:]], ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_predictor_destroy(self.h)
+            self.h = None
+
+    def reset(self):
+        _check(_lib.klsa_predictor_reset(self.h))
+
+    def step(self, alm, guess_max_iter=6):
+        used = np.zeros(1, dtype=np.int32)
+        st = _check(_lib.klsa_alm_step_learned(alm.h, self.h, int(guess_max_iter), _ptr(used)))
+        return st, bool(used[0])

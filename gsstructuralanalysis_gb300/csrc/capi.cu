@@ -7,6 +7,8 @@
 #include "../../include/klshell_gb300.h"
 #include "eigen.h"
 #include "linalg.h"
+#include "mlp.h"
+#include "predictor.h"
 #include "problem.h"
 #include "solvers.h"
 
@@ -37,6 +39,14 @@ struct klsa_alm {
     klsa_problem* prob;
     std::unique_ptr<ALMGPU> A;
     DevBuf<double> v;
+};
+struct klsa_mlp {
+    std::unique_ptr<MLP> net;
+};
+struct klsa_predictor {
+    klsa_problem* prob;
+    std::unique_ptr<LearnedPredictor> pred;
+    DevBuf<double> ug, u;
 };
 
 namespace {
@@ -475,6 +485,143 @@ int klsa_problem_stats(klsa_problem* prob, double* out) {
         out[6] = P.flops_tangent();
         out[7] = (double)P.tree.nodes.size();
         return KLSA_SUCCESS;
+    });
+}
+
+// ---- learned predictor ------------------------------------------------------------------------
+int klsa_mlp_create(int n_in, int n_h1, int n_h2, int n_out, uint64_t seed, klsa_mlp** out) {
+    if (!out || n_in < 1 || n_h1 < 1 || n_h2 < 1 || n_out < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        auto h = new klsa_mlp();
+        try {
+            h->net.reset(new MLP(n_in, n_h1, n_h2, n_out, seed));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_mlp_destroy(klsa_mlp* net) {
+    return guarded([&] {
+        delete net;
+        return KLSA_SUCCESS;
+    });
+}
+int64_t klsa_mlp_num_params(const klsa_mlp* net) { return net ? net->net->nparams : -1; }
+int klsa_mlp_get_params(klsa_mlp* net, float* params) {
+    if (!net || !params) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        MLP& m = *net->net;
+        KL_CUDA(cudaMemcpyAsync(params, m.params.get(), sizeof(float) * m.nparams, cudaMemcpyDeviceToHost, m.stream));
+        KL_CUDA(cudaStreamSynchronize(m.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_mlp_set_params(klsa_mlp* net, const float* params) {
+    if (!net || !params) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        MLP& m = *net->net;
+        KL_CUDA(cudaMemcpyAsync(m.params.get(), params, sizeof(float) * m.nparams, cudaMemcpyHostToDevice, m.stream));
+        m.m.zero(m.stream);
+        m.v.zero(m.stream);
+        m.t_adam = 0;
+        KL_CUDA(cudaStreamSynchronize(m.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_mlp_forward(klsa_mlp* net, const float* X, int batch, float* Y) {
+    if (!net || !X || !Y || batch < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        MLP& m = *net->net;
+        DevBuf<float> dX;
+        dX.upload(X, (size_t)batch * m.in, m.stream);
+        m.forward(dX.get(), batch);
+        KL_CUDA(cudaMemcpyAsync(Y, m.Y.get(), sizeof(float) * batch * m.out, cudaMemcpyDeviceToHost, m.stream));
+        KL_CUDA(cudaStreamSynchronize(m.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_mlp_loss_grad(klsa_mlp* net, const float* X, const float* T, int batch, float* loss, float* grad) {
+    if (!net || !X || !T || batch < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        MLP& m = *net->net;
+        DevBuf<float> dX, dT;
+        dX.upload(X, (size_t)batch * m.in, m.stream);
+        dT.upload(T, (size_t)batch * m.out, m.stream);
+        float l = m.loss_grad(dX.get(), dT.get(), batch);
+        if (loss) *loss = l;
+        if (grad) {
+            KL_CUDA(cudaMemcpyAsync(grad, m.grad.get(), sizeof(float) * m.nparams, cudaMemcpyDeviceToHost, m.stream));
+            KL_CUDA(cudaStreamSynchronize(m.stream));
+        }
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_mlp_train(klsa_mlp* net, const float* X, const float* T, int nsamples, int epochs, int batch, float lr,
+                   uint64_t seed, float* final_loss) {
+    if (!net || !X || !T || nsamples < 1 || epochs < 0 || batch < 1) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        float l = net->net->train(X, T, nsamples, epochs, batch, lr, seed);
+        if (final_loss) *final_loss = l;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_predictor_create(klsa_problem* prob, klsa_mlp* net, const double* modes, int nmodes, const double* in_mean,
+                          const double* in_std, const double* out_mean, const double* out_std, klsa_predictor** out) {
+    if (!prob || !out || nmodes < 0 || (nmodes > 0 && !modes)) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        auto h = new klsa_predictor();
+        h->prob = prob;
+        try {
+            h->pred.reset(new LearnedPredictor(*prob->P, net ? net->net.get() : nullptr, modes, nmodes, in_mean, in_std,
+                                               out_mean, out_std));
+            h->ug.alloc(prob->P->nfree);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_predictor_destroy(klsa_predictor* pr) {
+    return guarded([&] {
+        delete pr;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_predictor_reset(klsa_predictor* pr) {
+    if (!pr) return KLSA_INVALID_ARGUMENT;
+    pr->pred->reset();
+    return KLSA_SUCCESS;
+}
+int klsa_alm_step_learned(klsa_alm* a, klsa_predictor* pr, int guess_max_iter, int* used_guess) {
+    if (!a || !pr || pr->prob != a->prob) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ALMGPU& A = *a->A;
+        LearnedPredictor& L = *pr->pred;
+        if (used_guess) *used_guess = 0;
+        if (L.count == 0) L.push(A.U(), A.L());
+        double Lg = 0.0;
+        if (L.guess(pr->ug.get(), &Lg)) {
+            A.set_initial_guess(pr->ug.get(), Lg);
+            A.set_guess_place(true);
+            int saved = A.max_iter();
+            A.set_max_iter(guess_max_iter > 1 ? guess_max_iter : saved);
+            int st = A.step();
+            A.set_max_iter(saved);
+            A.set_guess_place(false);
+            if (st == KLSA_SUCCESS) {
+                L.push(A.U(), A.L());
+                if (used_guess) *used_guess = 1;
+                return KLSA_SUCCESS;
+            }
+        }
+        int st = A.step();   // plain tangent predictor (the state is unchanged by a failed attempt)
+        if (st == KLSA_SUCCESS) L.push(A.U(), A.L());
+        return st;
     });
 }
 

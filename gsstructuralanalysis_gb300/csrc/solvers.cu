@@ -336,6 +336,15 @@ void ALMGPU::predictor() {
 
 void ALMGPU::predictor_guess() {
     cudaStream_t s = P_.stream;
+    if (guess_place_) {
+        // start the corrector at the guess: no tangent at U, no u_t solve
+        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), DU_.get(), n_, s);
+        KL_CUDA(cudaMemcpyAsync(dU_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        DL_ = dL_ = Lguess_ - L_;
+        ut_valid_ = false;
+        has_guess_ = false;
+        return;
+    }
     compute_jacobian();
     if (method_ == Crisfield) {
         // gsALMCrisfield.hpp:167-191

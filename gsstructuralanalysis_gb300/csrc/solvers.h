@@ -93,6 +93,13 @@ public:
     double phi() const { return phi_; }
     bool converged() const { return converged_; }
     LinearSolver& lin() { return *S_; }
+    // Guess placement (no reference counterpart): when set, predictor_guess starts the corrector
+    // from the guessed point itself (DU = Uguess - U, DL = Lguess - L) instead of using the guess
+    // only for the direction of the tangent predictor (gsALMCrisfield.hpp:167-191).
+    void set_guess_place(bool on) { guess_place_ = on; }
+    int max_iter() const { return maxIt_; }
+    void set_max_iter(int it) { maxIt_ = it; }
+    Problem& problem() { return P_; }
     // per-step work counters
     int n_jac = 0, n_res = 0, n_solve = 0;
 
@@ -137,6 +144,7 @@ private:
     double eta_ = 1.0;
     double residueF_ = 0, residueU_ = 0, basisF_ = 0, basisU_ = 0;
     bool ut_valid_ = false;
+    bool guess_place_ = false;
 };
 
 }  // namespace klsa

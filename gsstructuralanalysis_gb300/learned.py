@@ -1,0 +1,136 @@
+"""Learned arc-length predictor: data generation, reduced modal basis, training.
+
+Pipeline (all arc-length paths are computed by the library's own GPU arc-length solver):
+  1. imperfection modes: the first buckling modes of the perfect shell (GPU Lanczos);
+  2. training paths: Crisfield arc-length runs on shells with seeded random imperfections
+     (sum of the modes, each scaled to unit max |w|, amplitudes ~ N(0, (a t)^2));
+  3. reduced modal basis Phi: proper orthogonal decomposition of the path increments (method of
+     snapshots), orthonormal, nm modes;
+  4. dataset: features of the last four points (q = Phi^T U and lambda, newest absolute, older
+     relative) -> target = correction of the cubic extrapolation inside the modal subspace;
+  5. the MLP (4(nm+1) -> 256 -> 256 -> nm+1, GELU) is trained on the GPU by the library's
+     forward/backward/Adam kernels.
+At run time the predictor proposes U_ext + Phi dq, L_ext + dL as the corrector's start and the
+plain tangent predictor takes over whenever that start does not converge.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import problems as P
+
+EXTRAP = np.array([4.0, -6.0, 4.0, -1.0])   # cubic extrapolation weights of P_k, P_{k-1}, P_{k-2}, P_{k-3}
+
+
+def buckling_modes(G, prob, nmodes=5, shift=-0.5, scaling=1000.0):
+    """First buckling modes (full layout), sign fixed so that the largest |w| entry is positive."""
+    gp = G.Problem(prob)
+    st, vals, vecs = G.buckling(gp, nmodes, shift=shift, scaling=scaling)
+    modes = []
+    for v in vecs:
+        full = np.zeros(prob.ndof_full)
+        full[prob.free_index()] = v
+        w = full[2 * prob.ncp:]
+        if w[np.argmax(np.abs(w))] < 0:
+            full = -full
+        modes.append(full)
+    gp.close()
+    return modes, vals, st
+
+
+def imperfect_problem(prob, modes, seed, amp=0.01):
+    a = np.random.default_rng(seed).normal(0.0, amp * prob.t, size=len(modes))
+    return P.add_imperfection(prob, modes, a)
+
+
+def step_with_retry(alm, G, retries=6):
+    for _ in range(retries):
+        if alm.step() == G.SUCCESS:
+            return True
+        alm.reduceLength(0.5)
+    return False
+
+
+def generate_path(G, prob, alm_opts, nsteps):
+    """Converged points (U, lambda) of one Crisfield path, including the undeformed start."""
+    gp = G.Problem(prob)
+    alm = G.ALMCrisfield(gp, alm_opts)
+    alm.initialize()
+    Us = [np.zeros(gp.ndof)]
+    Ls = [0.0]
+    for _ in range(nsteps):
+        if not step_with_retry(alm, G):
+            break
+        Us.append(alm.solutionU())
+        Ls.append(alm.solutionL())
+    gp.close()
+    return np.array(Us), np.array(Ls)
+
+
+def pod_modes(paths, nm):
+    """Orthonormal POD basis of the path increments (method of snapshots)."""
+    S = np.concatenate([np.diff(U, axis=0) for U, _ in paths], axis=0)   # (N, n)
+    C = S @ S.T
+    w, V = np.linalg.eigh(C)
+    order = np.argsort(w)[::-1][:nm]
+    Phi = (V[:, order].T @ S) / np.sqrt(np.maximum(w[order], 1e-300))[:, None]
+    Q, _ = np.linalg.qr(Phi.T)
+    return Q.T.copy()
+
+
+def features_targets(paths, Phi):
+    nm = Phi.shape[0]
+    X, T = [], []
+    for U, L in paths:
+        q = U @ Phi.T                     # (N, nm)
+        for k in range(3, len(U) - 1):
+            f = []
+            for b in range(4):
+                if b == 0:
+                    f.extend(q[k]); f.append(L[k])
+                else:
+                    f.extend(q[k - b] - q[k]); f.append(L[k - b] - L[k])
+            qe = sum(EXTRAP[b] * q[k - b] for b in range(4))
+            le = sum(EXTRAP[b] * L[k - b] for b in range(4))
+            X.append(f)
+            T.append(np.concatenate([q[k + 1] - qe, [L[k + 1] - le]]))
+    return np.array(X), np.array(T)
+
+
+@dataclass
+class TrainedPredictor:
+    Phi: np.ndarray
+    net: object
+    in_mean: np.ndarray
+    in_std: np.ndarray
+    out_mean: np.ndarray
+    out_std: np.ndarray
+    train_loss: float
+    nsamples: int
+    seconds: dict
+
+
+def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0):
+    t0 = time.perf_counter()
+    Phi = pod_modes(paths, nm)
+    X, T = features_targets(paths, Phi)
+    mu, sd = X.mean(0), X.std(0) + 1e-30
+    omu, osd = T.mean(0), T.std(0) + 1e-30
+    sd[sd < 1e-12 * np.abs(mu).max()] = 1.0
+    Xn = (X - mu) / sd
+    Tn = (T - omu) / osd
+    t1 = time.perf_counter()
+    net = G.MLP(X.shape[1], hidden, hidden, T.shape[1], seed=seed)
+    loss = net.train(Xn, Tn, epochs=epochs, batch=min(batch, len(X)), lr=lr, seed=seed)
+    t2 = time.perf_counter()
+    return TrainedPredictor(Phi, net, mu, sd, omu, osd, loss, len(X), {"prep": t1 - t0, "train": t2 - t1})
+
+
+def make_predictor(G, gp, tp: TrainedPredictor | None, Phi=None, use_net=True):
+    if tp is None:
+        return G.Predictor(gp, None, np.zeros((0, gp.ndof)))
+    return G.Predictor(gp, tp.net if use_net else None, tp.Phi if Phi is None else Phi, tp.in_mean, tp.in_std,
+                       tp.out_mean, tp.out_std)

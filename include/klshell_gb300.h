@@ -147,6 +147,36 @@ int klsa_alm_info(klsa_alm* a, double* out);
 /* Copies the previous converged point (Uprev, Lprev) and the last step (DeltaUold, DeltaLold). */
 int klsa_alm_history(klsa_alm* a, double* Uprev, double* Lprev, double* DUold, double* DLold);
 
+/* ---- learned predictor (no counterpart in the reference; it feeds setInitialGuess,
+ * gsALMSolvers/gsALMBase.h:184) ---------------------------------------------------------- */
+typedef struct klsa_mlp klsa_mlp;
+typedef struct klsa_predictor klsa_predictor;
+/* Fully connected n_in -> n_h1 -> n_h2 -> n_out network, GELU, FP32, Glorot init from seed. */
+int klsa_mlp_create(int n_in, int n_h1, int n_h2, int n_out, uint64_t seed, klsa_mlp** out);
+int klsa_mlp_destroy(klsa_mlp* net);
+int64_t klsa_mlp_num_params(const klsa_mlp* net);
+int klsa_mlp_get_params(klsa_mlp* net, float* params);       /* W1, b1, W2, b2, W3, b3 (row-major) */
+int klsa_mlp_set_params(klsa_mlp* net, const float* params);
+int klsa_mlp_forward(klsa_mlp* net, const float* X, int batch, float* Y);
+/* MSE loss 1/(2 batch n_out) sum (Y - T)^2 and its gradient (layout of the parameters). */
+int klsa_mlp_loss_grad(klsa_mlp* net, const float* X, const float* T, int batch, float* loss, float* grad);
+/* Mini-batch Adam (cosine schedule) on the device; final_loss = mean loss of the last epoch. */
+int klsa_mlp_train(klsa_mlp* net, const float* X, const float* T, int nsamples, int epochs, int batch, float lr,
+                   uint64_t seed, float* final_loss);
+/* modes: nmodes x ndof orthonormal basis (public order).  Standardisation vectors of the
+ * 4 (nmodes + 1) features and nmodes + 1 targets (NULL: identity).  net may be NULL (plain cubic
+ * extrapolation of the last four points). */
+int klsa_predictor_create(klsa_problem* prob, klsa_mlp* net, const double* modes, int nmodes,
+                          const double* in_mean, const double* in_std, const double* out_mean,
+                          const double* out_std, klsa_predictor** out);
+int klsa_predictor_destroy(klsa_predictor* pr);
+int klsa_predictor_reset(klsa_predictor* pr);
+/* One arc-length point with the learned guess placed as the corrector's start (at most
+ * guess_max_iter iterations); on failure the step is redone with the plain tangent predictor.
+ * Keeps the predictor's history of converged points.  used_guess (may be NULL) = 1 if the
+ * learned guess converged. */
+int klsa_alm_step_learned(klsa_alm* a, klsa_predictor* pr, int guess_max_iter, int* used_guess);
+
 /* ---- eigen problems (gsEigenSolvers/gsEigenProblemBase.hpp:152-215) ------------------- */
 /* Buckling (gsBucklingSolver.h:127-149): u_L = K_L^-1 (scaling F), B = K(u_L) - K_L,
  * eigenpairs of K_L v = lambda B v by shift-invert Lanczos about ``shift``.

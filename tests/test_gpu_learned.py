@@ -1,0 +1,79 @@
+"""GPU tests of the learned predictor: MLP gradients vs the FP64 NumPy reference, training, and
+arc-length paths with the learned guess (same points as the plain path, fewer tangents)."""
+import numpy as np
+import pytest
+
+from gsstructuralanalysis_gb300 import learned, problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_gradient_matches_reference(lib):
+    import gsstructuralanalysis_gb300 as G
+    import mlp_ref
+    shape = (12, 16, 8, 5)
+    net = G.MLP(*shape, seed=3)
+    rng = np.random.default_rng(4)
+    p = (0.3 * rng.standard_normal(net.nparams)).astype(np.float32)
+    net.set_params(p)
+    X = rng.standard_normal((17, 12)).astype(np.float32)
+    T = rng.standard_normal((17, 5)).astype(np.float32)
+    Y = net.forward(X)
+    Yr, _ = mlp_ref.forward(p.astype(np.float64), shape, X.astype(np.float64))
+    assert np.abs(Y - Yr).max() <= 1e-5 * max(1.0, np.abs(Yr).max())
+    loss, g = net.loss_grad(X, T)
+    lr_, gr = mlp_ref.loss_grad(p.astype(np.float64), shape, X, T)
+    assert abs(loss - lr_) <= 1e-5 * lr_
+    assert np.linalg.norm(g - gr) <= 1e-4 * np.linalg.norm(gr)
+
+
+def test_mlp_training_fits_a_smooth_map(lib):
+    import gsstructuralanalysis_gb300 as G
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((512, 8)).astype(np.float32)
+    W = rng.standard_normal((8, 3))
+    T = (np.tanh(X @ W) + 0.1 * X[:, :3]).astype(np.float32)
+    net = G.MLP(8, 64, 64, 3, seed=1)
+    l0, _ = net.loss_grad(X, T)
+    loss = net.train(X, T, epochs=300, batch=64, lr=3e-3, seed=2)
+    assert loss < 0.05 * l0
+
+
+def _paths(G, seeds, modes, opts, nsteps):
+    base = P.cylindrical_panel(m=12, p=2, load=1.0)
+    return [learned.generate_path(G, learned.imperfect_problem(base, modes, s), opts, nsteps) for s in seeds]
+
+
+def test_learned_predictor_same_path_fewer_tangents(lib):
+    import gsstructuralanalysis_gb300 as G
+    opts = dict(Length=0.0025, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25)
+    base = P.cylindrical_panel(m=12, p=2, load=1.0)
+    modes, _, st = learned.buckling_modes(G, base, nmodes=3, shift=-0.5)
+    assert st == 0
+    paths = _paths(G, [0, 1, 2], modes, opts, 40)
+    tp = learned.train(G, paths, nm=16, hidden=64, epochs=300, batch=64, lr=2e-3)
+    test_prob = learned.imperfect_problem(base, modes, 1000)
+    results = {}
+    for mode in ("plain", "extrapolation", "learned"):
+        gp = G.Problem(test_prob)
+        alm = G.ALMCrisfield(gp, opts)
+        alm.initialize()
+        pred = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
+        pts, used = [], 0
+        for _ in range(30):
+            if pred is None:
+                assert alm.step() == 0
+            else:
+                st, u = pred.step(alm, guess_max_iter=6)
+                assert st == 0
+                used += u
+            pts.append((alm.solutionU(), alm.solutionL()))
+        results[mode] = (pts, alm.info()["n_jac"], used)
+    Up, Lp = results["plain"][0][-1]
+    for mode in ("extrapolation", "learned"):
+        U, L = results[mode][0][-1]
+        assert np.linalg.norm(U - Up) <= 1e-5 * np.linalg.norm(Up)
+        assert abs(L - Lp) <= 1e-5 * abs(Lp)
+        assert results[mode][2] >= 20                     # the guess is used on most steps
+        assert results[mode][1] < results["plain"][1]     # fewer tangent assemblies/factorisations
+    print({k: (v[1], v[2]) for k, v in results.items()})
