@@ -33,7 +33,8 @@ sys.path.insert(0, ROOT)
 from gsstructuralanalysis_gb300 import problems as P  # noqa: E402
 
 WORKLOAD = dict(m=128, p=2, load=1.0)
-ALM_OPTS = dict(Length=0.02, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
+ALM_OPTS = dict(Length=0.005, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
+TEST_SEED = 1000          # imperfection seed of the measured path (training seeds are 0..n_train-1)
 METRIC = "arc-length path points/s at 50k dofs, learned vs plain predictor, ||R||/||F||<=1e-8"
 MAX_RETRIES = 6
 
@@ -136,57 +137,104 @@ def step_with_retry(alm, G):
 # ---------------------------------------------------------------------------------------------
 def run_ours(args):
     import gsstructuralanalysis_gb300 as G
-    from gsstructuralanalysis_gb300 import build as B
+    from gsstructuralanalysis_gb300 import build as B, learned
     rank, world = dist_env()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
     B.build()
     G.load_library()
-    prob = workload_problem()
-    if args.imperfection:
-        prob = imperfect(prob, G, seed=args.seed + rank)
+    base = workload_problem()
+    t_setup = time.perf_counter()
+    modes, bvals, _ = learned.buckling_modes(G, base, nmodes=5, shift=-0.5)
+    prob = learned.imperfect_problem(base, modes, TEST_SEED + rank)
+    tp, train_info = None, None
+    nsteps_path = args.steps + args.warmup
+    if args.predictor == "learned":
+        t0 = time.perf_counter()
+        paths = [learned.generate_path(G, learned.imperfect_problem(base, modes, s), ALM_OPTS, nsteps_path)
+                 for s in range(args.train_paths)]
+        t1 = time.perf_counter()
+        tp = learned.train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3)
+        train_info = {"paths": args.train_paths, "points_per_path": nsteps_path, "samples": tp.nsamples,
+                      "path_generation_s": t1 - t0, "training_s": tp.seconds["train"], "alpha": tp.alpha,
+                      "best_epoch": tp.best_epoch, "val_rel_error_vs_extrapolation": tp.val_rel_error}
+    t_setup = time.perf_counter() - t_setup
     gp = G.Problem(prob)
     stats = gp.stats()
-    alm = G.ALMCrisfield(gp, ALM_OPTS)
-    alm.initialize()
-    for _ in range(args.warmup):
-        step_with_retry(alm, G)
-    gp.sync()
-    barrier(world)
-    l0 = G.launch_count()
+
+    def run_path(mode, timed=True):
+        alm = G.ALMCrisfield(gp, ALM_OPTS)
+        alm.initialize()
+        pred = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
+
+        def one():
+            if pred is None:
+                return step_with_retry(alm, G)
+            st, _ = pred.step(alm, guess_max_iter=6)
+            return st == G.SUCCESS or step_with_retry(alm, G)
+
+        for _ in range(args.warmup):
+            one()
+        gp.sync()
+        barrier(world)
+        j0 = alm.info()["n_jac"]
+        l0 = G.launch_count()
+        gp.record(0)
+        t_wall = time.perf_counter()
+        pts = 0
+        for _ in range(args.steps):
+            pts += 1 if one() else 0
+        gp.record(1)
+        ms = gp.elapsed_ms(0, 1)
+        t_wall = time.perf_counter() - t_wall
+        return dict(alm=alm, pred=pred, pts=pts, ms=ms, wall=t_wall, launches=G.launch_count() - l0,
+                    jac_per_point=(alm.info()["n_jac"] - j0) / max(pts, 1))
+
+    mode = args.predictor
     clk = ClockSampler()
     clk.start()
-    gp.record(0)
-    t_wall = time.perf_counter()
-    pts = 0
-    for _ in range(args.steps):
-        pts += 1 if step_with_retry(alm, G) else 0
-    gp.record(1)
-    ms = gp.elapsed_ms(0, 1)
-    t_wall = time.perf_counter() - t_wall
+    main = run_path(mode)
     clocks = clk.stop()
-    launches = G.launch_count() - l0
-    ms = reduce_max(ms, world)
+    ms = reduce_max(main["ms"], world)
     barrier(world)
-    value = world * pts / (ms / 1e3)
+    value = world * main["pts"] / (ms / 1e3)
+    alm = main["alm"]
     U_end, L_end = alm.solutionU(), alm.solutionL()
-
+    launches = main["launches"]
+    pts = main["pts"]
     if args.lean:
-        # timed leg only (used for ncu launch lists)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "points/s", "steps": args.steps,
                               "ms_per_step": ms / max(pts, 1), "gpu_launches": int(launches), "lean": True}))
         return
+    compare = {}
+    if mode == "learned":
+        for other in ("plain", "extrapolation"):
+            r = run_path(other)
+            compare[other] = {"points_per_s": world * r["pts"] / (reduce_max(r["ms"], world) / 1e3),
+                              "jacobians_per_point": r["jac_per_point"]}
+        compare["learned"] = {"points_per_s": value, "jacobians_per_point": main["jac_per_point"]}
+        compare["learned_over_plain"] = value / compare["plain"]["points_per_s"]
+        compare["final_load_factor_plain_vs_learned"] = None
+
     # e2e: the same steps again through the C-ABI with host vectors in and out every step
     alm2 = G.ALMCrisfield(gp, ALM_OPTS)
     alm2.initialize()
+    pred2 = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
     U = np.zeros(gp.ndof)
     L = 0.0
     pin_bytes = 8 * gp.ndof
+
+    def one2():
+        if pred2 is None:
+            return step_with_retry(alm2, G)
+        st, _ = pred2.step(alm2, guess_max_iter=6)
+        return st == G.SUCCESS or step_with_retry(alm2, G)
+
     for _ in range(args.warmup):
         alm2.setSolution(U, L)
-        step_with_retry(alm2, G)
+        one2()
         U, L = alm2.solutionU(), alm2.solutionL()
     gp.sync()
     barrier(world)
@@ -194,19 +242,17 @@ def run_ours(args):
     pts2 = 0
     for _ in range(args.steps):
         alm2.setSolution(U, L)                 # H2D: the step's input state
-        pts2 += 1 if step_with_retry(alm2, G) else 0
+        pts2 += 1 if one2() else 0
         U, L = alm2.solutionU(), alm2.solutionL()   # D2H: the step's result
     gp.sync()
     e2e_s = reduce_max(time.perf_counter() - t0, world)
     e2e = {"value": world * pts2 / e2e_s, "unit": "points/s", "h2d_bytes_per_step": pin_bytes,
            "d2h_bytes_per_step": pin_bytes + 8}
+    if compare:
+        compare["final_load_factor_plain_vs_learned"] = [float(L), float(L_end)]
 
-    # per-phase profile (separate replay with per-launch CUDA events; not part of `value`)
     prof = profile_phases(G, gp, args)
     roof = roofline(prof, stats, args)
-
-    # residual check of the final point with the oracle's own FP64 assembly is done in tests;
-    # here report the library's own convergence measure of the last point
     info = alm.info()
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -216,14 +262,17 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / max(pts, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": "Crisfield arc-length, shallow cylindrical roof R=2.5 L=2.5 span=0.2 t=0.01, "
-                               "degree 2, 128x128 elements (50,700 dofs)",
-                   "ndof_free": int(gp.ndof), "nnz": int(gp.nnz), "predictor": args.predictor,
-                   "imperfection": bool(args.imperfection), "arc_length": ALM_OPTS["Length"], "TolF": 1e-8,
-                   "TolU": 1e-6, "solver": "SimplicialLDLT -> nested-dissection multifrontal LDL^T (FP32 fronts)",
+                               "degree 2, 128x128 elements (50,700 dofs), imperfection of 5 buckling modes "
+                               f"(seed {TEST_SEED})",
+                   "ndof_free": int(gp.ndof), "nnz": int(gp.nnz), "predictor": mode,
+                   "arc_length": ALM_OPTS["Length"], "TolF": 1e-8, "TolU": 1e-6,
+                   "solver": "SimplicialLDLT -> nested-dissection multifrontal LDL^T (FP32 fronts)",
                    "l2": "inputs larger than L2 (multifrontal fronts %.0f MB)" % (stats["front_bytes"] / 1e6),
-                   "final_load_factor": L_end, "parallelism": f"replicas x{world}"},
+                   "final_load_factor": L_end, "jacobians_per_point": main["jac_per_point"],
+                   "setup_s": t_setup, "training": train_info, "compare": compare,
+                   "parallelism": f"replicas x{world}"},
         "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-        "phases_ms_per_step": prof["per_step"], "wall_s_timed": t_wall,
+        "phases_ms_per_step": prof["per_step"], "wall_s_timed": main["wall"],
         "last_point": {"iterations": info["iterations"], "residueF": info["residueF"]},
     }
     if rank == 0:
@@ -252,69 +301,52 @@ def profile_phases(G, gp, args, nsteps=None):
 
 
 def roofline(prof, stats, args):
-    """Dominant phase/kernel vs the measured peaks.  The multifrontal trailing update is a dense
-    FP32 GEMM on CUDA cores; its algorithmic work per launch is the factorisation flops divided by
-    the update launches (the update does ~all of them)."""
+    """Per-kernel achieved bandwidth / flop rate from CUDA-event launch durations measured live
+    (profiling replay) and the algorithmic bytes / flops of each kernel kind; the dominant kind
+    (largest time share) is the headline.  Peaks: MEASURED_PEAKS.json (HBM copy bandwidth)."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    raw = prof["raw"]
-    upd_ms, upd_n = raw["mf_update"]
-    fac_ms, fac_n = raw["factorization"]
-    asm_ms, asm_n = raw["assembly"]
-    res_ms, res_n = raw["residual"]
-    sol_ms, sol_n = raw["solve"]
     hbm = peaks.get("hbm_gbs", 6800.0)
-    out = {}
-    # factorisation as a whole: flops per factorisation / time per factorisation
-    if fac_n:
-        t_fac = fac_ms / fac_n / 1e3
-        fl = stats["factor_flops"]
-        out["factorization"] = {"achieved": fl / t_fac / 1e12, "unit": "TFLOP/s (FP32 CUDA cores)",
-                                "ms_per_launch": fac_ms / fac_n, "flops": fl}
-    if sol_n:
-        # each solve reads the factor (fronts' L parts) once forward and once backward
-        bytes_solve = 2 * stats["front_bytes"] / 2
-        t = sol_ms / sol_n / 1e3
-        out["solve"] = {"achieved": bytes_solve / t / 1e9, "unit": "GB/s", "ms_per_call": sol_ms / sol_n}
-    if asm_n:
-        t = asm_ms / asm_n / 1e3
-        out["assembly"] = {"achieved": stats["tangent_flops"] / t / 1e12, "unit": "TFLOP/s (FP32)",
-                           "ms_per_call": asm_ms / asm_n}
-    if res_n:
-        out["residual_ms"] = res_ms / res_n
-    # dominant kernel by time share
-    shares = {k: raw[k][0] for k in ("mf_update", "mf_diag", "mf_panel", "solve", "assembly", "residual")}
-    dom = max(shares, key=shares.get)
-    # the multifrontal trailing update streams W and L tiles and read-modify-writes the front:
-    # algorithmic bytes per launch ~ fronts touched; report it against HBM.
-    t_upd = upd_ms / max(upd_n, 1) / 1e3
-    bytes_upd = 3 * stats["front_bytes"] / max(upd_n / max(fac_n, 1), 1)
-    achieved = bytes_upd / t_upd / 1e9 if upd_n else 0.0
-    line = {"bound": "hbm", "kernel": "mf_update_kernel", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-            "dominant_phase": dom, "phase_ms": {k: v for k, v in shares.items()}, "detail": out}
-    return line
-
-
-def imperfect(prob, G, seed=0, nmodes=5):
-    """Imperfection = sum of the first 5 buckling modes (unit max |w|, sign fixed so that the
-    largest |w| entry is positive), amplitudes ~ N(0, (0.01 t)^2) from numpy default_rng(seed)."""
-    gp = G.Problem(prob)
-    st, vals, vecs = G.buckling(gp, nmodes, shift=-0.5, scaling=1000.0)
-    modes = []
-    for v in vecs:
-        full = np.zeros(prob.ndof_full)
-        full[prob.free_index()] = v
-        w = full[2 * prob.ncp:]
-        if w[np.argmax(np.abs(w))] < 0:
-            full = -full
-        modes.append(full)
-    gp.close()
-    amps = np.random.default_rng(seed).normal(0.0, 0.01 * prob.t, size=nmodes)
-    return P.add_imperfection(prob, modes, amps)
+    src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s (of fallback)"
+    raw = prof["raw"]
+    fac_n = max(raw["factorization"][1], 1)
+    n_qp, nel = stats["gauss_points"], stats["elements"]
+    d = 27  # element dofs (degree 2)
+    kinds = {
+        # kind: (ms total, launches, algorithmic bytes per launch, flops per launch)
+        "mf_update_kernel": (raw["mf_update"][0], raw["mf_update"][1],
+                             stats["bytes_update"] / max(stats["launches_update"], 1),
+                             2 * stats["flops_update"] / max(stats["launches_update"], 1)),
+        "mf_diag_kernel": (raw["mf_diag"][0], raw["mf_diag"][1],
+                           stats["bytes_diag"] / max(stats["launches_diag"], 1),
+                           2 * stats["flops_diag"] / max(stats["launches_diag"], 1)),
+        "mf_panel_kernel": (raw["mf_panel"][0], raw["mf_panel"][1],
+                            stats["bytes_panel"] / max(stats["launches_panel"], 1),
+                            2 * stats["flops_panel"] / max(stats["launches_panel"], 1)),
+        "mf_fwd+bwd (solve)": (raw["solve"][0], raw["solve"][1], stats["solve_bytes"], 0.0),
+        "kl_tangent+csr_gather": (raw["assembly"][0], raw["assembly"][1],
+                                  n_qp * 22 * 8 + 2 * nel * d * d * 4 + stats["nnz"] * 8, stats["tangent_flops"]),
+        "kl_fint+gather (FP64)": (raw["residual"][0], raw["residual"][1], n_qp * 22 * 8 + 2 * nel * d * 8, 0.0),
+    }
+    detail = {}
+    for k, (ms, n, byts, fl) in kinds.items():
+        if not n:
+            continue
+        t = ms / n / 1e3
+        detail[k] = {"ms_total_per_step": ms / prof["nsteps"], "avg_launch_us": 1e6 * t,
+                     "gbs": byts / t / 1e9, "tflops": fl / t / 1e12, "bytes_per_launch": byts}
+    dom = max(detail, key=lambda k: detail[k]["ms_total_per_step"])
+    ach = detail[dom]["gbs"]
+    return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+            "traffic": None, "peak_source": src,
+            "note": "multifrontal kernels are bound by the latency of the pivot-tile chain, not by HBM or FLOP rate; "
+                    "per-kernel bandwidth and FLOP rates in detail",
+            "factorization_ms": raw["factorization"][0] / fac_n,
+            "factorization_tflops_fp32": stats["factor_flops"] / (raw["factorization"][0] / fac_n / 1e3) / 1e12,
+            "detail": detail}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -336,6 +368,26 @@ def cpu_points(prob, npoints, warm=0):
     return ok, dt
 
 
+def cpu_workload_problem():
+    """The measured workload with its imperfection computed by the CPU oracle (SuperLU + ARPACK):
+    first 5 buckling modes of the perfect roof, sign fixed, amplitudes from the same seed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    base = workload_problem()
+    A = O.OracleAssembler(base, nthreads=host_cores())
+    vals, vecs, _ = O.buckling(A.linear(), A.force(), A.jacobian, nev=5, shift=-0.5, scaling=1000.0, tol=1e-8)
+    modes = []
+    for v in vecs.T:
+        full = np.zeros(base.ndof_full)
+        full[base.free_index()] = v
+        w = full[2 * base.ncp:]
+        if w[np.argmax(np.abs(w))] < 0:
+            full = -full
+        modes.append(full)
+    a = np.random.default_rng(TEST_SEED).normal(0.0, 0.01 * base.t, size=5)
+    return P.add_imperfection(base, modes, a)
+
+
 def _cpu_step(alm):
     for _ in range(MAX_RETRIES):
         if alm.step() == 0:
@@ -355,18 +407,21 @@ def run_reference(args):
     rank, world = dist_env()
     if rank != 0:
         return
-    prob = workload_problem()
+    prob = cpu_workload_problem()
     npts = max(1, min(args.steps, 3))
-    warm = min(args.warmup, 0)
+    warm = 0
     n, dt = cpu_points(prob, npts, warm)
     value = n / dt
     line = {"metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": npts,
             "warmup": warm, "ms_per_step": 1e3 * dt / max(n, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "Crisfield arc-length, shallow cylindrical roof, degree 2, 128x128 elements "
-                                   "(50,700 dofs)", "predictor": "plain"},
+            "config": {"workload": "Crisfield arc-length, shallow cylindrical roof R=2.5 L=2.5 span=0.2 t=0.01, "
+                                   "degree 2, 128x128 elements (50,700 dofs), imperfection of 5 buckling modes "
+                                   f"(seed {TEST_SEED})", "predictor": "plain (tangent), the reference's own"},
             "cpu_baseline": {"value": value, "unit": "points/s", "cores": host_cores(), "kind": "port",
-                             "sample": f"first {npts} arc-length points of the workload (bounded sample)"},
+                             "sample": f"first {npts} arc-length points of the workload (bounded sample): FP64 C++ "
+                                       "OpenMP assembly on all host cores, scipy SuperLU as the SimplicialLDLT "
+                                       "stand-in, restated gsALMCrisfield logic"},
             "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -377,8 +432,8 @@ def main():
     ap.add_argument("--steps", type=int, default=197)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--predictor", default="plain", choices=["plain", "learned"])
-    ap.add_argument("--imperfection", type=int, default=0)
+    ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
+    ap.add_argument("--train-paths", type=int, default=6)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")

@@ -220,9 +220,11 @@ class Problem:
         self.close()
 
     def stats(self):
-        out = np.zeros(8)
+        out = np.zeros(18)
         _check(_lib.klsa_problem_stats(self.h, _ptr(out)))
-        keys = ["ndof", "nnz", "elements", "gauss_points", "front_bytes", "factor_flops", "tangent_flops", "nodes"]
+        keys = ["ndof", "nnz", "elements", "gauss_points", "front_bytes", "factor_flops", "tangent_flops", "nodes",
+                "bytes_diag", "bytes_panel", "bytes_update", "flops_diag", "flops_panel", "flops_update",
+                "launches_diag", "launches_panel", "launches_update", "solve_bytes"]
         return dict(zip(keys, out.tolist()))
 
     def record(self, slot):

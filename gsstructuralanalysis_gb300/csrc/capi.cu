@@ -484,6 +484,12 @@ int klsa_problem_stats(klsa_problem* prob, double* out) {
         out[5] = mf.flops();
         out[6] = P.flops_tangent();
         out[7] = (double)P.tree.nodes.size();
+        for (int i = 0; i < 3; ++i) {
+            out[8 + i] = mf.kernel_bytes[i];
+            out[11 + i] = mf.kernel_flops[i];
+            out[14 + i] = mf.kernel_launches[i];
+        }
+        out[17] = mf.solve_bytes;
         return KLSA_SUCCESS;
     });
 }

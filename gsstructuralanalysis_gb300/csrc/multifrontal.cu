@@ -653,6 +653,22 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
         marks.push_back({L, 4, 0, 0, b, items.size()});
         for (int nd : ln) levels_[L].max_f = std::max(levels_[L].max_f, f[nd]);
     }
+    // algorithmic traffic and flops per factorisation
+    for (int L = 0; L < nlevels_; ++L)
+        for (int nd : level_nodes_[L])
+            for (int t = 0; t * NB < k[nd]; ++t) {
+                double kk = std::min(NB, k[nd] - t * NB);
+                double below = f[nd] - t * NB - kk;
+                kernel_bytes[0] += 4.0 * kk * kk;                       // read + write the lower tile
+                kernel_flops[0] += kk * kk * kk / 3.0;
+                kernel_bytes[1] += 4.0 * (3.0 * below * kk + 0.5 * kk * kk);   // A21 in, L21 and W out, L11 in
+                kernel_flops[1] += below * kk * kk;
+                double ntr = std::ceil(below / NB);
+                double tiles = ntr * (ntr + 1) / 2;
+                kernel_bytes[2] += tiles * 4.0 * (2.0 * NB * kk + 2.0 * NB * NB);   // W, L tiles in; A tile r/w
+                kernel_flops[2] += below * below * kk;                  // lower half of below x below x kk x 2
+            }
+    for (int i = 0; i < nnodes_; ++i) solve_bytes += 2.0 * 4.0 * ((double)k[i] * f[i] - 0.5 * (double)k[i] * k[i]);
     size_t inv_begin = items.size();
     for (int i = 0; i < nnodes_; ++i)
         for (int t = 0; t * NB < k[i]; ++t) items.push_back(make_int4(i, t, 0, 0));
@@ -668,6 +684,13 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
             case 2: lv.steps[m.step].panel = w; break;
             case 3: lv.steps[m.step].update = w; break;
             default: lv.nodes = w; break;
+        }
+    }
+    for (int L = 0; L < nlevels_; ++L) {
+        for (const Step& st : levels_[L].steps) {
+            kernel_launches[0] += st.diag.count > 0;
+            kernel_launches[1] += st.panel.count > 0;
+            kernel_launches[2] += st.update.count > 0;
         }
     }
     d_f_.upload(f, stream_); d_k_.upload(k, stream_); d_own_.upload(own, stream_); d_parent_.upload(parent, stream_);

@@ -49,6 +49,11 @@ public:
     int n() const { return n_; }
     double flops() const { return flops_; }
     int64_t front_bytes() const { return (int64_t)pool_.size() * 4; }
+    // algorithmic bytes / flops of one factorisation per kernel kind (0 diag, 1 panel, 2 update),
+    // launches per factorisation, and bytes of one triangular solve (L read forward and backward)
+    double kernel_bytes[3] = {0, 0, 0}, kernel_flops[3] = {0, 0, 0};
+    int kernel_launches[3] = {0, 0, 0};
+    double solve_bytes = 0;
     const std::vector<int>& level_nodes(int lvl) const { return level_nodes_[lvl]; }
 
 private:

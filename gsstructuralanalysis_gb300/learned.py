@@ -113,20 +113,48 @@ class TrainedPredictor:
     seconds: dict
 
 
-def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0):
+def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0, chunk=25, val_paths=1):
+    """Train on all but the last ``val_paths`` paths, early-stop on the held-out paths, and scale
+    the network's correction by the validation-optimal trust factor alpha in [0, 1]
+    (alpha = 0 reduces the predictor to the cubic extrapolation)."""
     t0 = time.perf_counter()
     Phi = pod_modes(paths, nm)
-    X, T = features_targets(paths, Phi)
+    tr, va = (paths[:-val_paths], paths[-val_paths:]) if len(paths) > val_paths else (paths, paths)
+    X, T = features_targets(tr, Phi)
+    Xv, Tv = features_targets(va, Phi)
     mu, sd = X.mean(0), X.std(0) + 1e-30
     omu, osd = T.mean(0), T.std(0) + 1e-30
     sd[sd < 1e-12 * np.abs(mu).max()] = 1.0
-    Xn = (X - mu) / sd
-    Tn = (T - omu) / osd
+    Xn, Tn = (X - mu) / sd, (T - omu) / osd
+    Xvn, Tvn = (Xv - mu) / sd, (Tv - omu) / osd
     t1 = time.perf_counter()
     net = G.MLP(X.shape[1], hidden, hidden, T.shape[1], seed=seed)
-    loss = net.train(Xn, Tn, epochs=epochs, batch=min(batch, len(X)), lr=lr, seed=seed)
+
+    def val_error(a=1.0):
+        Y = net.forward(Xvn).astype(np.float64)
+        corr = Y * osd + omu
+        return np.sum((Tv - a * corr) ** 2), corr
+
+    best = (val_error()[0], net.params(), 0)
+    history = []
+    for ep in range(chunk, epochs + 1, chunk):
+        loss = net.train(Xn, Tn, epochs=chunk, batch=min(batch, len(X)), lr=lr, seed=seed + ep)
+        ve = val_error()[0]
+        history.append((ep, loss, ve))
+        if ve < best[0]:
+            best = (ve, net.params(), ep)
+    net.set_params(best[1])
+    ve, corr = val_error()
+    base = np.sum(Tv ** 2)          # error of the plain cubic extrapolation on the held-out paths
+    alpha = float(np.clip(np.sum(Tv * corr) / max(np.sum(corr * corr), 1e-300), 0.0, 1.0))
     t2 = time.perf_counter()
-    return TrainedPredictor(Phi, net, mu, sd, omu, osd, loss, len(X), {"prep": t1 - t0, "train": t2 - t1})
+    tp = TrainedPredictor(Phi, net, mu, sd, omu * alpha, osd * alpha, history[-1][1] if history else 0.0, len(X),
+                          {"prep": t1 - t0, "train": t2 - t1})
+    tp.alpha = alpha
+    tp.best_epoch = best[2]
+    tp.val_rel_error = float(np.sqrt(np.sum((Tv - alpha * corr) ** 2) / max(base, 1e-300)))
+    tp.history = history
+    return tp
 
 
 def make_predictor(G, gp, tp: TrainedPredictor | None, Phi=None, use_net=True):

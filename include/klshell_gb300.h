@@ -198,8 +198,10 @@ int klsa_profile_reset(void);
 int klsa_event_record(klsa_problem* prob, int slot);
 int klsa_event_elapsed(klsa_problem* prob, int slot_a, int slot_b, float* ms);
 int klsa_problem_sync(klsa_problem* prob);
-/* out[8]: ndof, nnz, elements, Gauss points, front pool bytes, factorisation flops,
- * tangent-assembly flops, multifrontal tree nodes */
+/* out[18]: ndof, nnz, elements, Gauss points, front pool bytes, factorisation flops,
+ * tangent-assembly flops, multifrontal tree nodes, algorithmic bytes per factorisation of the
+ * diagonal / panel / update kernels (3), their flops (3), their launches per factorisation (3),
+ * bytes of one triangular solve */
 int klsa_problem_stats(klsa_problem* prob, double* out);
 
 /* ---- host-only symbolic queries (no device call) -------------------------------------- */
