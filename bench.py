@@ -35,6 +35,7 @@ from gsstructuralanalysis_gb300 import problems as P  # noqa: E402
 WORKLOAD = dict(m=128, p=2, load=1.0)
 ALM_OPTS = dict(Length=0.005, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
 TEST_SEED = 1000          # imperfection seed of the measured path (training seeds are 0..n_train-1)
+COARSE_M = 16             # imperfection modes: buckling modes of the 16x16 roof, transferred exactly
 METRIC = "arc-length path points/s at 50k dofs, learned vs plain predictor, ||R||/||F||<=1e-8"
 MAX_RETRIES = 6
 
@@ -146,7 +147,7 @@ def run_ours(args):
     G.load_library()
     base = workload_problem()
     t_setup = time.perf_counter()
-    modes, bvals, _ = learned.buckling_modes(G, base, nmodes=5, shift=-0.5)
+    modes, bvals, _ = learned.buckling_modes(G, base, nmodes=5, shift=-0.5, coarse=workload_problem(m=COARSE_M))
     prob = learned.imperfect_problem(base, modes, TEST_SEED + rank)
     tp, train_info = None, None
     nsteps_path = args.steps + args.warmup
@@ -369,21 +370,17 @@ def cpu_points(prob, npoints, warm=0):
 
 
 def cpu_workload_problem():
-    """The measured workload with its imperfection computed by the CPU oracle (SuperLU + ARPACK):
-    first 5 buckling modes of the perfect roof, sign fixed, amplitudes from the same seed."""
+    """The measured workload with its imperfection computed by the CPU oracle: first 5 buckling
+    modes of the 16x16 roof (SuperLU + ARPACK), sign fixed, transferred exactly into the 128x128
+    spline space, amplitudes from the same seed."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
+    from gsstructuralanalysis_gb300 import learned
     base = workload_problem()
-    A = O.OracleAssembler(base, nthreads=host_cores())
-    vals, vecs, _ = O.buckling(A.linear(), A.force(), A.jacobian, nev=5, shift=-0.5, scaling=1000.0, tol=1e-8)
-    modes = []
-    for v in vecs.T:
-        full = np.zeros(base.ndof_full)
-        full[base.free_index()] = v
-        w = full[2 * base.ncp:]
-        if w[np.argmax(np.abs(w))] < 0:
-            full = -full
-        modes.append(full)
+    coarse = workload_problem(m=COARSE_M)
+    A = O.OracleAssembler(coarse, nthreads=host_cores())
+    vals, vecs, _ = O.buckling(A.linear(), A.force(), A.jacobian, nev=5, shift=-0.5, scaling=1000.0, tol=1e-10)
+    modes = [P.transfer_field(coarse, m, base) for m in learned.sign_fixed_modes(coarse, vecs.T)]
     a = np.random.default_rng(TEST_SEED).normal(0.0, 0.01 * base.t, size=5)
     return P.add_imperfection(base, modes, a)
 

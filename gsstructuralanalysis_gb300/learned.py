@@ -25,10 +25,8 @@ from . import problems as P
 EXTRAP = np.array([4.0, -6.0, 4.0, -1.0])   # cubic extrapolation weights of P_k, P_{k-1}, P_{k-2}, P_{k-3}
 
 
-def buckling_modes(G, prob, nmodes=5, shift=-0.5, scaling=1000.0):
-    """First buckling modes (full layout), sign fixed so that the largest |w| entry is positive."""
-    gp = G.Problem(prob)
-    st, vals, vecs = G.buckling(gp, nmodes, shift=shift, scaling=scaling)
+def sign_fixed_modes(prob, vecs):
+    """Free-dof eigenvectors -> full-layout modes, sign fixed so that the largest |w| is positive."""
     modes = []
     for v in vecs:
         full = np.zeros(prob.ndof_full)
@@ -37,7 +35,20 @@ def buckling_modes(G, prob, nmodes=5, shift=-0.5, scaling=1000.0):
         if w[np.argmax(np.abs(w))] < 0:
             full = -full
         modes.append(full)
+    return modes
+
+
+def buckling_modes(G, prob, nmodes=5, shift=-0.5, scaling=1000.0, coarse=None):
+    """First buckling modes of ``prob`` (GPU Lanczos, Buckling mode).  With ``coarse`` (a nested
+    coarser patch of the same surface) the modes are computed there and transferred exactly into
+    the spline space of ``prob``."""
+    src = coarse if coarse is not None else prob
+    gp = G.Problem(src)
+    st, vals, vecs = G.buckling(gp, nmodes, shift=shift, scaling=scaling)
     gp.close()
+    modes = sign_fixed_modes(src, vecs)
+    if coarse is not None:
+        modes = [P.transfer_field(coarse, m, prob) for m in modes]
     return modes, vals, st
 
 

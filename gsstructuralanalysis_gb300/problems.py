@@ -195,3 +195,54 @@ def add_imperfection(prob: PatchProblem, modes_full: np.ndarray, amplitudes: np.
         if s > 0:
             d += a * ph / s
     return prob.with_ctrl(prob.ctrl + d)
+
+
+def bspline_basis_matrix(knots: np.ndarray, p: int, pts: np.ndarray) -> np.ndarray:
+    """B[k, i] = N_{i,p}(pts[k]) on an open knot vector (Cox-de Boor, right end included)."""
+    knots = np.asarray(knots, dtype=np.float64)
+    n = len(knots) - p - 1
+    pts = np.asarray(pts, dtype=np.float64)
+    B = np.zeros((len(pts), n))
+    for k, u in enumerate(pts):
+        N = np.zeros(len(knots) - 1)
+        if u >= knots[-1]:
+            N[n - 1] = 1.0
+        else:
+            j = np.searchsorted(knots, u, side="right") - 1
+            N[j] = 1.0
+        for d in range(1, p + 1):
+            M = np.zeros(len(knots) - 1 - d)
+            for i in range(len(M)):
+                a = knots[i + d] - knots[i]
+                b = knots[i + d + 1] - knots[i + 1]
+                v = 0.0
+                if a > 0:
+                    v += (u - knots[i]) / a * N[i]
+                if b > 0:
+                    v += (knots[i + d + 1] - u) / b * N[i + 1]
+                M[i] = v
+            N = M
+        B[k] = N[:n]
+    return B
+
+
+def greville(knots: np.ndarray, p: int) -> np.ndarray:
+    n = len(knots) - p - 1
+    return np.array([np.mean(knots[i + 1:i + p + 1]) for i in range(n)])
+
+
+def transfer_field(coarse: PatchProblem, field_full: np.ndarray, fine: PatchProblem) -> np.ndarray:
+    """Exact transfer of a spline field (full component-blocked layout) from ``coarse`` to the
+    nested spline space of ``fine`` (same degree, fine knots a superset of the coarse ones):
+    interpolation at the fine Greville points of the coarse field."""
+    T = []
+    for Uc, Uf in ((coarse.knots1, fine.knots1), (coarse.knots2, fine.knots2)):
+        g = greville(Uf, fine.p)
+        Af = bspline_basis_matrix(Uf, fine.p, g)
+        Ac = bspline_basis_matrix(Uc, coarse.p, g)
+        T.append(np.linalg.solve(Af, Ac))
+    out = np.zeros(3 * fine.ncp)
+    for c in range(3):
+        C = field_full[c * coarse.ncp:(c + 1) * coarse.ncp].reshape(coarse.n2, coarse.n1)
+        out[c * fine.ncp:(c + 1) * fine.ncp] = (T[1] @ C @ T[0].T).ravel()
+    return out

@@ -242,16 +242,19 @@ void element_kl(const Patch& P, const Elem& e, const double* ufull, int ncp, boo
             Vec3 A1, A2;
             eval_qp(P, e, xi1, xi2, gw[q1] * gw[q2] * jac, q, A1, A2);
             // reference and deformed derivatives
+            // reference derivatives from X, displacement derivatives from u (kept separate so that
+            // small displacements are not lost in X + u)
             Vec3 X11{0, 0, 0}, X22{0, 0, 0}, X12{0, 0, 0};
-            Vec3 a1{0, 0, 0}, a2{0, 0, 0}, x11{0, 0, 0}, x22{0, 0, 0}, x12{0, 0, 0};
+            Vec3 d1{0, 0, 0}, d2{0, 0, 0}, d11{0, 0, 0}, d22{0, 0, 0}, d12{0, 0, 0};
             for (int k = 0; k < nb; ++k) {
                 int A = q.cp[k];
                 Vec3 XA{P.X[3 * A], P.X[3 * A + 1], P.X[3 * A + 2]};
-                Vec3 xA = XA + Vec3{ufull[A], ufull[ncp + A], ufull[2 * ncp + A]};
+                Vec3 uA{ufull[A], ufull[ncp + A], ufull[2 * ncp + A]};
                 X11 = X11 + q.N11[k] * XA; X22 = X22 + q.N22[k] * XA; X12 = X12 + q.N12[k] * XA;
-                a1 = a1 + q.N1[k] * xA; a2 = a2 + q.N2[k] * xA;
-                x11 = x11 + q.N11[k] * xA; x22 = x22 + q.N22[k] * xA; x12 = x12 + q.N12[k] * xA;
+                d1 = d1 + q.N1[k] * uA; d2 = d2 + q.N2[k] * uA;
+                d11 = d11 + q.N11[k] * uA; d22 = d22 + q.N22[k] * uA; d12 = d12 + q.N12[k] * uA;
             }
+            Vec3 a1 = A1 + d1, a2 = A2 + d2, x11 = X11 + d11, x22 = X22 + d22, x12 = X12 + d12;
             Vec3 At = cross(A1, A2);
             double J0 = std::sqrt(dot(At, At));
             Vec3 A3 = (1.0 / J0) * At;
@@ -262,7 +265,11 @@ void element_kl(const Patch& P, const Elem& e, const double* ufull, int ncp, boo
             double am[3] = {dot(a1, a1), dot(a2, a2), dot(a1, a2)};
             double Bc[3] = {dot(X11, A3), dot(X22, A3), dot(X12, A3)};
             double bc[3] = {dot(x11, a3), dot(x22, a3), dot(x12, a3)};
-            double eps[3] = {0.5 * (am[0] - Am[0]), 0.5 * (am[1] - Am[1]), am[2] - Am[2]};
+            // membrane strain from the displacement gradient d_a = a_a - A_a (the same value as
+            // 1/2 (a_ab - A_ab) without the cancellation of two nearly equal metrics)
+            double eps[3] = {dot(A1, d1) + 0.5 * dot(d1, d1), dot(A2, d2) + 0.5 * dot(d2, d2),
+                             dot(A1, d2) + dot(d1, A2) + dot(d1, d2)};
+            (void)am;
             double kap[3] = {Bc[0] - bc[0], Bc[1] - bc[1], 2.0 * (Bc[2] - bc[2])};
             double C[3][3];
             material(P, Am[0], Am[2], Am[1], C);
