@@ -44,6 +44,17 @@ def workload_problem(m=None, p=None):
     return P.cylindrical_panel(m=m or WORKLOAD["m"], p=p or WORKLOAD["p"], load=WORKLOAD["load"])
 
 
+def profiler_range(on):
+    """Mark the timed region for a profiler started with --profile-from-start off (driver API
+    cuProfilerStart/Stop on the current context); a no-op when the driver library is absent."""
+    try:
+        import ctypes
+        cu = ctypes.CDLL("libcuda.so.1")
+        (cu.cuProfilerStart if on else cu.cuProfilerStop)()
+    except OSError:
+        pass
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
@@ -181,12 +192,14 @@ def run_ours(args):
         barrier(world)
         j0 = alm.info()["n_jac"]
         l0 = G.launch_count()
+        profiler_range(True)
         gp.record(0)
         t_wall = time.perf_counter()
         pts = 0
         for _ in range(args.steps):
             pts += 1 if one() else 0
         gp.record(1)
+        profiler_range(False)
         ms = gp.elapsed_ms(0, 1)
         t_wall = time.perf_counter() - t_wall
         return dict(alm=alm, pred=pred, pts=pts, ms=ms, wall=t_wall, launches=G.launch_count() - l0,
@@ -379,7 +392,7 @@ def cpu_workload_problem():
     base = workload_problem()
     coarse = workload_problem(m=COARSE_M)
     A = O.OracleAssembler(coarse, nthreads=host_cores())
-    vals, vecs, _ = O.buckling(A.linear(), A.force(), A.jacobian, nev=5, shift=-0.5, scaling=1000.0, tol=1e-10)
+    vals, vecs, _ = O.buckling_dense(A.linear(), A.force(), A.jacobian, nev=5, shift=-0.5, scaling=1000.0)
     modes = [P.transfer_field(coarse, m, base) for m in learned.sign_fixed_modes(coarse, vecs.T)]
     a = np.random.default_rng(TEST_SEED).normal(0.0, 0.01 * base.t, size=5)
     return P.add_imperfection(base, modes, a)
@@ -423,6 +436,364 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------------------------
+# batched uneven Newton solves (256 panels)
+# ---------------------------------------------------------------------------------------------
+BATCH_N = 256
+BATCH_SEED = 5000
+BATCH_OPTS = {"tol": 1e-8, "maxIt": 25}
+BATCH_METRIC = "batched Newton solves/s, 256 uneven roof panels (16..96 elements, degree 2/3), |R|/|R0|<=1e-8"
+
+
+def batch_spec(i, seed=BATCH_SEED):
+    """Instance i: elements per direction ~ U{16..96}, degree ~ U{2,3}, thickness log-uniform in
+    [0.005, 0.05], imperfection amplitudes ~ N(0, (0.01 t)^2) on 5 buckling modes."""
+    rng = np.random.default_rng(seed + i)
+    m = int(rng.integers(16, 97))
+    p = int(rng.choice([2, 3]))
+    t = float(np.exp(rng.uniform(np.log(0.005), np.log(0.05))))
+    amps = rng.normal(0.0, 0.01 * t, size=5)
+    return m, p, t, amps
+
+
+def batch_instance(G, i, seed=BATCH_SEED):
+    """Imperfect roof with its point load at 50% of the peak load.  Peak load: the lowest linear
+    buckling load under the downward central point load of the perfect roof, from a 16x16-element
+    patch of the same degree and thickness (the imperfection modes come from the same analysis,
+    interpolated into the instance's spline space at its Greville points, exact when nested)."""
+    from gsstructuralanalysis_gb300 import learned
+    m, p, t, amps = batch_spec(i, seed)
+    base = P.cylindrical_panel(m=m, p=p, t=t)
+    coarse = P.cylindrical_panel(m=16, p=p, t=t)
+    scale = 2560.0 * (t / 0.01) ** 2.5          # keeps the wanted eigenvalues near the shift -0.5
+    modes, vals, _ = learned.buckling_modes(G, base, nmodes=5, shift=-0.5, scaling=scale, coarse=coarse)
+    neg = [abs(v) for v in vals if v < 0]
+    peak = scale * (min(neg) if neg else abs(vals[0]))
+    prob = P.add_imperfection(base, modes, amps)
+    prob.point_loads = np.array([[0.5, 0.5, 0.0, 0.0, -0.5 * peak]])
+    prob.name = f"batch-{i}-p{p}-m{m}"
+    return prob, {"m": m, "p": p, "t": t, "peak_load": peak}
+
+
+def run_batched(args):
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    rank, world = dist_env()
+    B.build()
+    G.load_library()
+    n = args.batch
+    t0 = time.perf_counter()
+    made = [batch_instance(G, rank * n + i) for i in range(n)]
+    probs = [pm[0] for pm in made]
+    t_inst = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bp = G.BatchedProblem(probs)
+    info = bp.info()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tune = bp.autotune()
+    t_tune = time.perf_counter() - t0
+    bn = G.BatchedNewton(bp, BATCH_OPTS)
+    for _ in range(args.warmup):
+        bn.reset()
+        bn.solve()
+    bp.sync()
+    barrier(world)
+    l0 = G.launch_count()
+    clk = ClockSampler()
+    clk.start()
+    profiler_range(True)
+    bp.record(0)
+    statuses = []
+    for _ in range(args.steps):
+        bn.reset()
+        statuses.append(bn.solve())
+    bp.record(1)
+    profiler_range(False)
+    clocks = clk.stop()
+    ms = reduce_max(bp.elapsed_ms(0, 1), world)
+    launches = G.launch_count() - l0
+    st, its = bn.results()
+    value = world * n * args.steps / (ms / 1e3)
+    # end to end: the same solves through the public API with every solution read back to host
+    U = None
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bn.reset()
+        bn.solve()
+        U = [bn.solution(i) for i in range(n)]
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    d2h = 8 * sum(len(u) for u in U)
+    # size-independent parity: the oracle's FP64 residual at the GPU solutions of a few instances
+    check = []
+    if rank == 0 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        order = np.argsort([pm[1]["m"] for pm in made])
+        for i in list(order[:2]) + list(order[-1:]):
+            A = O.OracleAssembler(probs[i], nthreads=host_cores())
+            R = A.residual(U[i])
+            check.append({"instance": int(i), "m": made[i][1]["m"], "p": made[i][1]["p"],
+                          "rel_residual_oracle": float(np.linalg.norm(R) / np.linalg.norm(A.force()))})
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = batch_cpu_baseline(probs, made)
+    hist = {int(k): int(v) for k, v in zip(*np.unique(its, return_counts=True))}
+    line = {
+        "metric": BATCH_METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{n} independent imperfect roofs per GPU, one Newton solve each from zero to 50% "
+                               "of the linear buckling load (seeded per instance)",
+                   "instances": n, "ndof_free_total": int(info["ndof"]), "nnz_total": int(info["nnz"]),
+                   "front_pool_GB": info["front_bytes"] / 1e9, "options": BATCH_OPTS,
+                   "degree_counts": {str(p): sum(1 for pm in made if pm[1]["p"] == p) for p in (2, 3)},
+                   "newton_iterations_histogram": hist, "all_converged": bool((st == 0).all()),
+                   "setup_s": {"instances_and_imperfection_modes": t_inst, "batch_symbolic": t_batch,
+                               "autotune": t_tune},
+                   "autotuned_blocks_per_sm": tune_summary(tune),
+                   "l2": "inputs larger than L2 (front pool %.1f GB)" % (info["front_bytes"] / 1e9),
+                   "parallelism": f"instances sharded, x{world}"},
+        "e2e": {"value": world * n * args.steps / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu, "oracle_residual_check": check,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_batched_reference(args):
+    """The oracle's CPU Newton on a bounded sample of the batch (its two smallest instances)."""
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    rank, world = dist_env()
+    if rank != 0:
+        return
+    B.build()
+    G.load_library()
+    made = [batch_instance(G, i) for i in range(args.batch)]
+    probs = [pm[0] for pm in made]
+    cpu = batch_cpu_baseline(probs, made)
+    line = {"metric": BATCH_METRIC, "value": cpu["value"], "unit": "solves/s", "n_gpus": world, "steps": 2,
+            "warmup": 0, "ms_per_step": 1e3 / cpu["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{args.batch} imperfect roofs; bounded sample: {cpu['sample']}"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def tune_summary(log):
+    best = {}
+    for kind, deg, bps, ms in log:
+        key = ("tangent" if kind == 0 else "internal_force") + f"_p{int(deg)}"
+        if key not in best or ms < best[key][1]:
+            best[key] = (int(bps), float(ms))
+    return {k: {"blocks_per_sm": v[0], "ms": v[1]} for k, v in best.items()}
+
+
+def batch_cpu_baseline(probs, made):
+    """The oracle's gsStaticNewton restatement (FP64 C++ OpenMP assembly, SuperLU) on the two
+    smallest instances: a bounded sample, reported per solve."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    order = np.argsort([pm[1]["m"] for pm in made])[:2]
+    t0 = time.perf_counter()
+    for i in order:
+        A = O.OracleAssembler(probs[i], nthreads=host_cores())
+        ref = O.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(BATCH_OPTS))
+        ref.solve()
+    dt = time.perf_counter() - t0
+    return {"value": len(order) / dt, "unit": "solves/s", "cores": host_cores(), "kind": "port",
+            "sample": "the two smallest instances (%s elements per direction): FP64 C++ OpenMP assembly, scipy "
+                      "SuperLU, restated gsStaticNewton; the batch's average instance is larger"
+                      % ", ".join(str(made[i][1]["m"]) for i in order)}
+
+
+# ---------------------------------------------------------------------------------------------
+# static Newton load ramp (degree 3, 64x64 elements)
+# ---------------------------------------------------------------------------------------------
+RAMP_M, RAMP_P, RAMP_LOAD, RAMP_STEPS = 64, 3, 30000.0, 10
+RAMP_OPTS = {"Solver": "SimplicialLDLT", "tol": 1e-8, "maxIt": 50}
+RAMP_METRIC = "static Newton load steps/s, degree-3 64x64 roof (13,467 dofs), 10-step ramp through snap-through"
+
+
+def centre_deflection(prob, U):
+    full = np.zeros(prob.ndof_full)
+    full[prob.free_index()] = U
+    b1 = P.bspline_basis_matrix(prob.knots1, prob.p, [0.5])[0]
+    b2 = P.bspline_basis_matrix(prob.knots2, prob.p, [0.5])[0]
+    return float(b2 @ full[2 * prob.ncp:].reshape(prob.n2, prob.n1) @ b1)
+
+
+def run_ramp(args):
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    rank, world = dist_env()
+    B.build()
+    G.load_library()
+    prob = P.cylindrical_panel(m=RAMP_M, p=RAMP_P, load=RAMP_LOAD)
+    gp = G.Problem(prob)
+
+    def ramp():
+        st = G.StaticNewton(gp, RAMP_OPTS)
+        its = []
+        for k in range(1, RAMP_STEPS + 1):
+            st.setLoad(k / RAMP_STEPS)
+            if st.solve() != G.SUCCESS:
+                raise RuntimeError(f"load step {k} did not converge")
+            its.append(st.iterations())
+        return st, its
+
+    for _ in range(args.warmup):
+        ramp()
+    gp.sync()
+    barrier(world)
+    l0 = G.launch_count()
+    clk = ClockSampler()
+    clk.start()
+    profiler_range(True)
+    gp.record(0)
+    for _ in range(args.steps):
+        st, its = ramp()
+    gp.record(1)
+    profiler_range(False)
+    clocks = clk.stop()
+    ms = reduce_max(gp.elapsed_ms(0, 1), world)
+    launches = G.launch_count() - l0
+    U = st.solution()
+    value = world * RAMP_STEPS * args.steps / (ms / 1e3)
+    # end to end through the public API: the ramp with the solution read back after every step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        stn = G.StaticNewton(gp, RAMP_OPTS)
+        for k in range(1, RAMP_STEPS + 1):
+            stn.setLoad(k / RAMP_STEPS)
+            stn.solve()
+            stn.solution()
+    e2e_s = reduce_max(time.perf_counter() - t0, world)
+    cpu, parity = None, None
+    if rank == 0 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        A = O.OracleAssembler(prob, nthreads=host_cores())
+        F = A.force()
+        R = F - A.fint(U)
+        parity = {"rel_residual_oracle_final_step": float(np.linalg.norm(R) / np.linalg.norm(F))}
+        t0 = time.perf_counter()
+        ref = O.StaticNewton(A.linear(), F / RAMP_STEPS, A.jacobian, lambda x: F / RAMP_STEPS - A.fint(x),
+                             dict(tol=1e-8, maxIt=50))
+        ref.solve()
+        dt = time.perf_counter() - t0
+        cpu = {"value": 1.0 / dt, "unit": "load steps/s", "cores": host_cores(), "kind": "port",
+               "sample": "the first load step (from zero to 10% of the peak load, past the limit point): FP64 C++ "
+                         "OpenMP assembly, scipy SuperLU, restated gsStaticNewton"}
+    line = {
+        "metric": RAMP_METRIC, "value": value, "unit": "load steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"shallow roof degree {RAMP_P}, {RAMP_M}x{RAMP_M} elements, central point load ramped "
+                               f"to {RAMP_LOAD:g} N in {RAMP_STEPS} steps; one step = the whole ramp",
+                   "ndof_free": gp.ndof, "options": RAMP_OPTS, "newton_iterations_per_load_step": its,
+                   "centre_deflection_over_t": -centre_deflection(prob, U) / prob.t,
+                   "l2": "fronts %.0f MB + CSR; working set near L2 size" % (gp.stats()["front_bytes"] / 1e6)},
+        "e2e": {"value": world * RAMP_STEPS * args.steps / e2e_s, "unit": "load steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8 * gp.ndof * RAMP_STEPS},
+        "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu, "parity": parity,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------------------------
+# linear buckling + modal (degree 3, 256x256 elements)
+# ---------------------------------------------------------------------------------------------
+EIG_M, EIG_P, EIG_NEV = 256, 3, 20
+EIG_SCALING = 5.0e4     # reference load of the buckling analysis: the lowest buckling factors near -1.2
+EIG_METRIC = "buckling + modal eigenpairs/s, degree-3 256x256 roof (201,243 dofs), 20 + 20 pairs"
+
+
+def run_eigen(args):
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    import scipy.sparse as sp
+    rank, world = dist_env()
+    B.build()
+    G.load_library()
+    prob = P.axial_panel(m=args.eig_m, p=EIG_P)
+    gp = G.Problem(prob)
+    bopt = {"tolerance": 1e-10, "ncvFac": 3}
+
+    def both():
+        st1, bv, bvec = G.buckling(gp, EIG_NEV, shift=args.eig_shift, scaling=EIG_SCALING, options=bopt)
+        st2, mv, mvec = G.modal(gp, EIG_NEV, shift=0.0, options=bopt)
+        return st1, bv, bvec, st2, mv, mvec
+
+    for _ in range(args.warmup):
+        both()
+    gp.sync()
+    l0 = G.launch_count()
+    clk = ClockSampler()
+    clk.start()
+    profiler_range(True)
+    gp.record(0)
+    for _ in range(args.steps):
+        res = both()
+    gp.record(1)
+    profiler_range(False)
+    clocks = clk.stop()
+    ms = gp.elapsed_ms(0, 1)
+    launches = G.launch_count() - l0
+    st1, bv, bvec, st2, mv, mvec = res
+    value = 2 * EIG_NEV * args.steps / (ms / 1e3)
+    # size-independent check in FP64 on the host: relative eigen-residuals of every pair
+    KL = gp.jacobian(np.zeros(gp.ndof), 1)
+    M = gp.mass()
+    sn = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "Refinement": 20, "RefineTol": 1e-14})
+    sn.setLoad(EIG_SCALING)
+    sn.solveLinear()
+    uL = sn.solution()
+    Bm = gp.jacobian(uL, 1) - KL
+    rb = [float(np.linalg.norm(KL @ v - lam * (Bm @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(bv, bvec)]
+    rm = [float(np.linalg.norm(KL @ v - lam * (M @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(mv, mvec)]
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = eigen_cpu_baseline()
+    line = {
+        "metric": EIG_METRIC, "value": value, "unit": "eigenpairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"roof degree {EIG_P}, {args.eig_m}x{args.eig_m} elements under uniform axial compression: "
+                               f"{EIG_NEV} buckling pairs (shift {args.eig_shift}) + {EIG_NEV} modal pairs (shift 0); "
+                               "one step = both analyses",
+                   "ndof_free": gp.ndof, "nnz": gp.nnz, "status": [int(st1), int(st2)],
+                   "buckling_values": bv.tolist(), "modal_values": mv.tolist(),
+                   "max_rel_residual_buckling": max(rb), "max_rel_residual_modal": max(rm),
+                   "l2": "inputs larger than L2 (fronts %.1f GB)" % (gp.stats()["front_bytes"] / 1e9)},
+        "e2e": {"value": value, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 8 * gp.ndof * 2 * EIG_NEV},
+        "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def eigen_cpu_baseline():
+    """scipy ARPACK shift-invert (SuperLU) modal analysis with the oracle's FP64 matrices on the
+    same roof at 64x64 elements (13k dofs): a bounded sample, per eigenpair."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    prob = P.axial_panel(m=64, p=EIG_P)
+    A = O.OracleAssembler(prob, nthreads=host_cores())
+    t0 = time.perf_counter()
+    K, M = A.linear(), A.mass()
+    O.modal(K, M, nev=EIG_NEV, shift=0.0)
+    dt = time.perf_counter() - t0
+    return {"value": EIG_NEV / dt, "unit": "eigenpairs/s", "cores": host_cores(), "kind": "port",
+            "sample": "20 modal pairs of the same roof at 64x64 elements (13k dofs, not the 201k-dof case): FP64 "
+                      "C++ OpenMP assembly, scipy SuperLU + ARPACK"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -434,7 +805,23 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
+    ap.add_argument("--workload", default="arc-length", choices=["arc-length", "batched", "ramp", "eigen"],
+                    help="arc-length: the headline path-following workload; batched: 256 uneven Newton solves; "
+                         "ramp: degree-3 static Newton load ramp; eigen: buckling + modal at 201k dofs")
+    ap.add_argument("--batch", type=int, default=BATCH_N, help="instances per GPU of the batched workload")
+    ap.add_argument("--eig-m", type=int, default=EIG_M, help="elements per direction of the eigen workload")
+    ap.add_argument("--eig-shift", type=float, default=-1.0, help="buckling shift of the eigen workload")
     args = ap.parse_args()
+    if args.workload == "ramp":
+        return run_ramp(args)
+    if args.workload == "eigen":
+        return run_eigen(args)
+    if args.workload == "batched":
+        if args.impl == "reference":
+            run_batched_reference(args)
+        else:
+            run_batched(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

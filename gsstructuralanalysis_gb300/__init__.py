@@ -68,7 +68,9 @@ SIGNATURES = {
     "klsa_static_iterations": (_c_int, [_c_vp]),
     "klsa_alm_create": (_c_int, [_c_vp, _c_char_p, _c_vp, ctypes.POINTER(_c_vp)]),
     "klsa_alm_destroy": (_c_int, [_c_vp]),
-    "klsa_alm_initialize": (_c_int, [_c_vp]),
+    "klsa_alm_initialize": (_c_int, [_c_vp, _c_int]),
+    "klsa_alm_compute_stability": (_c_int, [_c_vp, _c_int, _c_dbl]),
+    "klsa_alm_stability": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_alm_step": (_c_int, [_c_vp]),
     "klsa_alm_set_length": (_c_int, [_c_vp, _c_dbl]),
     "klsa_alm_reduce_length": (_c_int, [_c_vp, _c_dbl]),
@@ -93,6 +95,20 @@ SIGNATURES = {
     "klsa_alm_step_learned": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
+    "klsa_batch_create": (_c_int, [_c_vp, _c_int, ctypes.POINTER(_c_vp)]),
+    "klsa_batch_destroy": (_c_int, [_c_vp]),
+    "klsa_batch_info": (_c_int, [_c_vp, _c_vp]),
+    "klsa_batch_instance_ndof": (_c_i64, [_c_vp, _c_int]),
+    "klsa_batch_autotune": (_c_int, [_c_vp, _c_vp, _c_int]),
+    "klsa_batch_newton_create": (_c_int, [_c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_batch_newton_destroy": (_c_int, [_c_vp]),
+    "klsa_batch_newton_solve": (_c_int, [_c_vp]),
+    "klsa_batch_newton_reset": (_c_int, [_c_vp]),
+    "klsa_batch_newton_results": (_c_int, [_c_vp, _c_vp, _c_vp]),
+    "klsa_batch_newton_solution": (_c_int, [_c_vp, _c_int, _c_vp]),
+    "klsa_batch_sync": (_c_int, [_c_vp]),
+    "klsa_batch_event_record": (_c_int, [_c_vp, _c_int]),
+    "klsa_batch_event_elapsed": (_c_int, [_c_vp, _c_int, _c_int, _c_vp]),
     "klsa_profile_enable": (_c_int, [_c_int]),
     "klsa_profile_read": (_c_int, [_c_vp, _c_vp]),
     "klsa_profile_reset": (_c_int, []),
@@ -185,6 +201,23 @@ class Options:
             self.h = None
 
 
+def _patch_desc(prob, keep):
+    """PatchDesc of a problems.PatchProblem; the arrays it points to are stored in ``keep``."""
+    k = dict(
+        k1=np.ascontiguousarray(prob.knots1, dtype=np.float64),
+        k2=np.ascontiguousarray(prob.knots2, dtype=np.float64),
+        X=np.ascontiguousarray(prob.ctrl, dtype=np.float64),
+        fx=np.ascontiguousarray(prob.fixed, dtype=np.uint8),
+        qs=np.ascontiguousarray(prob.surface_load, dtype=np.float64),
+        pl=np.ascontiguousarray(prob.point_loads, dtype=np.float64).reshape(-1, 5),
+        ed=np.ascontiguousarray(prob.edge_loads, dtype=np.float64).reshape(-1, 4),
+    )
+    keep.append(k)
+    return PatchDesc(prob.p, prob.n1, prob.n2, prob.nq, _ptr(k["k1"]), _ptr(k["k2"]), _ptr(k["X"]),
+                     prob.E, prob.nu, prob.t, prob.rho, _ptr(k["fx"]), _ptr(k["qs"]),
+                     len(k["pl"]), _ptr(k["pl"]), len(k["ed"]), _ptr(k["ed"]))
+
+
 class Problem:
     """Device-resident patch problem: the Jacobian_t / Residual_t / ALResidual_t / Mass_t /
     Force_t callbacks of the reference (gsStructuralAnalysisTypes.h:58-93)."""
@@ -192,19 +225,8 @@ class Problem:
     def __init__(self, prob):
         L = load_library()
         self.prob = prob
-        self._keep = dict(
-            k1=np.ascontiguousarray(prob.knots1, dtype=np.float64),
-            k2=np.ascontiguousarray(prob.knots2, dtype=np.float64),
-            X=np.ascontiguousarray(prob.ctrl, dtype=np.float64),
-            fx=np.ascontiguousarray(prob.fixed, dtype=np.uint8),
-            qs=np.ascontiguousarray(prob.surface_load, dtype=np.float64),
-            pl=np.ascontiguousarray(prob.point_loads, dtype=np.float64).reshape(-1, 5),
-            ed=np.ascontiguousarray(prob.edge_loads, dtype=np.float64).reshape(-1, 4),
-        )
-        k = self._keep
-        d = PatchDesc(prob.p, prob.n1, prob.n2, prob.nq, _ptr(k["k1"]), _ptr(k["k2"]), _ptr(k["X"]),
-                      prob.E, prob.nu, prob.t, prob.rho, _ptr(k["fx"]), _ptr(k["qs"]),
-                      len(k["pl"]), _ptr(k["pl"]), len(k["ed"]), _ptr(k["ed"]))
+        self._keep = []
+        d = _patch_desc(prob, self._keep)
         h = _c_vp()
         _check(L.klsa_problem_create(ctypes.byref(d), ctypes.byref(h)))
         self.h = h
@@ -363,8 +385,33 @@ class _ALM:
             _lib.klsa_alm_destroy(self.h)
             self.h = None
 
-    def initialize(self):
-        _check(_lib.klsa_alm_initialize(self.h))
+    def initialize(self, stability=True):
+        """initialize(bool stability = true) (gsALMBase.h:110-115) -> gsStatus of the stability test."""
+        return _check(_lib.klsa_alm_initialize(self.h, 1 if stability else 0))
+
+    def computeStability(self, jacobian=True, shift=-1e2):
+        return _check(_lib.klsa_alm_compute_stability(self.h, 1 if jacobian else 0, float(shift)))
+
+    def indicator(self):
+        v = ctypes.c_double()
+        _check(_lib.klsa_alm_stability(self.h, ctypes.byref(v), None, None, None))
+        return v.value
+
+    def stability(self):
+        """+1 unstable, -1 stable (gsALMBase.hpp:616-619)."""
+        v = ctypes.c_int()
+        _check(_lib.klsa_alm_stability(self.h, None, ctypes.byref(v), None, None))
+        return v.value
+
+    def stabilityChange(self):
+        v = ctypes.c_int()
+        _check(_lib.klsa_alm_stability(self.h, None, None, ctypes.byref(v), None))
+        return bool(v.value)
+
+    def negatives(self):
+        v = ctypes.c_int64()
+        _check(_lib.klsa_alm_stability(self.h, None, None, None, ctypes.byref(v)))
+        return v.value
 
     def step(self):
         return _check(_lib.klsa_alm_step(self.h))
@@ -428,6 +475,11 @@ class ALMRiks(_ALM):
 class ALMLoadControl(_ALM):
     """gsALMLoadControl (gsALMSolvers/gsALMLoadControl.hpp)."""
     method = "LoadControl"
+
+
+class ALMConsistentCrisfield(_ALM):
+    """gsALMConsistentCrisfield (gsALMSolvers/gsALMConsistentCrisfield.hpp)."""
+    method = "ConsistentCrisfield"
 
 
 def buckling(problem: Problem, nev: int, shift: float, scaling: float = 1.0, options: dict | None = None,
@@ -524,3 +576,82 @@ class Predictor:
         used = np.zeros(1, dtype=np.int32)
         st = _check(_lib.klsa_alm_step_learned(alm.h, self.h, int(guess_max_iter), _ptr(used)))
         return st, bool(used[0])
+
+
+class BatchedProblem:
+    """Many independent patches sharing every launch (no reference counterpart: the reference
+    runs one assembler and one gsStaticNewton per patch)."""
+
+    def __init__(self, probs):
+        L = load_library()
+        self.probs = list(probs)
+        self._keep = []
+        arr = (PatchDesc * len(self.probs))(*[_patch_desc(p, self._keep) for p in self.probs])
+        self._arr = arr
+        h = _c_vp()
+        _check(L.klsa_batch_create(ctypes.cast(arr, _c_vp), len(self.probs), ctypes.byref(h)))
+        self.h = h
+        self.ndofs = [int(L.klsa_batch_instance_ndof(h, i)) for i in range(len(self.probs))]
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.klsa_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def info(self):
+        out = np.zeros(4)
+        _check(_lib.klsa_batch_info(self.h, _ptr(out)))
+        return dict(zip(["instances", "ndof", "nnz", "front_bytes"], out.tolist()))
+
+    def autotune(self):
+        log = np.zeros((256, 4))
+        rows = _check(_lib.klsa_batch_autotune(self.h, _ptr(log), 256))
+        return log[:rows]
+
+    def sync(self):
+        _check(_lib.klsa_batch_sync(self.h))
+
+    def record(self, slot):
+        _check(_lib.klsa_batch_event_record(self.h, int(slot)))
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_float()
+        _check(_lib.klsa_batch_event_elapsed(self.h, int(a), int(b), ctypes.byref(ms)))
+        return float(ms.value)
+
+
+class BatchedNewton:
+    """gsStaticNewton::solve() on every instance of a BatchedProblem (gsStaticNewton.hpp:101-193)."""
+
+    def __init__(self, batch: BatchedProblem, options: dict | None = None):
+        self.batch = batch
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_batch_newton_create(batch.h, self.opts.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_batch_newton_destroy(self.h)
+            self.h = None
+
+    def solve(self):
+        return _check(_lib.klsa_batch_newton_solve(self.h))
+
+    def reset(self):
+        _check(_lib.klsa_batch_newton_reset(self.h))
+
+    def results(self):
+        n = len(self.batch.probs)
+        st = np.zeros(n, dtype=np.int32)
+        it = np.zeros(n, dtype=np.int32)
+        _check(_lib.klsa_batch_newton_results(self.h, _ptr(st), _ptr(it)))
+        return st, it
+
+    def solution(self, i):
+        U = np.zeros(self.batch.ndofs[i])
+        _check(_lib.klsa_batch_newton_solution(self.h, int(i), _ptr(U)))
+        return U

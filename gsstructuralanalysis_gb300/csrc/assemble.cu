@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <utility>
 
+#include "batch.h"
 #include "problem.h"
 
 namespace klsa {
@@ -156,18 +157,15 @@ __device__ __forceinline__ void cp_data(const QPState<T>& s, T N1, T N2, T N11, 
     }
 }
 
+// Tangent of element e by one warp (smw: the warp's shared-memory control-point records).
 template <int P, class T>
-__global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1, int ncp, int nq,
-                                                         const double* __restrict__ tab1, const double* __restrict__ tab2,
-                                                         const double* __restrict__ qpgeo,
-                                                         const double* __restrict__ ufull, double tmd, double tbd,
-                                                         T* __restrict__ elemK) {
+__device__ __forceinline__ void tangent_element(int e, int m1, int n1, int ncp, int nq,
+                                                const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                                double tmd, double tbd, T* __restrict__ elemK, CPData<T>* smw,
+                                                int lane) {
     constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
     constexpr int NPS = PairTable<P>::NPS, NPAIR = PairTable<P>::NPAIR;
-    __shared__ CPData<T> sm[4][NB];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int e = blockIdx.x * 4 + warp;
-    if (e >= nel) return;
     const int e1 = e % m1, e2 = e / m1;
     const int la = lane % NB1, lb = lane / NB1;
     const bool own = lane < NB;
@@ -199,15 +197,15 @@ __global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1
             const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * 22;
             QPState<T> st;
             qp_state<P, T>(geo, du, tm, tb, st);
-            if (own) cp_data<T>(st, N1, N2, N11, N22, N12, sm[warp][lane], true);
+            if (own) cp_data<T>(st, N1, N2, N11, N22, N12, smw[lane], true);
             __syncwarp();
             const T dV = st.dV;
 #pragma unroll
             for (int s = 0; s < NPS; ++s) {
                 int pi = lane + 32 * s;
                 if (pi >= NPAIR) break;
-                const CPData<T>& A = sm[warp][c_pairA[P - 1][pi]];
-                const CPData<T>& B = sm[warp][c_pairB[P - 1][pi]];
+                const CPData<T>& A = smw[c_pairA[P - 1][pi]];
+                const CPData<T>& B = smw[c_pairB[P - 1][pi]];
                 T Sm = st.n[0] * A.N1 * B.N1 + st.n[1] * A.N2 * B.N2 + st.n[2] * (A.N1 * B.N2 + A.N2 * B.N1);
                 T cr = (A.N1 * B.N2 - A.N2 * B.N1) * st.il;
                 T wv[3] = {st.w.x, st.w.y, st.w.z};
@@ -248,6 +246,49 @@ __global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1
     }
 }
 
+
+template <int P, class T>
+__global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1, int ncp, int nq,
+                                                         const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                         const double* __restrict__ qpgeo,
+                                                         const double* __restrict__ ufull, double tmd, double tbd,
+                                                         T* __restrict__ elemK) {
+    __shared__ CPData<T> sm[4][(P + 1) * (P + 1)];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    if (e >= nel) return;
+    tangent_element<P, T>(e, m1, n1, ncp, nq, tab1, tab2, qpgeo, ufull, tmd, tbd, elemK, sm[warp], lane);
+}
+
+// Instance of a flat work index: the largest k with off[k] <= g (off ascending, off[0] = 0).
+__device__ __forceinline__ int find_segment(const int* __restrict__ off, int n, int g) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Persistent batched tangent (FP32): every warp walks the flat element list of all instances of
+// degree P (instance list `insts`, element prefix sums `elem_off`) with a grid-stride loop.
+template <int P>
+__global__ void __launch_bounds__(128) kl_tangent_batch_kernel(int ninst, const int* __restrict__ insts,
+                                                               const int* __restrict__ elem_off,
+                                                               const BatchInst* __restrict__ desc) {
+    __shared__ CPData<float> sm[4][(P + 1) * (P + 1)];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = elem_off[ninst];
+    for (int g = blockIdx.x * 4 + warp; g < total; g += gridDim.x * 4) {
+        const int k = find_segment(elem_off, ninst, g);
+        const BatchInst& d = desc[insts[k]];
+        tangent_element<P, float>(g - elem_off[k], d.m1, d.n1, d.ncp, d.nq, d.tab1, d.tab2, d.qpgeo, d.ufull, d.tm,
+                                  d.tb, d.elemK, sm[warp], lane);
+        __syncwarp();
+    }
+}
+
 // Internal force in FP64.  A warp holds ES = 32 / max((p+1)^2, nq^2) elements: lanes first act
 // as Gauss points (one lane evaluates one point's deformed geometry and stress resultants, no
 // redundant per-lane work), then as control points (one lane accumulates one control point's
@@ -255,28 +296,28 @@ __global__ void __launch_bounds__(128) kl_tangent_kernel(int nel, int m1, int n1
 // shared memory).
 constexpr int QSTATE = 16;   // G1, G2, S11, S22, S12 of one Gauss point
 
+// Internal forces of the elements of warp work unit `grp` (elements grp*es .. grp*es+es-1);
+// usw / qsw: the warp's shared-memory displacement and Gauss-point records.
 template <int P>
-__global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, int ncp, int nq,
-                                                      const double* __restrict__ tab1, const double* __restrict__ tab2,
-                                                      const double* __restrict__ qpgeo, const double* __restrict__ ufull,
-                                                      double tm, double tb, double* __restrict__ elemR) {
+__device__ __forceinline__ void fint_group(int grp, int nel, int m1, int n1, int ncp, int nq,
+                                           const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                           const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                           double tm, double tb, double* __restrict__ elemR, double (*usw)[3],
+                                           double (*qsw)[QSTATE], int lane) {
     constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
-    __shared__ double us[4][32][3];
-    __shared__ double qs[4][32][QSTATE];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nqp = nq * nq;
     const int lpe = NB > nqp ? NB : nqp;
     const int es = 32 / lpe;
     const int slot = lane / lpe, idx = lane % lpe;
-    const int e = (blockIdx.x * 4 + warp) * es + slot;
+    const int e = grp * es + slot;
     const bool live = slot < es && e < nel;
     const int e1 = live ? e % m1 : 0, e2 = live ? e / m1 : 0;
     // phase 0: displacements of the element's control points
     if (live && idx < NB) {
         int A = (e2 + idx / NB1) * n1 + (e1 + idx % NB1);
-        us[warp][slot * NB + idx][0] = ufull[A];
-        us[warp][slot * NB + idx][1] = ufull[ncp + A];
-        us[warp][slot * NB + idx][2] = ufull[2 * ncp + A];
+        usw[slot * NB + idx][0] = ufull[A];
+        usw[slot * NB + idx][1] = ufull[ncp + A];
+        usw[slot * NB + idx][2] = ufull[2 * ncp + A];
     }
     __syncwarp();
     // phase 1: one lane per Gauss point
@@ -292,7 +333,7 @@ __global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, i
             int a = c % NB1, b = c / NB1;
             double N1 = t1[NB1 + a] * t2[b], N2 = t1[a] * t2[NB1 + b];
             double N11 = t1[2 * NB1 + a] * t2[b], N22 = t1[a] * t2[2 * NB1 + b], N12 = t1[NB1 + a] * t2[NB1 + b];
-            const double* u = us[warp][slot * NB + c];
+            const double* u = usw[slot * NB + c];
             double Ns[5] = {N1, N2, N11, N22, N12};
 #pragma unroll
             for (int g = 0; g < 5; ++g) {
@@ -309,7 +350,7 @@ __global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, i
         //   S11 = dV m0 a3, S22 = dV m1 a3, S12 = 2 dV m2 a3   (w = v - (v.a3) a3)
         const double dV = st.dV;
         V3T<double> u1 = cross3(st.a2, st.w), u2 = cross3(st.w, st.a1);
-        double* o = qs[warp][slot * nqp + idx];
+        double* o = qsw[slot * nqp + idx];
         o[0] = dV * (st.n[0] * st.a1.x + st.n[2] * st.a2.x - u1.x * st.il);
         o[1] = dV * (st.n[0] * st.a1.y + st.n[2] * st.a2.y - u1.y * st.il);
         o[2] = dV * (st.n[0] * st.a1.z + st.n[2] * st.a2.z - u1.z * st.il);
@@ -332,12 +373,43 @@ __global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, i
             const double* t2 = tab2 + (((size_t)e2 * nq + q2) * 3) * NB1;
             double N1 = t1[NB1 + a] * t2[b], N2 = t1[a] * t2[NB1 + b];
             double N11 = t1[2 * NB1 + a] * t2[b], N22 = t1[a] * t2[2 * NB1 + b], N12 = t1[NB1 + a] * t2[NB1 + b];
-            const double* o = qs[warp][slot * nqp + qq];
+            const double* o = qsw[slot * nqp + qq];
 #pragma unroll
             for (int i = 0; i < 3; ++i)
                 f[i] += N1 * o[i] + N2 * o[3 + i] - N11 * o[6 + i] - N22 * o[9 + i] - N12 * o[12 + i];
         }
         for (int i = 0; i < 3; ++i) elemR[(size_t)e * D + 3 * idx + i] = f[i];
+    }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, int ncp, int nq,
+                                                      const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                      const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                                      double tm, double tb, double* __restrict__ elemR) {
+    __shared__ double us[4][32][3];
+    __shared__ double qs[4][32][QSTATE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    fint_group<P>(blockIdx.x * 4 + warp, nel, m1, n1, ncp, nq, tab1, tab2, qpgeo, ufull, tm, tb, elemR, us[warp],
+                  qs[warp], lane);
+}
+
+// Persistent batched internal force: warps walk the flat list of element groups of all
+// instances of degree P (group prefix sums `grp_off`).
+template <int P>
+__global__ void __launch_bounds__(128) kl_fint_batch_kernel(int ninst, const int* __restrict__ insts,
+                                                            const int* __restrict__ grp_off,
+                                                            const BatchInst* __restrict__ desc) {
+    __shared__ double us[4][32][3];
+    __shared__ double qs[4][32][QSTATE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = grp_off[ninst];
+    for (int g = blockIdx.x * 4 + warp; g < total; g += gridDim.x * 4) {
+        const int k = find_segment(grp_off, ninst, g);
+        const BatchInst& d = desc[insts[k]];
+        fint_group<P>(g - grp_off[k], d.nel, d.m1, d.n1, d.ncp, d.nq, d.tab1, d.tab2, d.qpgeo, d.ufull, d.tm, d.tb,
+                      d.elemR, us[warp], qs[warp], lane);
+        __syncwarp();
     }
 }
 
@@ -457,6 +529,63 @@ __global__ void spmv_kernel(int n, const int* __restrict__ rowptr, const int* __
     if (lane == 0) y[row] = s;
 }
 
+// Batched CSR gather (FP32 values): one warp per row of the merged block-diagonal matrix; the
+// instance of the row by binary search over the row offsets.
+__global__ void csr_gather_batch_kernel(int nrows, int ninst, const int* __restrict__ dof_off,
+                                        const BatchInst* __restrict__ desc, const int* __restrict__ rowptr,
+                                        const int* __restrict__ cols, float* __restrict__ vals) {
+    int R = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    int lane = threadIdx.x & 31;
+    if (R >= nrows) return;
+    const BatchInst& d = desc[find_segment(dof_off, ninst, R)];
+    const int p = d.p, n1 = d.n1, m1 = d.m1, m2 = d.m2, ncp = d.ncp, off = d.dof_off;
+    int fr = d.int2full[R - off];
+    int ci = fr / ncp, Ar = fr - ci * ncp;
+    int ir = Ar % n1, jr = Ar / n1;
+    int NB1 = p + 1, D = 3 * NB1 * NB1;
+    for (int z = rowptr[R] + lane; z < rowptr[R + 1]; z += 32) {
+        int fc = d.int2full[cols[z] - off];
+        int cj = fc / ncp, Ac = fc - cj * ncp;
+        int ic = Ac % n1, jc = Ac / n1;
+        int e1lo = max(max(ir, ic) - p, 0), e1hi = min(min(ir, ic), m1 - 1);
+        int e2lo = max(max(jr, jc) - p, 0), e2hi = min(min(jr, jc), m2 - 1);
+        double sum = 0.0;
+        for (int e2 = e2lo; e2 <= e2hi; ++e2)
+            for (int e1 = e1lo; e1 <= e1hi; ++e1) {
+                int la = (jr - e2) * NB1 + (ir - e1), lb = (jc - e2) * NB1 + (ic - e1);
+                sum += (double)d.elemK[((size_t)(e2 * m1 + e1) * D + 3 * la + ci) * D + 3 * lb + cj];
+            }
+        vals[z] = (float)sum;
+    }
+}
+
+__global__ void vec_gather_batch_kernel(int nrows, int ninst, const int* __restrict__ dof_off,
+                                        const BatchInst* __restrict__ desc, double* __restrict__ out) {
+    int R = blockIdx.x * blockDim.x + threadIdx.x;
+    if (R >= nrows) return;
+    const BatchInst& d = desc[find_segment(dof_off, ninst, R)];
+    const int p = d.p, n1 = d.n1, m1 = d.m1, m2 = d.m2, ncp = d.ncp;
+    int fr = d.int2full[R - d.dof_off];
+    int ci = fr / ncp, A = fr - ci * ncp;
+    int i = A % n1, j = A / n1;
+    int NB1 = p + 1, D = 3 * NB1 * NB1;
+    double sum = 0.0;
+    for (int e2 = max(j - p, 0); e2 <= min(j, m2 - 1); ++e2)
+        for (int e1 = max(i - p, 0); e1 <= min(i, m1 - 1); ++e1) {
+            int la = (j - e2) * NB1 + (i - e1);
+            sum += d.elemR[(size_t)(e2 * m1 + e1) * D + 3 * la + ci];
+        }
+    out[R] = sum;
+}
+
+__global__ void scatter_free_batch_kernel(int nrows, int ninst, const int* __restrict__ dof_off,
+                                          const BatchInst* __restrict__ desc, const double* __restrict__ x) {
+    int R = blockIdx.x * blockDim.x + threadIdx.x;
+    if (R >= nrows) return;
+    const BatchInst& d = desc[find_segment(dof_off, ninst, R)];
+    d.ufull[d.int2full[R - d.dof_off]] = x[R];
+}
+
 bool g_pairs_ready = false;
 
 void init_pairs() {
@@ -562,6 +691,65 @@ void Problem::internal_force_elements(double* elemR) {
         default: throw std::invalid_argument("unsupported degree");
     }
     count_launch();
+}
+
+// ---- batched launches --------------------------------------------------------------------
+void BatchedProblem::launch_tangent(int d, int bps) {
+    DegreeList& L = deg[d];
+    if (L.ninst == 0) return;
+    init_pairs();
+    int grid = std::max(1, std::min(ceil_div(L.nel, 4), num_sms * bps));
+    if (d == 0)
+        kl_tangent_batch_kernel<2><<<grid, 128, 0, stream>>>(L.ninst, L.insts.get(), L.elem_off.get(), d_desc.get());
+    else
+        kl_tangent_batch_kernel<3><<<grid, 128, 0, stream>>>(L.ninst, L.insts.get(), L.elem_off.get(), d_desc.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void BatchedProblem::launch_gather_K() {
+    csr_gather_batch_kernel<<<ceil_div((int64_t)nfree * 32, 256), 256, 0, stream>>>(
+        nfree, ninst, d_dof_off.get(), d_desc.get(), d_rowptr.get(), d_cols.get(), d_vals32.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void BatchedProblem::launch_fint(int d, int bps) {
+    DegreeList& L = deg[d];
+    if (L.ninst == 0) return;
+    int grid = std::max(1, std::min(ceil_div(L.ngrp, 4), num_sms * bps));
+    if (d == 0)
+        kl_fint_batch_kernel<2><<<grid, 128, 0, stream>>>(L.ninst, L.insts.get(), L.grp_off.get(), d_desc.get());
+    else
+        kl_fint_batch_kernel<3><<<grid, 128, 0, stream>>>(L.ninst, L.insts.get(), L.grp_off.get(), d_desc.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void BatchedProblem::launch_gather_R(double* d_out) {
+    vec_gather_batch_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, ninst, d_dof_off.get(), d_desc.get(),
+                                                                     d_out);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void BatchedProblem::set_displacement(const double* d_x) {
+    scatter_free_batch_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, ninst, d_dof_off.get(), d_desc.get(),
+                                                                       d_x);
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
+void BatchedProblem::tangent_f32() {
+    launch_tangent(0, tangent_bps[0]);
+    launch_tangent(1, tangent_bps[1]);
+    launch_gather_K();
+}
+
+void BatchedProblem::internal_force(double* d_out) {
+    launch_fint(0, fint_bps[0]);
+    launch_fint(1, fint_bps[1]);
+    launch_gather_R(d_out);
 }
 
 void Problem::pub_to_int(const double* d_pub, double* d_int, int nv) {

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "../../include/klshell_gb300.h"
+#include "batch.h"
 #include "eigen.h"
 #include "linalg.h"
 #include "mlp.h"
@@ -47,6 +48,19 @@ struct klsa_predictor {
     klsa_problem* prob;
     std::unique_ptr<LearnedPredictor> pred;
     DevBuf<double> ug, u;
+};
+
+struct klsa_batch {
+    std::unique_ptr<BatchedProblem> B;
+    cudaEvent_t ev[16] = {};
+    ~klsa_batch() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+struct klsa_batch_newton {
+    klsa_batch* b;
+    std::unique_ptr<BatchedNewton> N;
 };
 
 namespace {
@@ -318,6 +332,7 @@ int klsa_alm_create(klsa_problem* prob, const char* method, const klsa_options* 
         if (s == "Crisfield") m = ALMGPU::Crisfield;
         else if (s == "Riks") m = ALMGPU::Riks;
         else if (s == "LoadControl") m = ALMGPU::LoadControl;
+        else if (s == "ConsistentCrisfield") m = ALMGPU::ConsistentCrisfield;
         else {
             g_err = "unknown arc-length method " + s;
             return KLSA_INVALID_ARGUMENT;
@@ -340,12 +355,24 @@ int klsa_alm_destroy(klsa_alm* a) {
         return KLSA_SUCCESS;
     });
 }
-int klsa_alm_initialize(klsa_alm* a) {
+int klsa_alm_initialize(klsa_alm* a, int stability) {
     if (!a) return KLSA_INVALID_ARGUMENT;
     return guarded([&] {
-        a->A->initialize();
-        return KLSA_SUCCESS;
+        a->A->initialize(false);
+        return stability ? a->A->compute_stability(true, -1e2) : KLSA_SUCCESS;
     });
+}
+int klsa_alm_compute_stability(klsa_alm* a, int jacobian, double shift) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return a->A->compute_stability(jacobian != 0, shift); });
+}
+int klsa_alm_stability(klsa_alm* a, double* indicator, int* stability, int* change, int64_t* negatives) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    if (indicator) *indicator = a->A->indicator();
+    if (stability) *stability = a->A->stability();
+    if (change) *change = a->A->stability_change() ? 1 : 0;
+    if (negatives) *negatives = a->A->negatives();
+    return KLSA_SUCCESS;
 }
 int klsa_alm_step(klsa_alm* a) {
     if (!a) return KLSA_INVALID_ARGUMENT;
@@ -643,6 +670,134 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values, double* vectors) {
     if (!prob || !values || nev < 1) return KLSA_INVALID_ARGUMENT;
     return guarded([&] { return modal_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, values, vectors); });
+}
+
+}  // extern "C"
+
+// ---- batched Newton ------------------------------------------------------------------------
+extern "C" {
+
+int klsa_batch_create(const klsa_patch_desc* descs, int n, klsa_batch** out) {
+    if (!descs || n < 1 || !out) return KLSA_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<const klsa_patch_desc*> v(n);
+        for (int i = 0; i < n; ++i) v[i] = descs + i;
+        std::unique_ptr<klsa_batch> b(new klsa_batch);
+        b->B.reset(new BatchedProblem(v));
+        *out = b.release();
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_destroy(klsa_batch* b) {
+    delete b;
+    return KLSA_SUCCESS;
+}
+
+int klsa_batch_info(klsa_batch* b, double* out) {
+    if (!b || !out) return KLSA_INVALID_ARGUMENT;
+    out[0] = b->B->ninst;
+    out[1] = b->B->nfree;
+    out[2] = (double)b->B->nnz;
+    out[3] = (double)b->B->mf->front_bytes();
+    return KLSA_SUCCESS;
+}
+
+int64_t klsa_batch_instance_ndof(klsa_batch* b, int i) {
+    if (!b || i < 0 || i >= b->B->ninst) return -1;
+    return b->B->inst[i]->nfree;
+}
+
+int klsa_batch_autotune(klsa_batch* b, double* log, int cap) {
+    if (!b) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        b->B->autotune();
+        int rows = (int)b->B->tune_log.size() / 4;
+        if (log)
+            for (int r = 0; r < std::min(rows, cap); ++r)
+                for (int c = 0; c < 4; ++c) log[4 * r + c] = b->B->tune_log[4 * r + c];
+        return rows;
+    });
+}
+
+int klsa_batch_newton_create(klsa_batch* b, const klsa_options* opt, klsa_batch_newton** out) {
+    if (!b || !out) return KLSA_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guarded([&] {
+        Options o = opt ? opt->o : Options{};
+        std::unique_ptr<klsa_batch_newton> s(new klsa_batch_newton);
+        s->b = b;
+        s->N.reset(new BatchedNewton(*b->B, o));
+        *out = s.release();
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_newton_destroy(klsa_batch_newton* s) {
+    delete s;
+    return KLSA_SUCCESS;
+}
+
+int klsa_batch_newton_solve(klsa_batch_newton* s) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return s->N->solve(); });
+}
+
+int klsa_batch_newton_reset(klsa_batch_newton* s) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        s->N->reset();
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_newton_results(klsa_batch_newton* s, int* status, int* iterations) {
+    if (!s) return KLSA_INVALID_ARGUMENT;
+    const int n = s->b->B->ninst;
+    for (int i = 0; i < n; ++i) {
+        if (status) status[i] = s->N->status()[i];
+        if (iterations) iterations[i] = s->N->iterations()[i];
+    }
+    return KLSA_SUCCESS;
+}
+
+int klsa_batch_newton_solution(klsa_batch_newton* s, int i, double* U) {
+    if (!s || !U || i < 0 || i >= s->b->B->ninst) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        BatchedProblem& B = *s->b->B;
+        Problem& P = *B.inst[i];
+        KL_CUDA(cudaStreamSynchronize(B.stream));
+        P.download_pub(s->N->U() + B.dof_off[i], U, 1);
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_sync(klsa_batch* b) {
+    if (!b) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        KL_CUDA(cudaStreamSynchronize(b->B->stream));
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_event_record(klsa_batch* b, int slot) {
+    if (!b || slot < 0 || slot >= 16) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!b->ev[slot]) KL_CUDA(cudaEventCreate(&b->ev[slot]));
+        KL_CUDA(cudaEventRecord(b->ev[slot], b->B->stream));
+        return KLSA_SUCCESS;
+    });
+}
+
+int klsa_batch_event_elapsed(klsa_batch* b, int slot_a, int slot_b, float* ms) {
+    if (!b || !ms || slot_a < 0 || slot_a >= 16 || slot_b < 0 || slot_b >= 16 || !b->ev[slot_a] || !b->ev[slot_b])
+        return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        KL_CUDA(cudaEventSynchronize(b->ev[slot_b]));
+        KL_CUDA(cudaEventElapsedTime(ms, b->ev[slot_a], b->ev[slot_b]));
+        return KLSA_SUCCESS;
+    });
 }
 
 }  // extern "C"

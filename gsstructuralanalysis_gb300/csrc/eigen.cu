@@ -87,6 +87,14 @@ __global__ void combine_kernel(int64_t n, double a, const double* __restrict__ x
     if (i < n) z[i] = a * x[i] + b * y[i];
 }
 
+// values of the identity matrix on the CSR pattern (the pattern always holds the diagonal)
+__global__ void identity_vals_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ cols,
+                                     double* __restrict__ vals) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) vals[k] = (cols[k] == r) ? 1.0 : 0.0;
+}
+
 // cyclic Jacobi eigen-decomposition of a symmetric m x m matrix (row-major H, column eigvecs in Q)
 void jacobi_eig(int m, std::vector<double> H, std::vector<double>& w, std::vector<double>& Q) {
     Q.assign((size_t)m * m, 0.0);
@@ -139,6 +147,8 @@ struct Lanczos {
     DevBuf<double> V, Y, w, z, rhs, partial, dh, Sbuf, tmpV;
     std::vector<double> hpart;
     int restarts = 0, op_count = 0;
+
+    bool largest_alge = false;   // wanted Ritz values: largest |theta| (false) or largest theta (true)
 
     Lanczos(Problem& P_, MFSolver& S_, const double* valsC_, int nev_, int m_, double tol_, int maxr)
         : P(P_), S(S_), valsC(valsC_), n(P_.nfree), m(m_), nev(nev_), tol(tol_), max_restarts(maxr) {
@@ -227,7 +237,10 @@ struct Lanczos {
             jacobi_eig(m, H, theta, Q);
             order.resize(m);
             std::iota(order.begin(), order.end(), 0);
-            std::sort(order.begin(), order.end(), [&](int a, int b) { return std::fabs(theta[a]) > std::fabs(theta[b]); });
+            if (largest_alge)
+                std::sort(order.begin(), order.end(), [&](int a, int b) { return theta[a] > theta[b]; });
+            else
+                std::sort(order.begin(), order.end(), [&](int a, int b) { return std::fabs(theta[a]) > std::fabs(theta[b]); });
             int nconv = 0;
             for (int i = 0; i < nev; ++i) {
                 int c = order[i];
@@ -268,8 +281,11 @@ struct Lanczos {
     }
 };
 
+// largest_alge: select the largest transformed values nu (Spectra LargestAlge) instead of the
+// largest |nu| (LargestMagn); sort_alge: return the eigenvalues ascending (SmallestAlge) instead
+// of by ascending |lambda| (SmallestMagn).
 int run_pencil(Problem& P, const Options& opt, const double* valsA, const double* valsB, bool buckling_mode, int nev,
-               double shift, double* values, double* vectors) {
+               double shift, double* values, double* vectors, bool largest_alge = false, bool sort_alge = false) {
     int n = P.nfree;
     int64_t nnz = P.nnz;
     if (nev >= n) throw std::invalid_argument("nev must be smaller than the number of dofs");
@@ -287,6 +303,7 @@ int run_pencil(Problem& P, const Options& opt, const double* valsA, const double
     KL_CUDA(cudaMemcpyAsync(valsC.get(), buckling_mode ? valsA : valsB, sizeof(double) * nnz, cudaMemcpyDeviceToDevice,
                             P.stream));
     Lanczos lz(P, S, valsC.get(), nev, m, tol, (int)opt.integer("maxRestarts", 200));
+    lz.largest_alge = largest_alge;
     std::vector<double> theta, Q;
     std::vector<int> sel;
     int nconv = lz.run(theta, Q, sel);
@@ -298,7 +315,10 @@ int run_pencil(Problem& P, const Options& opt, const double* valsA, const double
     }
     std::vector<int> idx(nev);
     std::iota(idx.begin(), idx.end(), 0);
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return std::fabs(lam[a]) < std::fabs(lam[b]); });
+    if (sort_alge)
+        std::sort(idx.begin(), idx.end(), [&](int a, int b) { return lam[a] < lam[b]; });
+    else
+        std::sort(idx.begin(), idx.end(), [&](int a, int b) { return std::fabs(lam[a]) < std::fabs(lam[b]); });
     for (int i = 0; i < nev; ++i) values[i] = lam[idx[i]];
     if (vectors) {
         std::vector<double> Ssel((size_t)m * nev);
@@ -343,6 +363,19 @@ int buckling_gpu(Problem& P, const Options& opt, int nev, double shift, double s
     combine_kernel<<<ceil_div(nnz, 256), 256, 0, P.stream>>>(nnz, 1.0, P.d_vals64.get(), -1.0, KL.get(), B.get());
     count_launch();
     return run_pencil(P, opt, KL.get(), B.get(), true, nev, shift, values, vectors);
+}
+
+int standard_eigs_gpu(Problem& P, const double* valsA, int nev, int ncv_fac, double shift, double tol, double* values) {
+    int64_t nnz = P.nnz;
+    DevBuf<double> A(nnz), I(nnz);
+    KL_CUDA(cudaMemcpyAsync(A.get(), valsA, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, P.stream));
+    identity_vals_kernel<<<ceil_div(P.nfree, 256), 256, 0, P.stream>>>(P.nfree, P.d_rowptr.get(), P.d_cols.get(), I.get());
+    count_launch();
+    Options o;
+    o.ints["ncvFac"] = ncv_fac;
+    o.reals["tolerance"] = tol;
+    o.ints["maxRestarts"] = 1000;
+    return run_pencil(P, o, A.get(), I.get(), false, nev, shift, values, nullptr, true, true);
 }
 
 int modal_gpu(Problem& P, const Options& opt, int nev, double shift, double* values, double* vectors) {

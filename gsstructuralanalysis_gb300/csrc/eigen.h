@@ -13,6 +13,13 @@ int buckling_gpu(Problem& P, const Options& opt, int nev, double shift, double s
 // gsModalSolver (gsEigenSolvers/gsModalSolver.h:46-51) + Spectra ShiftInvert mode: K v = lambda M v.
 int modal_gpu(Problem& P, const Options& opt, int nev, double shift, double* values, double* vectors);
 
+// Standard symmetric problem A v = lambda v in shift-invert mode, the stability indicator of
+// gsALMBase::_computeStability (gsALMSolvers/gsALMBase.hpp:570-598): Spectra SymShiftSolver with
+// ncv = ncv_fac * nev, selection LargestAlge of nu = 1/(lambda - shift), values returned ascending
+// (SmallestAlge).  valsA: FP64 values on the problem's CSR pattern.  Uses the problem's
+// factorisation workspace (the caller's factorisation is overwritten).
+int standard_eigs_gpu(Problem& P, const double* valsA, int nev, int ncv_fac, double shift, double tol, double* values);
+
 // y = A x with an explicit FP64 value array over the problem's CSR pattern
 void spmv_vals(const Problem& P, const double* vals, const double* x, double* y);
 

@@ -3,15 +3,17 @@
 // Per level of the elimination tree (leaves first):
 //   1. extend-add of the children's Schur complements into the parent fronts (one launch
 //      per child slot, so sibling updates never race and the sum order is fixed);
-//   2. per 64-column tile step of the pivots: diagonal LDL^T + explicit inverse of the unit
-//      lower tile (one CTA per front), panel L21 = A21 L11^-T D^-1 and W = L21 D (one CTA per
-//      64-row block), trailing lower update A22 -= W L21^T (one CTA per 64x64 tile).
+//   2. per 64-column tile step of the pivots: diagonal LDL^T + explicit inverse X = L11^-1 of
+//      the unit lower tile (one CTA per front), panel W = A21 X^T and L21 = W D^-1 as a small
+//      GEMM (one CTA per 64-row block), trailing lower update A22 -= W L21^T (one CTA per
+//      64x64 tile).
 // No pivoting (as Eigen's SimplicialLDLT); a zero or non-finite pivot sets the status word.
 #include "multifrontal.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <thread>
 
 namespace klsa {
 
@@ -59,218 +61,170 @@ __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restri
     for (; b < hc; b += 32) dcol[mp[b]] += scol[b];
 }
 
-// One warp factors an n x n (n <= 16) symmetric block in shared memory (row-major, leading
-// dimension ld, lower triangle): lane i < 16 holds row i in registers; each pivot step is one
-// shuffle broadcast per column.  L (strict lower) and D (diagonal) overwrite the block.
-__device__ __noinline__ void warp_ldlt16(float* A, int ld, int n, bool* bad) {
-    const int i = threadIdx.x & 31;
-    float a[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) a[c] = (i < n && c <= i) ? A[i * ld + c] : 0.f;
-    bool b = false;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        if (j < n) {
-            float d = __shfl_sync(0xffffffffu, a[j], j);
-            if (!(fabsf(d) > 0.f) || !isfinite(d)) { b = true; d = 1.f; }
-            const float lij = (i > j && i < n) ? a[j] / d : 0.f;
-#pragma unroll
-            for (int c = j + 1; c < 16; ++c) {
-                float v = __shfl_sync(0xffffffffu, a[j], c);   // A(c, j) before scaling
-                if (c <= i) a[c] -= lij * v;
-            }
-            if (i > j && i < n) a[j] = lij;
-        }
-    }
-    if (b && i == 0) *bad = true;
-#pragma unroll
-    for (int c = 0; c < 16; ++c)
-        if (i < n && c <= i) A[i * ld + c] = a[c];
-}
-
-// Diagonal tile (kk <= 64 pivots): right-looking LDL^T in 16-column panels -- warp 0 factors the
-// 16x16 diagonal block, one thread per row solves the panel below it, all threads apply the
-// rank-16 update of the rest of the tile.  Writes L (strict lower) and D back to the front and D
-// to Dvec.  The inverse of the unit lower factor is not needed here (the panel kernel solves by
-// substitution) and is formed later, off the critical path, by mf_inverse_kernel.
+// Diagonal tile (kk <= 64 pivots), 256 threads.  Every entry of the packed lower triangle of the
+// 64x64 tile (e = r(r+1)/2 + c) lives in a register of a fixed owner (thread e % 256, slot
+// e / 256); rows and columns beyond kk are padded with the identity.
+//   LDL^T, right-looking: step j, the owners of column j publish it to shared memory (double
+//   buffered), one barrier, then every thread applies -A(r,j) A(c,j) / d_j to its entries with
+//   c > j and scales its column-j entries to L(r,j).
+//   X = L^-1 (unit lower), same ownership: step j publishes row j of X, rows r > j subtract
+//   L(r,j) X(j,:).
+// Writes L (strict lower) and D (diagonal) into the front, D into Dvec and X into the tile's slot
+// of linv (row-major), which the panel GEMM and the triangular solves use.
+constexpr int DIAG_SLOTS = (NB * (NB + 1) / 2 + 255) / 256;
 __global__ void __launch_bounds__(256) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                       const int* __restrict__ k, const int* __restrict__ own,
-                                                      const int64_t* __restrict__ front_off, float* pool, float* Dvec,
-                                                      int* status) {
-    __shared__ float A[NB][NB + 1];      // row-major tile
-    __shared__ float Wp[NB][17];         // W = L D of the current panel
-    __shared__ bool bad;
-    int nd = items[blockIdx.x].x;
-    int fN = f[nd], kN = k[nd];
-    int c0 = t * NB;
-    int kk = min(NB, kN - c0);
+                                                      const int64_t* __restrict__ front_off,
+                                                      const int64_t* __restrict__ linv_off, float* pool, float* Dvec,
+                                                      float* linv, int* status) {
+    __shared__ float Ls[NB][NB + 1];
+    __shared__ float buf[2][NB];
+    __shared__ int bad;
+    const int nd = items[blockIdx.x].x;
+    const int fN = f[nd], kN = k[nd];
+    const int c0 = t * NB;
+    const int kk = min(NB, kN - c0);
     float* F = pool + front_off[nd];
-    const int tid = threadIdx.x, warp = tid >> 5;
-    if (tid == 0) bad = false;
-    {
-        float v[16];
+    const int tid = threadIdx.x;
+    if (tid == 0) bad = 0;
+    // stage the tile, column-major walk (coalesced)
+    for (int e = tid; e < NB * NB; e += 256) {
+        const int c = e / NB, r = e % NB;
+        Ls[r][c] = (r < kk && c <= r) ? F[(int64_t)(c0 + c) * fN + c0 + r] : 0.f;
+    }
+    int rr[DIAG_SLOTS], cc[DIAG_SLOTS];
+    float v[DIAG_SLOTS];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            int e = tid + 256 * q, c = e / NB, r = e % NB;   // column-major walk: coalesced
-            v[q] = (r < kk && c <= r) ? F[(int64_t)(c0 + c) * fN + c0 + r] : 0.f;
-        }
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            int e = tid + 256 * q;
-            A[e % NB][e / NB] = v[q];
-        }
+    for (int q = 0; q < DIAG_SLOTS; ++q) {
+        const int e = tid + 256 * q;
+        int r = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
+        while (r * (r + 1) / 2 > e) --r;
+        while ((r + 1) * (r + 2) / 2 <= e) ++r;
+        const bool live = e < NB * (NB + 1) / 2;
+        rr[q] = live ? r : -1;
+        cc[q] = live ? e - r * (r + 1) / 2 : NB;
     }
     __syncthreads();
-    for (int p0 = 0; p0 < kk; p0 += 16) {
-        const int np = min(16, kk - p0);
-        if (warp == 0) warp_ldlt16(&A[p0][p0], NB + 1, np, &bad);
-        __syncthreads();
-        // panel: rows r >= p0+np solve  w L_pp^T = a  (w = L D), L(r, p0+j) = w_j / D_j
-        const int r = p0 + np + tid;
-        if (r < kk) {
-            float w[16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                float s = (j < np) ? A[r][p0 + j] : 0.f;
-#pragma unroll
-                for (int m = 0; m < j; ++m) s -= w[m] * A[p0 + j][p0 + m];
-                w[j] = s;
-            }
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                Wp[r][j] = w[j];
-                if (j < np) A[r][p0 + j] = w[j] / A[p0 + j][p0 + j];
-            }
-        }
-        __syncthreads();
-        // rank-np update of the trailing lower part of the tile
-        const int t0 = p0 + np, nt = kk - t0;
-        for (int e = tid; e < nt * nt; e += 256) {
-            int rr = t0 + e / nt, cc = t0 + e % nt;
-            if (cc > rr) continue;
-            float s = 0.f;
-#pragma unroll
-            for (int j = 0; j < 16; ++j)
-                if (j < np) s += Wp[rr][j] * A[cc][p0 + j];
-            A[rr][cc] -= s;
-        }
-        __syncthreads();
+    for (int q = 0; q < DIAG_SLOTS; ++q) {
+        const int r = rr[q], c = cc[q];
+        v[q] = (r < 0) ? 0.f : (r < kk ? Ls[r][c] : (r == c ? 1.f : 0.f));
     }
-    if (tid == 0 && bad) atomicExch(status, 1);
+    for (int j = 0; j < NB; ++j) {
+        float* b = buf[j & 1];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-        int e = tid + 256 * q, c = e / NB, r = e % NB;
-        if (r < kk && c <= r) F[(int64_t)(c0 + c) * fN + c0 + r] = A[r][c];
-    }
-    if (tid < kk) Dvec[own[nd] + c0 + tid] = A[tid][tid];
-}
-
-// Inverse of the unit lower factor of one diagonal tile (used only by the triangular solves):
-// launched once for every tile of every node after the factorisation.  Thread (ty, r) keeps row r
-// of X, columns ty + 4q, in registers; row j of X is final at step j and rows r > j subtract
-// L(r, j) X(j, :).
-__global__ void __launch_bounds__(256) mf_inverse_kernel(const int4* __restrict__ items, const int* __restrict__ f,
-                                                         const int* __restrict__ k,
-                                                         const int64_t* __restrict__ front_off,
-                                                         const int64_t* __restrict__ linv_off,
-                                                         const float* __restrict__ pool, float* linv) {
-    __shared__ float L[NB][NB + 1];
-    __shared__ float rowb[2][NB];
-    int4 it = items[blockIdx.x];
-    int nd = it.x, t = it.y;
-    int fN = f[nd], kN = k[nd];
-    int c0 = t * NB;
-    int kk = min(NB, kN - c0);
-    const float* F = pool + front_off[nd];
-    const int tid = threadIdx.x, r = tid & (NB - 1), ty = tid >> 6;
-    {
-        float v[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            int e = tid + 256 * q, c = e / NB, rr = e % NB;
-            v[q] = (rr < kk && c < rr) ? F[(int64_t)(c0 + c) * fN + c0 + rr] : 0.f;
+        for (int q = 0; q < DIAG_SLOTS; ++q)
+            if (cc[q] == j) b[rr[q]] = v[q];
+        __syncthreads();
+        float d = b[j];
+        if (!(fabsf(d) > 0.f) || !isfinite(d)) {
+            d = 1.f;
+            if (tid == 0) bad = 1;
         }
+        const float inv = 1.f / d;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            int e = tid + 256 * q;
-            L[e % NB][e / NB] = v[q];
+        for (int q = 0; q < DIAG_SLOTS; ++q) {
+            if (cc[q] > j && cc[q] < NB) v[q] -= b[rr[q]] * inv * b[cc[q]];
+            else if (cc[q] == j && rr[q] > j) v[q] *= inv;
         }
     }
-    float x[16];
+    // L and D back to shared memory (the front and the inverse read them from there)
 #pragma unroll
-    for (int q = 0; q < 16; ++q) x[q] = (ty + 4 * q == r && r < kk) ? 1.f : 0.f;
+    for (int q = 0; q < DIAG_SLOTS; ++q)
+        if (rr[q] >= 0) Ls[rr[q]][cc[q]] = v[q];
     __syncthreads();
-    for (int j = 0; j < kk; ++j) {
-        const int buf = j & 1;
-        if (r == j) {
+    for (int e = tid; e < NB * NB; e += 256) {
+        const int c = e / NB, r = e % NB;
+        if (r < kk && c <= r) F[(int64_t)(c0 + c) * fN + c0 + r] = Ls[r][c];
+    }
+    if (tid < kk) Dvec[own[nd] + c0 + tid] = Ls[tid][tid];
+    // X = L^-1
 #pragma unroll
-            for (int q = 0; q < 16; ++q) rowb[buf][ty + 4 * q] = x[q];
-        }
+    for (int q = 0; q < DIAG_SLOTS; ++q) v[q] = (rr[q] >= 0 && rr[q] == cc[q]) ? 1.f : 0.f;
+    for (int j = 0; j < NB; ++j) {
+        float* b = buf[j & 1];
+#pragma unroll
+        for (int q = 0; q < DIAG_SLOTS; ++q)
+            if (rr[q] == j) b[cc[q]] = v[q];
         __syncthreads();
-        if (r > j && r < kk) {
-            const float l = L[r][j];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                int c = ty + 4 * q;
-                if (c <= j) x[q] -= l * rowb[buf][c];
-            }
-        }
+        for (int q = 0; q < DIAG_SLOTS; ++q)
+            if (rr[q] > j && cc[q] <= j) v[q] -= Ls[rr[q]][j] * b[cc[q]];
     }
     float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
 #pragma unroll
-    for (int q = 0; q < 16; ++q) Li[r * NB + ty + 4 * q] = (r < kk) ? x[q] : 0.f;
+    for (int q = 0; q < DIAG_SLOTS; ++q)
+        if (rr[q] >= 0) Li[rr[q] * NB + cc[q]] = rr[q] < kk ? v[q] : 0.f;
+    for (int e = tid; e < NB * NB; e += 256)
+        if (e % NB > e / NB) Li[e] = 0.f;
+    if (tid == 0 && bad && kk > 0) atomicExch(status, 1);
 }
 
-// Panel: one thread per row r of the block below the diagonal tile solves w L11^T = a by
-// substitution (L11 staged in shared memory), writes L21 = w D^-1 in place and keeps W = w for
-// the trailing update.
-constexpr int PANEL_THREADS = 64;
-__global__ void __launch_bounds__(PANEL_THREADS) mf_panel_kernel(const int4* __restrict__ items, int t,
-                                                                 const int* __restrict__ f, const int* __restrict__ k,
-                                                                 const int64_t* __restrict__ front_off,
-                                                                 const int64_t* __restrict__ ws_off, float* pool,
-                                                                 float* ws) {
-    __shared__ float Ls[NB][NB + 1];   // Ls[j][m] = L11(j, m), Ls[j][j] = D_j
-    int4 it = items[blockIdx.x];
-    int nd = it.x, r0 = it.y;
-    int fN = f[nd], kN = k[nd];
-    int c0 = t * NB;
-    int kk = min(NB, kN - c0);
+// Panel rows [r0, r0 + 64) below the diagonal tile: W = A21 X^T (X = L11^-1 from the diagonal
+// kernel), L21 = W D^-1 written in place and W kept for the trailing update.  A 64 x 64 x kk
+// product per CTA: thread (tx, ty) owns rows tx + 16 i and columns ty + 16 q.
+__global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
+                                                       const int* __restrict__ k, const int64_t* __restrict__ front_off,
+                                                       const int64_t* __restrict__ linv_off,
+                                                       const int64_t* __restrict__ ws_off, float* pool,
+                                                       const float* __restrict__ linv, float* ws) {
+    __shared__ float As[NB][NB + 1];   // As[m][rr] = A21(r0 + rr, m)
+    __shared__ float Xs[NB][NB + 1];   // Xs[m][jj] = X(jj, m)
+    __shared__ float Ds[NB];
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, r0 = it.y;
+    const int fN = f[nd], kN = k[nd];
+    const int c0 = t * NB;
+    const int kk = min(NB, kN - c0);
     float* F = pool + front_off[nd];
-    const int tid = threadIdx.x;
+    const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
     {
-        // stage L11 (64 x 64) with 64 threads: column-major walk, 64 loads per thread
-#pragma unroll 8
-        for (int q = 0; q < NB; ++q) {
-            int c = q, rr = tid;
-            Ls[rr][c] = (rr < kk && c <= rr) ? F[(int64_t)(c0 + c) * fN + c0 + rr] : 0.f;
+        float va[16], vx[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int m = lg + 4 * q;
+            va[q] = (m < kk && r0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + r0 + lt] : 0.f;
+            vx[q] = Li[m * NB + lt];   // X(m, lt): row m of X
         }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            As[lg + 4 * q][lt] = va[q];
+            Xs[lt][lg + 4 * q] = vx[q];
+        }
+        if (threadIdx.x < NB) Ds[threadIdx.x] = threadIdx.x < kk ? F[(int64_t)(c0 + threadIdx.x) * fN + c0 + threadIdx.x] : 1.f;
     }
     __syncthreads();
-    const int r = r0 + tid;
-    if (r >= fN) return;
-    float w[NB];
+    float acc[4][4];
 #pragma unroll
-    for (int j = 0; j < NB; ++j) w[j] = (j < kk) ? F[(int64_t)(c0 + j) * fN + r] : 0.f;
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 1; j < NB; ++j) {
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;   // four independent chains
+        for (int q = 0; q < 4; ++q) acc[i][q] = 0.f;
+    for (int m = 0; m < kk; ++m) {
+        float a[4], b[4];
 #pragma unroll
-        for (int m = 0; m < j; ++m) {
-            const float v = w[m] * Ls[j][m];
-            if ((m & 3) == 0) s0 += v;
-            else if ((m & 3) == 1) s1 += v;
-            else if ((m & 3) == 2) s2 += v;
-            else s3 += v;
-        }
-        w[j] -= (s0 + s1) + (s2 + s3);
+        for (int i = 0; i < 4; ++i) a[i] = As[m][tx + 16 * i];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) b[q] = Xs[m][ty + 16 * q];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(a[i], b[q], acc[i][q]);
     }
     float* W = ws + ws_off[nd];
 #pragma unroll
-    for (int j = 0; j < NB; ++j) {
-        if (j < kk) {
-            W[(int64_t)j * fN + r] = w[j];
-            F[(int64_t)(c0 + j) * fN + r] = w[j] / Ls[j][j];
+    for (int q = 0; q < 4; ++q) {
+        const int j = ty + 16 * q;
+        if (j >= kk) continue;
+        const float dinv = 1.f / Ds[j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int R = r0 + tx + 16 * i;
+            if (R < fN) {
+                W[(int64_t)j * fN + R] = acc[i][q];
+                F[(int64_t)(c0 + j) * fN + R] = acc[i][q] * dinv;
+            }
         }
     }
 }
@@ -592,16 +546,29 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
     // CSR lower entries -> front positions
     nnz_ = cols.size();
     std::vector<int64_t> fpos(nnz_, -1);
-    for (int R = 0; R < n_; ++R)
-        for (int e = rowptr[R]; e < rowptr[R + 1]; ++e) {
-            int C = cols[e];
-            if (C > R) continue;
-            int nd = T.node_of[C];
-            int lc = C - T.nodes[nd].own_start;
-            int lr = T.local_index(nd, R);
-            if (lr < 0) throw std::logic_error("multifrontal: matrix entry outside its front");
-            fpos[e] = front_off[nd] + (int64_t)lc * f[nd] + lr;
-        }
+    {
+        // rows are independent: split them over the host threads
+        const int nt = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 32u));
+        std::vector<std::thread> pool;
+        std::vector<int> bad(nt, 0);
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&, t] {
+                const int r0 = (int)((int64_t)n_ * t / nt), r1 = (int)((int64_t)n_ * (t + 1) / nt);
+                for (int R = r0; R < r1; ++R)
+                    for (int e = rowptr[R]; e < rowptr[R + 1]; ++e) {
+                        int C = cols[e];
+                        if (C > R) continue;
+                        int nd = T.node_of[C];
+                        int lc = C - T.nodes[nd].own_start;
+                        int lr = T.local_index(nd, R);
+                        if (lr < 0) { bad[t] = 1; return; }
+                        fpos[e] = front_off[nd] + (int64_t)lc * f[nd] + lr;
+                    }
+            });
+        for (auto& th : pool) th.join();
+        for (int b : bad)
+            if (b) throw std::logic_error("multifrontal: matrix entry outside its front");
+    }
     // levels and work lists
     nlevels_ = T.max_height + 1;
     level_nodes_.assign(nlevels_, {});
@@ -659,22 +626,17 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
             for (int t = 0; t * NB < k[nd]; ++t) {
                 double kk = std::min(NB, k[nd] - t * NB);
                 double below = f[nd] - t * NB - kk;
-                kernel_bytes[0] += 4.0 * kk * kk;                       // read + write the lower tile
-                kernel_flops[0] += kk * kk * kk / 3.0;
-                kernel_bytes[1] += 4.0 * (3.0 * below * kk + 0.5 * kk * kk);   // A21 in, L21 and W out, L11 in
-                kernel_flops[1] += below * kk * kk;
+                kernel_bytes[0] += 4.0 * kk * kk + 4.0 * NB * NB;      // lower tile in + out, X = L^-1 out
+                kernel_flops[0] += 2.0 * kk * kk * kk / 3.0;            // LDL^T + triangular inverse
+                kernel_bytes[1] += 4.0 * (3.0 * below * kk + NB * NB);  // A21 in, L21 and W out, X in
+                kernel_flops[1] += below * kk * kk;                     // below x kk x kk/2 FMAs
                 double ntr = std::ceil(below / NB);
                 double tiles = ntr * (ntr + 1) / 2;
                 kernel_bytes[2] += tiles * 4.0 * (2.0 * NB * kk + 2.0 * NB * NB);   // W, L tiles in; A tile r/w
                 kernel_flops[2] += below * below * kk;                  // lower half of below x below x kk x 2
             }
     for (int i = 0; i < nnodes_; ++i) solve_bytes += 2.0 * 4.0 * ((double)k[i] * f[i] - 0.5 * (double)k[i] * k[i]);
-    size_t inv_begin = items.size();
-    for (int i = 0; i < nnodes_; ++i)
-        for (int t = 0; t * NB < k[i]; ++t) items.push_back(make_int4(i, t, 0, 0));
-    size_t inv_end = items.size();
     items_.upload(items, stream_);
-    inv_items_ = MFWork{items_.get() + inv_begin, (int)(inv_end - inv_begin)};
     for (const Pending& m : marks) {
         MFWork w{items_.get() + m.begin, (int)(m.end - m.begin)};
         Level& lv = levels_[m.level];
@@ -792,16 +754,18 @@ void Multifrontal::factorize_launches(const float* d_vals) {
             if (st.diag.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
                 mf_diag_kernel<<<st.diag.count, 256, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
-                                                                   d_own_.get(), d_front_off_.get(), pool_.get(),
-                                                                   D_.get(), status_.get());
+                                                                   d_own_.get(), d_front_off_.get(),
+                                                                   d_linv_off_.get(), pool_.get(), D_.get(),
+                                                                   linv_.get(), status_.get());
                 g_timer.end(stream_, 5, evk);
                 count_launch();
             }
             if (st.panel.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_panel_kernel<<<st.panel.count, PANEL_THREADS, 0, stream_>>>(st.panel.items, st.t, d_f_.get(),
-                                                                               d_k_.get(), d_front_off_.get(),
-                                                                               d_ws_off_.get(), pool_.get(), ws_.get());
+                mf_panel_kernel<<<st.panel.count, 256, 0, stream_>>>(st.panel.items, st.t, d_f_.get(), d_k_.get(),
+                                                                     d_front_off_.get(), d_linv_off_.get(),
+                                                                     d_ws_off_.get(), pool_.get(), linv_.get(),
+                                                                     ws_.get());
                 g_timer.end(stream_, 6, evk);
                 count_launch();
             }
@@ -814,12 +778,6 @@ void Multifrontal::factorize_launches(const float* d_vals) {
                 count_launch();
             }
         }
-    }
-    if (inv_items_.count) {
-        mf_inverse_kernel<<<inv_items_.count, 256, 0, stream_>>>(inv_items_.items, d_f_.get(), d_k_.get(),
-                                                                 d_front_off_.get(), d_linv_off_.get(), pool_.get(),
-                                                                 linv_.get());
-        count_launch();
     }
     KL_CHECK_LAUNCH();
 }
@@ -857,6 +815,10 @@ void Multifrontal::solve_impl(const float* d_b, float* d_x) {
     }
     KL_CHECK_LAUNCH();
 }
+
+void Multifrontal::enqueue_factorize(const float* d_vals) { factorize_launches(d_vals); }
+
+void Multifrontal::enqueue_solve(const float* d_b, float* d_x) { solve_impl<1>(d_b, d_x); }
 
 void Multifrontal::solve(const float* d_b, float* d_x, int nrhs) {
     switch (nrhs) {

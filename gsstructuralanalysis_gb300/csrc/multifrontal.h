@@ -45,6 +45,10 @@ public:
     void solve(const float* d_b, float* d_x, int nrhs);
     // min(D) and #negatives of D (after factorize)
     void stability(double* min_d, int64_t* negatives);
+    // The launch sequences alone (no graph of their own), for callers that capture a larger
+    // graph around them.
+    void enqueue_factorize(const float* d_vals);
+    void enqueue_solve(const float* d_b, float* d_x);
 
     int n() const { return n_; }
     double flops() const { return flops_; }
@@ -84,7 +88,6 @@ private:
     struct Step { MFWork diag, panel, update; int t; };
     struct Level { MFWork ea[2]; std::vector<Step> steps; MFWork nodes; int max_f = 0; };
     std::vector<Level> levels_;
-    MFWork inv_items_;
     std::vector<std::vector<int>> level_nodes_;
     int max_f_ = 0;
 };

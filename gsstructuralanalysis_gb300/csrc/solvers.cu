@@ -1,8 +1,12 @@
 // solvers.cu -- gsStaticNewton / gsALMCrisfield / gsALMRiks / gsALMLoadControl on the device.
 #include "solvers.h"
 
+#include "eigen.h"
+
+#include <algorithm>
 #include <cmath>
 #include <stdexcept>
+#include <vector>
 
 namespace klsa {
 
@@ -147,7 +151,7 @@ ALMGPU::ALMGPU(Problem& P, Method m, const Options& opt) : P_(P), method_(m), op
     // gsALMBase::defaultOptions: Solver = SimplicialLDLT (gsALMBase.hpp:48)
     S_ = solver_from_options(P_, opt_, "SimplicialLDLT");
     n_ = P_.nfree;
-    for (DevBuf<double>* b : {&U_, &DU_, &dU_, &dUt_, &dUbar_, &DUold_, &Uprev_, &Uguess_, &R_, &x_, &fint_, &tmp_}) {
+    for (DevBuf<double>* b : {&U_, &DU_, &dU_, &dUt_, &dUbar_, &DUold_, &Uprev_, &Uguess_, &R_, &x_, &fint_, &tmp_, &xjac_}) {
         b->alloc(n_);
         b->zero(P_.stream);
     }
@@ -171,6 +175,9 @@ void ALMGPU::apply_options() {
     phi_ = opt_.real("Scaling", -1.0);
     phi_user_ = phi_ != -1.0;
     angle_ = (int)opt_.integer("AngleMethod", 0);
+    // gsALMBase.hpp:39, 72-78: Eigenvalue by default; Determinant needs the LDL^T solver
+    bifurcation_ = (int)opt_.integer("BifurcationMethod", 1);
+    if (bifurcation_ == 0 && !S_->has_ldlt()) bifurcation_ = 1;
 }
 
 void ALMGPU::set_length(double l) {
@@ -178,9 +185,57 @@ void ALMGPU::set_length(double l) {
     arcLength_ = arcLength_prev_ = arcLength_ori_ = l;
 }
 
-void ALMGPU::initialize() {
+void ALMGPU::initialize(bool stability) {
     for (DevBuf<double>* b : {&U_, &DU_, &DUold_, &Uprev_}) b->zero(P_.stream);
     L_ = DL_ = DLold_ = Lprev_ = 0.0;
+    // gsALMBase::init (gsALMBase.hpp:95-103): stability at U with a fresh Jacobian
+    if (stability) stability_impl(true, -1e2);
+}
+
+void ALMGPU::stability_impl(bool jacobian, double shift) {
+    if (jacobian) {
+        // Jacobian at U, factorised (gsALMBase.hpp:549-554)
+        KL_CUDA(cudaMemcpyAsync(xjac_.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+        P_.set_displacement(xjac_.get());
+        ++n_jac;
+        if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ut_valid_ = false;
+        fact_stale_ = false;
+    }
+    if (bifurcation_ == 0) {
+        // Determinant (gsALMBase.hpp:557-569): D of the current LDL^T factorisation
+        double mn = 0.0;
+        int64_t neg = 0;
+        S_->stability(&mn, &neg);
+        indicator_ = mn;
+        negatives_ = neg;
+    } else if (bifurcation_ == 1) {
+        // Eigenvalue (gsALMBase.hpp:570-598): nev = min(floor(n/5), 10), ncv = 5 nev, tol 1e-6, on
+        // the Jacobian of the last iteration, evaluated in FP64
+        int number = std::min(n_ / 5, 10);
+        if (number < 1) throw Fail{ST_SOLVER_ERROR};
+        P_.set_displacement(xjac_.get());
+        P_.tangent_f64();
+        std::vector<double> vals(number);
+        int st = standard_eigs_gpu(P_, P_.d_vals64.get(), number, 5, shift, 1e-6, vals.data());
+        fact_stale_ = true;
+        if (st != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        negatives_ = std::count_if(vals.begin(), vals.end(), [](double v) { return v < 0; });
+        indicator_ = *std::min_element(vals.begin(), vals.end());
+    } else {
+        indicator_ = 0.0;
+        negatives_ = 0;
+    }
+    stability_ = indicator_ < 0 ? 1 : -1;
+}
+
+int ALMGPU::compute_stability(bool jacobian, double shift) {
+    try {
+        stability_impl(jacobian, shift);
+        return ST_SUCCESS;
+    } catch (const Fail& f) {
+        return f.code;
+    }
 }
 
 void ALMGPU::set_solution(const double* d_U, double L) {
@@ -204,7 +259,10 @@ void ALMGPU::compute_jacobian() {
     P_.set_displacement(x_.get());
     ++n_jac;
     if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    if (bifurcation_ == 1)
+        KL_CUDA(cudaMemcpyAsync(xjac_.get(), x_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
     ut_valid_ = false;
+    fact_stale_ = false;
 }
 
 void ALMGPU::compute_residual() {
@@ -326,6 +384,10 @@ void ALMGPU::predictor() {
         vec::axpby(0.0, dU_.get(), arcLength_, dU_.get(), n_, s);
         vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
         DL_ += dL_;
+    } else if (method_ == ConsistentCrisfield) {
+        // gsALMConsistentCrisfield.hpp:104-146: tangent direction on the first step, secant
+        // (U - Uprev, L - Lprev) / l_prev afterwards; phi from the last u_t
+        consistent_predictor(Uprev_.get(), Lprev_);
     } else {  // LoadControl
         DL_ = dL_ = arcLength_;
         if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
@@ -384,6 +446,9 @@ void ALMGPU::predictor_guess() {
         vec::axpby(0.0, dU_.get(), arcLength_, dU_.get(), n_, s);
         KL_CUDA(cudaMemcpyAsync(DU_.get(), dU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
         DL_ = dL_;
+    } else if (method_ == ConsistentCrisfield) {
+        // gsALMConsistentCrisfield.hpp:148-190: the same with (Uguess - U, Lguess - L)
+        consistent_predictor(nullptr, 0.0);
     } else {
         DL_ = dL_ = Lguess_ - L_;
         if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
@@ -391,6 +456,43 @@ void ALMGPU::predictor_guess() {
         vec::lincomb(dL_, dUt_.get(), 0.0, dUt_.get(), DU_.get(), n_, s);
     }
     has_guess_ = false;
+}
+
+// Predictor of gsALMConsistentCrisfield (Jacobian already factorised).  With `prevU` the secant
+// is (U - prevU, L - prevL) (predictor); with null it is (Uguess - U, Lguess - L) (predictorGuess).
+void ALMGPU::consistent_predictor(const double* prevU, double prevL) {
+    cudaStream_t s = P_.stream;
+    if (prevU) {
+        vec::lincomb(1.0, U_.get(), -1.0, prevU, tmp_.get(), n_, s);
+    } else {
+        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, s);
+    }
+    const double dLsec = prevU ? (L_ - prevL) : (Lguess_ - L_);
+    double d[2];
+    const double* xs[2] = {tmp_.get(), dUt_.get()};
+    vec::multidot(2, xs, xs, n_, d, s);
+    const double tol = 1e-10;
+    if (std::sqrt(d[0]) < tol && dLsec * dLsec < tol) {
+        const double DLs = 1.0;
+        if (S_->solve(P_.d_F.get(), dUt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        ++n_solve;
+        ut_valid_ = true;
+        double uu;
+        const double* a[1] = {dUt_.get()};
+        vec::multidot(1, a, a, n_, &uu, s);
+        const double den = std::sqrt(uu + DL_ * DLs);
+        vec::lincomb(1.0 / den, dUt_.get(), 0.0, dUt_.get(), dU_.get(), n_, s);
+        dL_ = DLs / den;
+        if (!phi_user_) phi_ = std::sqrt(uu / FF_);
+    } else {
+        dL_ = dLsec / arcLength_prev_;
+        vec::lincomb(1.0 / arcLength_prev_, tmp_.get(), 0.0, tmp_.get(), dU_.get(), n_, s);
+        if (!phi_user_) phi_ = std::sqrt(d[1] / FF_);
+    }
+    dL_ *= arcLength_;
+    vec::axpby(0.0, dU_.get(), arcLength_, dU_.get(), n_, s);
+    vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+    DL_ += dL_;
 }
 
 void ALMGPU::quasi_newton_iteration() {
@@ -465,6 +567,13 @@ void ALMGPU::lambdas_crisfield() {
 
 void ALMGPU::iteration() {
     cudaStream_t s = P_.stream;
+    if (fact_stale_) {
+        // a quasi-Newton iteration after an eigenvalue stability test: refactorise the Jacobian
+        P_.set_displacement(xjac_.get());
+        ++n_jac;
+        if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        fact_stale_ = false;
+    }
     if (method_ == Crisfield) {
         solve_ut_ubar(!ut_valid_);
         eta_ = 1.0;
@@ -480,6 +589,20 @@ void ALMGPU::iteration() {
             KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
             DLold_ = DL_;
         }
+    } else if (method_ == ConsistentCrisfield) {
+        // gsALMConsistentCrisfield.hpp:75-90 (Carrera 1994, eqs. 20-21)
+        solve_ut_ubar(!ut_valid_);
+        double d[3];
+        const double* xs[3] = {DU_.get(), DU_.get(), DU_.get()};
+        const double* ys[3] = {DU_.get(), dUbar_.get(), dUt_.get()};
+        vec::multidot(3, xs, ys, n_, d, s);
+        const double cres = d[0] + phi_ * phi_ * DL_ * DL_ * FF_ - arcLength_ * arcLength_;
+        const double num = cres + 2.0 * d[1];
+        const double denum = 2.0 * d[2] + phi_ * phi_ * 2.0 * DL_ * FF_;
+        dL_ = -num / denum;
+        vec::lincomb(dL_, dUt_.get(), 1.0, dUbar_.get(), dU_.get(), n_, s);
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
     } else if (method_ == Riks) {
         solve_ut_ubar(!ut_valid_);
         double d[3];
@@ -505,7 +628,7 @@ void ALMGPU::iteration_finish() {
     Lprev_ = L_;
     vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
     L_ += DL_;
-    if (method_ == Crisfield && angle_ == 0) {
+    if ((method_ == Crisfield && angle_ == 0) || method_ == ConsistentCrisfield) {
         KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
         DLold_ = DL_;
     }
@@ -530,9 +653,11 @@ void ALMGPU::step_impl() {
     if (quasi_ && !ut_valid_) {
         // quasiNewtonPredictor: keep the predictor's tangent
     }
+    stabilityPrev_ = stability_;
     for (num_it_ = 1; num_it_ < maxIt_; ++num_it_) {
         if (!quasi_ || (quasiInterval_ > 0 && num_it_ % quasiInterval_ == 0)) quasi_newton_iteration();
         iteration();
+        stability_impl(false, -1e2);   // gsALMBase.hpp:390
         compute_residual();
         compute_residual_norms();
         if (residueF_ < tolF_ && residueU_ < tolU_) {

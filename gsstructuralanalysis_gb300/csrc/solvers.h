@@ -67,14 +67,22 @@ private:
 };
 
 // gsALMBase + subclasses (gsALMSolvers/gsALMBase.hpp:22-416, gsALMCrisfield.hpp,
-// gsALMRiks.hpp, gsALMLoadControl.hpp).  ALResidual convention R = Fint(U) - L*F.
+// gsALMRiks.hpp, gsALMLoadControl.hpp, gsALMConsistentCrisfield.hpp).  ALResidual convention
+// R = Fint(U) - L*F.
 class ALMGPU {
 public:
-    enum Method { Crisfield = 0, Riks = 1, LoadControl = 2 };
+    enum Method { Crisfield = 0, Riks = 1, LoadControl = 2, ConsistentCrisfield = 3 };
     ALMGPU(Problem& P, Method m, const Options& opt);
     void apply_options();
-    void initialize();
+    void initialize(bool stability);
     int step();
+    // gsALMBase::computeStability (gsALMBase.hpp:521-545, 547-615) -> gsStatus
+    int compute_stability(bool jacobian, double shift);
+    double indicator() const { return indicator_; }
+    int stability() const { return stability_; }
+    bool stability_change() const { return stability_ * stabilityPrev_ < 0; }
+    int64_t negatives() const { return negatives_; }
+    int bifurcation_method() const { return bifurcation_; }
     void set_length(double l);
     double reduce_length(double fac) { arcLength_ *= fac; return arcLength_; }
     double length() const { return arcLength_; }
@@ -117,6 +125,8 @@ private:
     void solve_ut_ubar(bool need_ut);
     void compute_lambda_mu();
     void lambdas_crisfield();
+    void consistent_predictor(const double* prevU, double prevL);
+    void stability_impl(bool jacobian, double shift);
 
     Problem& P_;
     Method method_;
@@ -124,6 +134,7 @@ private:
     std::unique_ptr<LinearSolver> S_;
     int n_;
     DevBuf<double> U_, DU_, dU_, dUt_, dUbar_, DUold_, Uprev_, Uguess_, R_, x_, fint_, rhs2_, sol2_, tmp_;
+    DevBuf<double> xjac_;          // point of the last Jacobian (m_jacMat's argument)
     double L_ = 0, DL_ = 0, dL_ = 0, DLold_ = 0, Lprev_ = 0, Lguess_ = 0;
     bool has_guess_ = false;
     double FF_ = 0;
@@ -145,6 +156,12 @@ private:
     double residueF_ = 0, residueU_ = 0, basisF_ = 0, basisU_ = 0;
     bool ut_valid_ = false;
     bool guess_place_ = false;
+    // stability (BifurcationMethod -1 nothing, 0 determinant, 1 eigenvalue; gsALMBase.h:385-390)
+    int bifurcation_ = 1;
+    int stability_ = -1, stabilityPrev_ = -1;
+    double indicator_ = 0.0;
+    int64_t negatives_ = 0;
+    bool fact_stale_ = false;      // the eigenvalue indicator reused the factorisation workspace
 };
 
 }  // namespace klsa

@@ -25,14 +25,24 @@ from . import problems as P
 EXTRAP = np.array([4.0, -6.0, 4.0, -1.0])   # cubic extrapolation weights of P_k, P_{k-1}, P_{k-2}, P_{k-3}
 
 
+def sign_weights(ncp):
+    """Fixed positive weights of the control points for the sign convention of the modes.  The
+    largest |w| of a mode that is antisymmetric about a mid-line is met at two mirror points with
+    opposite signs, so "largest |w| positive" is decided by rounding; the sign of the weighted sum
+    sum_A c_A w_A with these non-symmetric weights is not."""
+    return np.random.default_rng(20240607).uniform(0.5, 1.5, size=ncp)
+
+
 def sign_fixed_modes(prob, vecs):
-    """Free-dof eigenvectors -> full-layout modes, sign fixed so that the largest |w| is positive."""
+    """Free-dof eigenvectors -> full-layout modes, sign fixed so that sum_A c_A w_A > 0 (c: fixed
+    weights of ``sign_weights``)."""
+    c = sign_weights(prob.ncp)
     modes = []
     for v in vecs:
         full = np.zeros(prob.ndof_full)
         full[prob.free_index()] = v
         w = full[2 * prob.ncp:]
-        if w[np.argmax(np.abs(w))] < 0:
+        if float(c @ w) < 0:
             full = -full
         modes.append(full)
     return modes
@@ -133,6 +143,8 @@ def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0, c
     tr, va = (paths[:-val_paths], paths[-val_paths:]) if len(paths) > val_paths else (paths, paths)
     X, T = features_targets(tr, Phi)
     Xv, Tv = features_targets(va, Phi)
+    if len(X) == 0 or len(Xv) == 0:
+        raise ValueError("training paths too short: every path needs at least 5 points")
     mu, sd = X.mean(0), X.std(0) + 1e-30
     omu, osd = T.mean(0), T.std(0) + 1e-30
     sd[sd < 1e-12 * np.abs(mu).max()] = 1.0

@@ -130,10 +130,18 @@ int klsa_static_iterations(klsa_static* s);
 
 /* ---- arc-length family (gsALMSolvers/gsALMBase.hpp:354-416 and subclasses) ------------
  * method: "Crisfield" (gsALMCrisfield.hpp), "Riks" (gsALMRiks.hpp), "LoadControl"
- * (gsALMLoadControl.hpp). */
+ * (gsALMLoadControl.hpp), "ConsistentCrisfield" (gsALMConsistentCrisfield.hpp). */
 int klsa_alm_create(klsa_problem* prob, const char* method, const klsa_options* opt, klsa_alm** out);
 int klsa_alm_destroy(klsa_alm* a);
-int klsa_alm_initialize(klsa_alm* a);                     /* initialize(false) */
+/* initialize(bool stability) (gsALMBase.h:110-115): with stability != 0 the Jacobian at U is
+   computed and factorised and the stability indicator of "BifurcationMethod" evaluated. */
+int klsa_alm_initialize(klsa_alm* a, int stability);
+/* computeStability(bool jacobian, T shift) (gsALMBase.h:251, gsALMBase.hpp:521-615) -> gsStatus */
+int klsa_alm_compute_stability(klsa_alm* a, int jacobian, double shift);
+/* indicator() (gsALMBase.h:161), stability() (+1 unstable / -1 stable, gsALMBase.hpp:616-619),
+   stabilityChange() (gsALMBase.hpp:624-627) and the number of negative entries of the
+   stability vector (inertia of the Jacobian for "Determinant"). Any out pointer may be NULL. */
+int klsa_alm_stability(klsa_alm* a, double* indicator, int* stability, int* change, int64_t* negatives);
 int klsa_alm_step(klsa_alm* a);                           /* step() -> gsStatus */
 int klsa_alm_set_length(klsa_alm* a, double length);      /* setLength */
 int klsa_alm_reduce_length(klsa_alm* a, double factor);   /* reduceLength */
@@ -186,6 +194,37 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 /* Modal (gsModalSolver.h:46-51): eigenpairs of K v = omega^2 M v about ``shift``. */
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
                double* vectors);
+
+/* ---- batched Newton solves of many patches (no counterpart in the reference) ------------
+ * Equivalent to one gsStaticNewton::solve() per instance (gsStaticNewton.hpp:101-193), each
+ * with its own assembler; here all instances share every launch: a persistent assembly kernel
+ * over the elements of all instances, one multifrontal factorisation of the merged
+ * block-diagonal tangent (an elimination forest), device-side convergence control and one
+ * CUDA graph per Newton iteration.  Instances: degree 2 or 3. */
+typedef struct klsa_batch klsa_batch;
+typedef struct klsa_batch_newton klsa_batch_newton;
+int klsa_batch_create(const klsa_patch_desc* descs, int n, klsa_batch** out);
+int klsa_batch_destroy(klsa_batch* b);
+/* out[4]: instances, free dofs (all instances), CSR nonzeros (all instances), front pool bytes */
+int klsa_batch_info(klsa_batch* b, double* out);
+/* free dofs of instance i (its public order, as klsa_problem_ndof) */
+int64_t klsa_batch_instance_ndof(klsa_batch* b, int i);
+/* Times the launch shapes of the persistent assembly kernels and keeps the fastest.  log:
+ * (kind 0 tangent / 1 internal force, degree, blocks per SM, ms) per trial, up to cap rows;
+ * returns the number of rows. */
+int klsa_batch_autotune(klsa_batch* b, double* log, int cap);
+/* Options as gsStaticNewton ("tol", "tolF", "tolU", "maxIt", "Relaxation") plus "LoadFactor". */
+int klsa_batch_newton_create(klsa_batch* b, const klsa_options* opt, klsa_batch_newton** out);
+int klsa_batch_newton_destroy(klsa_batch_newton* s);
+/* solve() of every instance -> Success when all converged, else NotConverged; per-instance
+ * statuses (gsStatus) and iteration counts from klsa_batch_newton_results. */
+int klsa_batch_newton_solve(klsa_batch_newton* s);
+int klsa_batch_newton_reset(klsa_batch_newton* s);   /* U = 0, next solve() starts linearly */
+int klsa_batch_newton_results(klsa_batch_newton* s, int* status, int* iterations);
+int klsa_batch_newton_solution(klsa_batch_newton* s, int i, double* U);   /* public order */
+int klsa_batch_sync(klsa_batch* b);
+int klsa_batch_event_record(klsa_batch* b, int slot);
+int klsa_batch_event_elapsed(klsa_batch* b, int slot_a, int slot_b, float* ms);
 
 /* ---- measurement helpers (no counterpart in the reference, which has no device) -------- */
 /* Per-phase device times from CUDA events on the problem streams: ms[8], counts[8] for

@@ -310,7 +310,7 @@ class _ALMBase:
         self.jacobian, self.res = jacobian, al_residual
         self.F = np.asarray(F, dtype=np.float64)
         self.opts = dict(MaxIter=100, Tol=1e-6, TolF=1e-3, TolU=1e-6, Length=1e-2, AdaptiveLength=False,
-                         AdaptiveIterations=10, Quasi=False, QuasiIterations=-1, BifurcationMethod=-1,
+                         AdaptiveIterations=10, Quasi=False, QuasiIterations=-1, BifurcationMethod=1,
                          Relaxation=1.0, Scaling=-1.0, AngleMethod=0)
         if options:
             self.opts.update(options)
@@ -328,6 +328,50 @@ class _ALMBase:
         self.num_iterations = 0
         self.converged = False
         self.counts = dict(jac=0, res=0, solve=0)
+        self.stabilityVec = np.zeros(0)
+        self.indicator = 0.0
+        self.negatives = 0
+        self.stability = -1
+        self.stabilityPrev = -1
+
+    def initialize(self, stability=True):
+        """gsALMBase::initialize / init (gsALMBase.h:110-115, gsALMBase.hpp:95-103)."""
+        if stability:
+            self.compute_stability(jacobian=True)
+
+    def compute_stability(self, jacobian=True, shift=-1e2):
+        """gsALMBase::_computeStability (gsALMBase.hpp:547-615).  Determinant (0): the reference
+        takes D of the LDL^T; its count of negative entries is the inertia of K (Sylvester's law),
+        which the oracle reads from the dense eigenvalues (min D itself depends on the elimination
+        order and is not restated).  Eigenvalue (1): shift-invert Lanczos with
+        nev = min(floor(n/5), 10), ncv = 5 nev, selection LargestAlge of 1/(lambda - shift),
+        values ascending; without enough dofs for that, all eigenvalues (the dense branch)."""
+        if jacobian:
+            K = self.jacobian(self.U)
+            self.counts["jac"] += 1
+            self.solver.compute(K)
+            self.jacMat = K
+        bm = int(self.opts["BifurcationMethod"])
+        K = self.jacMat
+        if bm == 0:
+            self.stabilityVec = np.linalg.eigvalsh(K.toarray())
+        elif bm == 1:
+            number = min(int(np.floor(K.shape[0] / 5.0)), 10)
+            if number < 1 or 5 * number >= K.shape[0]:
+                self.stabilityVec = np.linalg.eigvalsh(K.toarray())[:max(number, 1)]
+            else:
+                import scipy.sparse.linalg as _spla
+                w = _spla.eigsh(K.tocsc(), k=number, sigma=shift, which="LA", ncv=5 * number, tol=1e-12,
+                                v0=np.ones(K.shape[0]), return_eigenvectors=False)
+                self.stabilityVec = np.sort(w)
+        else:
+            self.stabilityVec = np.zeros(K.shape[0])
+        self.negatives = int(np.sum(self.stabilityVec < 0))
+        self.indicator = float(np.min(self.stabilityVec))
+        self.stability = 1 if self.indicator < 0 else -1
+
+    def stability_change(self):
+        return self.stability * self.stabilityPrev < 0
 
     def apply_options(self):
         o = self.opts
@@ -404,10 +448,15 @@ class _ALMBase:
             self.predictor()
         self.compute_residual()
         self.compute_residual_norms()
+        self.stabilityPrev = self.stability
         for it in range(1, self.maxIt):
             self.num_iterations = it
             self.quasi_newton_iteration()
             self.iteration()
+            if int(self.opts["BifurcationMethod"]) in (0, 1):
+                self.compute_stability(jacobian=False)
+            else:
+                self.indicator, self.negatives, self.stability = 0.0, 0, -1
             self.compute_residual()
             self.compute_residual_norms()
             if self.residueF < self.tolF and self.residueU < self.tolU:
@@ -679,6 +728,68 @@ class ALMLoadControl(_ALMBase):
         self.L += self.DeltaL
 
 
+class ALMConsistentCrisfield(_ALMBase):
+    """gsALMConsistentCrisfield restated (gsALMConsistentCrisfield.hpp:22-209): secant predictor,
+    linearised constraint corrector (Carrera 1994, eqs. 20-21)."""
+
+    def apply_options(self):
+        super().apply_options()
+        self.phi = float(self.opts["Scaling"])
+        self.phi_user = self.phi != -1
+
+    def initiate_step(self):
+        self.DeltaU = np.zeros(self.numDof); self.deltaU = np.zeros(self.numDof)
+        self.DeltaL = self.deltaL = 0.0
+
+    def quasi_newton_iteration(self):
+        self.compute_jacobian()
+        self.compute_ut()
+
+    def _predict(self, dU_sec, dL_sec):
+        tol = 1e-10
+        if np.linalg.norm(dU_sec) < tol and dL_sec * dL_sec < tol:
+            DL = 1.0
+            self.deltaUt = self.solve_system(self.F)
+            den = np.sqrt(float(self.deltaUt @ self.deltaUt) + self.DeltaL * DL)
+            self.deltaU = self.deltaUt / den
+            self.deltaL = DL / den
+        else:
+            self.deltaL = dL_sec / self.arcLength_prev
+            self.deltaU = dU_sec / self.arcLength_prev
+        if not self.phi_user:
+            self.phi = np.sqrt(float(self.deltaUt @ self.deltaUt) / float(self.F @ self.F))
+        self.deltaL *= self.arcLength
+        self.deltaU = self.deltaU * self.arcLength
+        self.DeltaU = self.DeltaU + self.deltaU
+        self.DeltaL += self.deltaL
+
+    def predictor(self):
+        self.compute_jacobian()
+        self._predict(self.U - self.Uprev, self.L - self.Lprev)
+
+    def predictor_guess(self):
+        self.compute_jacobian()
+        self._predict(self.Uguess - self.U, self.Lguess - self.L)
+
+    def iteration(self):
+        self.compute_ubar()
+        FF = float(self.F @ self.F)
+        cres = float(self.DeltaU @ self.DeltaU) + self.phi ** 2 * self.DeltaL ** 2 * FF - self.arcLength ** 2
+        num = cres + 2.0 * float(self.DeltaU @ self.deltaUbar)
+        denum = 2.0 * float(self.DeltaU @ self.deltaUt) + self.phi ** 2 * 2.0 * self.DeltaL * FF
+        self.deltaL = -num / denum
+        self.deltaU = self.deltaL * self.deltaUt + self.deltaUbar
+        self.DeltaU = self.DeltaU + self.deltaU
+        self.DeltaL += self.deltaL
+
+    def iteration_finish(self):
+        self.converged = True
+        self.Uprev, self.Lprev = self.U.copy(), self.L
+        self.U = self.U + self.DeltaU
+        self.L += self.DeltaL
+        self.DeltaUold, self.DeltaLold = self.DeltaU.copy(), self.DeltaL
+
+
 # ---------------------------------------------------------------------------------------------
 # Eigen problems (Spectra stand-in: scipy ARPACK)
 # ---------------------------------------------------------------------------------------------
@@ -694,6 +805,24 @@ def buckling(K_lin, F, jacobian, nev=10, shift=0.0, scaling=1.0, tol=1e-10):
                             v0=v0)
     order = np.argsort(np.abs(vals))
     return vals[order], vecs[:, order], uL
+
+
+def buckling_dense(K_lin, F, jacobian, nev=10, shift=0.0, scaling=1.0):
+    """Dense variant of ``buckling`` for small pencils: B v = mu K_L v with K_L symmetric positive
+    definite (scipy.linalg.eigh), lambda = 1/mu; the nev eigenvalues nearest ``shift`` (the set
+    Spectra's Buckling mode targets), ordered by |lambda|.  Unlike ARPACK from a start vector it
+    cannot miss an eigenvalue of the requested set."""
+    import scipy.linalg as sla
+    lu = SuperLUSolver()
+    lu.compute(K_lin)
+    uL = lu.solve(scaling * F)
+    B = (jacobian(uL) - K_lin).toarray()
+    mu, V = sla.eigh(B, K_lin.toarray())
+    keep = np.abs(mu) > 1e-300
+    lam, V = 1.0 / mu[keep], V[:, keep]
+    sel = np.argsort(np.abs(lam - shift))[:nev]
+    order = sel[np.argsort(np.abs(lam[sel]))]
+    return lam[order], V[:, order], uL
 
 
 def modal(K, M, nev=10, shift=0.0, tol=1e-10):

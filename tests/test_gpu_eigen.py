@@ -38,3 +38,19 @@ def test_buckling_panel_matches_arpack(lib, oracle_mod):
     assert st == 0
     ref, rvecs, _ = oracle_mod.buckling(oa.linear(), oa.force(), oa.jacobian, nev=5, shift=shift)
     np.testing.assert_allclose(np.sort(vals), np.sort(ref), rtol=1e-6)
+
+
+def test_imperfection_modes_agree_with_oracle(lib, oracle_mod):
+    """The benchmark's imperfection (buckling modes of the coarse roof, sign fixed, transferred to
+    the fine spline space) is the same whether computed on the GPU or by the CPU oracle."""
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import learned
+    coarse, fine = P.cylindrical_panel(m=16, p=2), P.cylindrical_panel(m=32, p=2)
+    gm, gvals, st = learned.buckling_modes(G, fine, nmodes=5, shift=-0.5, scaling=1000.0, coarse=coarse)
+    assert st == 0
+    oa = oracle_mod.OracleAssembler(coarse)
+    vals, vecs, _ = oracle_mod.buckling_dense(oa.linear(), oa.force(), oa.jacobian, nev=5, shift=-0.5, scaling=1000.0)
+    om = [P.transfer_field(coarse, m, fine) for m in learned.sign_fixed_modes(coarse, vecs.T)]
+    np.testing.assert_allclose(np.sort(gvals), np.sort(vals), rtol=1e-6)
+    for a, b in zip(gm, om):
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()

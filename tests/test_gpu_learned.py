@@ -46,7 +46,7 @@ def _paths(G, seeds, modes, opts, nsteps):
 
 def test_learned_predictor_same_path_fewer_tangents(lib):
     import gsstructuralanalysis_gb300 as G
-    opts = dict(Length=0.0025, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25)
+    opts = dict(Length=0.0025, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
     base = P.cylindrical_panel(m=12, p=2, load=1.0)
     modes, _, st = learned.buckling_modes(G, base, nmodes=3, shift=-0.5)
     assert st == 0

@@ -105,11 +105,15 @@ def _truss():
     return fint, jac, np.array([1.0, 0.0])
 
 
-@pytest.mark.parametrize("cls", ["ALMCrisfield", "ALMRiks"])
+@pytest.mark.parametrize("cls", ["ALMCrisfield", "ALMRiks", "ALMConsistentCrisfield"])
 def test_arc_length_traces_snap_through(oracle_mod, cls):
     fint, jac, F = _truss()
     res = lambda x, lam: fint(x) - lam * F
-    alm = getattr(oracle_mod, cls)(jac, res, F, dict(Length=0.05, TolF=1e-10, TolU=1e-10, MaxIter=30))
+    opts = dict(Length=0.05, TolF=1e-10, TolU=1e-10, MaxIter=30)
+    if cls == "ALMConsistentCrisfield":
+        # with the automatic phi = |u_t|/|F| the secant predictor turns back at the limit point
+        opts["Scaling"] = 0.0
+    alm = getattr(oracle_mod, cls)(jac, res, F, opts)
     lams, us = [], []
     for _ in range(80):
         assert alm.step() == 0
@@ -124,6 +128,18 @@ def test_crisfield_constraint_is_met(oracle_mod):
     fint, jac, F = _truss()
     res = lambda x, lam: fint(x) - lam * F
     alm = oracle_mod.ALMCrisfield(jac, res, F, dict(Length=0.05, TolF=1e-12, TolU=1e-12, MaxIter=30, Scaling=0.0))
+    for _ in range(10):
+        U0 = alm.U.copy()
+        assert alm.step() == 0
+        assert abs(np.linalg.norm(alm.U - U0) - 0.05) < 1e-9
+
+
+def test_consistent_crisfield_constraint_is_met(oracle_mod):
+    """At convergence the linearised constraint of gsALMConsistentCrisfield is the spherical one."""
+    fint, jac, F = _truss()
+    res = lambda x, lam: fint(x) - lam * F
+    alm = oracle_mod.ALMConsistentCrisfield(jac, res, F, dict(Length=0.05, TolF=1e-12, TolU=1e-12, MaxIter=30,
+                                                              Scaling=0.0))
     for _ in range(10):
         U0 = alm.U.copy()
         assert alm.step() == 0
