@@ -441,7 +441,7 @@ def run_reference(args):
 # ---------------------------------------------------------------------------------------------
 BATCH_N = 256
 BATCH_SEED = 5000
-BATCH_OPTS = {"tol": 1e-8, "maxIt": 25}
+BATCH_OPTS = {"tol": 1e-8, "maxIt": 25, "Refinement": 1}
 BATCH_METRIC = "batched Newton solves/s, 256 uneven roof panels (16..96 elements, degree 2/3), |R|/|R0|<=1e-8"
 
 

@@ -99,6 +99,18 @@ __global__ void finalize_kernel(int n, const int* __restrict__ dof_inst, const i
     }
 }
 
+// y = A x over the merged CSR (FP32 values, FP64 vectors), one warp per row
+__global__ void csr_spmv_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ cols,
+                                const float* __restrict__ vals, const double* __restrict__ x, double* __restrict__ y) {
+    const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s = 0.0;
+    for (int z = rowptr[row] + lane; z < rowptr[row + 1]; z += 32) s += (double)vals[z] * x[cols[z]];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) y[row] = s;
+}
+
 __global__ void masked_axpy_kernel(int n, const int* __restrict__ dof_inst, const int* __restrict__ active, double a,
                                    const double* __restrict__ x, double* __restrict__ y) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -270,6 +282,7 @@ BatchedNewton::BatchedNewton(BatchedProblem& B, const Options& opt) : B_(B) {
     tolF_ = opt.real("tolF", -1) != -1 ? opt.real("tolF", -1) : tol;
     tolU_ = opt.real("tolU", -1) != -1 ? opt.real("tolU", -1) : tol;
     maxIt_ = (int)opt.integer("maxIt", 25);
+    refine_ = (int)opt.integer("Refinement", 1);
     relax_ = opt.real("Relaxation", 1.0);
     L_ = opt.real("LoadFactor", 1.0);
     if (maxIt_ < 1) throw std::invalid_argument("maxIt must be positive");
@@ -324,6 +337,18 @@ void BatchedNewton::iteration_launches() {
     vec::to_f32(R_.get(), b32_.get(), n, s);
     B_.mf->enqueue_solve(b32_.get(), x32_.get());
     vec::to_f64(x32_.get(), dU_.get(), n, s);
+    // iterative refinement of the Newton step against the assembled (FP32) tangent: removes most
+    // of the FP32 factorisation error, so thin, ill-conditioned panels converge in a few steps
+    for (int r = 0; r < refine_; ++r) {
+        csr_spmv_kernel<<<ceil_div((int64_t)n * 32, 256), 256, 0, s>>>(n, B_.d_rowptr.get(), B_.d_cols.get(),
+                                                                      B_.d_vals32.get(), dU_.get(), x_.get());
+        count_launch();
+        vec::lincomb(1.0, R_.get(), -1.0, x_.get(), x_.get(), n, s);
+        vec::to_f32(x_.get(), b32_.get(), n, s);
+        B_.mf->enqueue_solve(b32_.get(), x32_.get());
+        vec::to_f64(x32_.get(), x_.get(), n, s);
+        vec::axpby(1.0, x_.get(), 1.0, dU_.get(), n, s);
+    }
     masked_axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, B_.d_dof_inst.get(), active_.get(), relax_, dU_.get(),
                                                        DU_.get());
     count_launch();

@@ -97,7 +97,7 @@ private:
     void iteration_launches();
     BatchedProblem& B_;
     double tolF_, tolU_, relax_, L_;
-    int maxIt_;
+    int maxIt_, refine_ = 1;
     DevBuf<double> U_, DU_, dU_, R_, x_, fint_, norms_, resIni_;
     DevBuf<float> b32_, x32_;
     DevBuf<int> active_, fin_, st_, its_, it_, count_;

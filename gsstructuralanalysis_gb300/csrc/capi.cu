@@ -201,7 +201,8 @@ int klsa_solver_create(klsa_problem* prob, const char* name, const klsa_options*
     return guarded([&] {
         Options o = opt ? opt->o : Options();
         auto s = make_linear_solver(*prob->P, name, (int)o.integer("Refinement", 0), o.real("RefineTol", 1e-12),
-                                    (int)o.integer("CGMaxIterations", 0), o.real("CGTolerance", 1e-10));
+                                    (int)o.integer("CGMaxIterations", 0), o.real("CGTolerance", 1e-10),
+                                    (int)o.integer("FrontPrecision", 32));
         if (!s) {
             g_err = std::string("unknown solver name ") + name;
             return KLSA_INVALID_ARGUMENT;

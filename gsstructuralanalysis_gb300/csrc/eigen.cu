@@ -296,7 +296,10 @@ int run_pencil(Problem& P, const Options& opt, const double* valsA, const double
     combine_kernel<<<ceil_div(nnz, 256), 256, 0, P.stream>>>(nnz, 1.0, valsA, -shift, valsB, P.d_vals64.get());
     count_launch();
     if (P.d_vals32.size() < (size_t)nnz) P.d_vals32.alloc(nnz);
-    MFSolver S(P, (int)opt.integer("Refinement", 12), opt.real("RefineTol", 1e-13));
+    // FP64 fronts by default: the FP32 factor of a large thin-shell pencil is too inaccurate for
+    // iterative refinement to converge ("FrontPrecision" 32 selects FP32 fronts + refinement)
+    MFSolver S(P, (int)opt.integer("Refinement", 12), opt.real("RefineTol", 1e-13),
+               opt.integer("FrontPrecision", 64) == 64);
     if (S.factor_current(true) != ST_SUCCESS) return ST_SOLVER_ERROR;
     // copy C values (they may alias a scratch buffer that the factorisation keeps)
     DevBuf<double> valsC(nnz);
@@ -353,7 +356,8 @@ int buckling_gpu(Problem& P, const Options& opt, int nev, double shift, double s
     P.tangent_f64();
     KL_CUDA(cudaMemcpyAsync(KL.get(), P.d_vals64.get(), sizeof(double) * nnz, cudaMemcpyDeviceToDevice, P.stream));
     {
-        MFSolver S(P, (int)opt.integer("Refinement", 12), opt.real("RefineTol", 1e-13));
+        MFSolver S(P, (int)opt.integer("Refinement", 12), opt.real("RefineTol", 1e-13),
+                   opt.integer("FrontPrecision", 64) == 64);
         if (S.factor_current(true) != ST_SUCCESS) return ST_SOLVER_ERROR;
         vec::lincomb(scaling, P.d_F.get(), 0.0, P.d_F.get(), rhs.get(), n, P.stream);
         S.solve(rhs.get(), uL.get(), 1);

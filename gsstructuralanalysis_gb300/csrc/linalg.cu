@@ -131,8 +131,10 @@ void multidot(int npairs, const double* const* xs, const double* const* ys, int6
 // ------------------------------------------------------------------------------------------
 // Multifrontal LDL^T (+ optional FP64 iterative refinement)
 // ------------------------------------------------------------------------------------------
-MFSolver::MFSolver(Problem& P, int refine, double refine_tol) : P_(P), refine_(refine), tol_(refine_tol) {
-    P_.solver();
+MFSolver::MFSolver(Problem& P, int refine, double refine_tol, bool fp64)
+    : P_(P), refine_(refine), tol_(refine_tol), fp64_(fp64) {
+    if (fp64_) P_.solver64();
+    else P_.solver();
     int n = P_.nfree;
     b32_.alloc((size_t)n * MF_MAX_RHS);
     x32_.alloc((size_t)n * MF_MAX_RHS);
@@ -141,6 +143,15 @@ MFSolver::MFSolver(Problem& P, int refine, double refine_tol) : P_(P), refine_(r
 }
 
 int MFSolver::factor_current(bool f64_for_refine) {
+    if (fp64_) {
+        // FP64 fronts straight from the FP64 values
+        if (P_.d_vals64.size() < (size_t)P_.nnz) throw std::logic_error("FP64 matrix values missing");
+        has64_ = true;
+        cudaEvent_t ev = g_timer.begin(P_.stream);
+        P_.solver64().factorize_async(P_.d_vals64.get());
+        g_timer.end(P_.stream, 1, ev);
+        return P_.solver64().read_status();
+    }
     // the caller assembled values into P_.d_vals32 (and d_vals64 when refining)
     if (f64_for_refine) {
         if (P_.d_vals64.size() < (size_t)P_.nnz) throw std::logic_error("FP64 matrix values missing");
@@ -158,7 +169,7 @@ int MFSolver::factor_current(bool f64_for_refine) {
 
 int MFSolver::compute_tangent() {
     cudaEvent_t ev = g_timer.begin(P_.stream);
-    if (refine_ > 0) P_.tangent_f64();
+    if (refine_ > 0 || fp64_) P_.tangent_f64();
     else P_.tangent_f32();
     g_timer.end(P_.stream, 0, ev);
     return factor_current(refine_ > 0);
@@ -167,6 +178,11 @@ int MFSolver::compute_tangent() {
 void MFSolver::solve_raw(const double* d_b, double* d_x, int nrhs) {
     int n = P_.nfree;
     cudaEvent_t ev = g_timer.begin(P_.stream);
+    if (fp64_) {
+        P_.solver64().solve(d_b, d_x, nrhs);
+        g_timer.end(P_.stream, 2, ev);
+        return;
+    }
     vec::to_f32(d_b, b32_.get(), (int64_t)n * nrhs, P_.stream);
     P_.solver().solve(b32_.get(), x32_.get(), nrhs);
     vec::to_f64(x32_.get(), d_x, (int64_t)n * nrhs, P_.stream);
@@ -205,7 +221,10 @@ int MFSolver::solve(const double* d_b, double* d_x, int nrhs) {
     return ST_SUCCESS;
 }
 
-void MFSolver::stability(double* min_d, int64_t* neg) { P_.solver().stability(min_d, neg); }
+void MFSolver::stability(double* min_d, int64_t* neg) {
+    if (fp64_) P_.solver64().stability(min_d, neg);
+    else P_.solver().stability(min_d, neg);
+}
 
 // ------------------------------------------------------------------------------------------
 // Jacobi-preconditioned CG ("CGDiagonal": Eigen ConjugateGradient + DiagonalPreconditioner)
@@ -268,9 +287,10 @@ int PCGSolver::solve(const double* d_b, double* d_x, int nrhs) {
 }
 
 std::unique_ptr<LinearSolver> make_linear_solver(Problem& P, const std::string& name, int refine, double refine_tol,
-                                                 int cg_max_it, double cg_tol) {
+                                                 int cg_max_it, double cg_tol, int front_precision) {
+    if (front_precision != 32 && front_precision != 64) throw std::invalid_argument("FrontPrecision must be 32 or 64");
     if (name == "SimplicialLDLT" || name == "GPUMultifrontalLDLT" || name == "SimplicialLLT" || name == "LDLT")
-        return std::unique_ptr<LinearSolver>(new MFSolver(P, refine, refine_tol));
+        return std::unique_ptr<LinearSolver>(new MFSolver(P, refine, refine_tol, front_precision == 64));
     if (name == "CGDiagonal" || name == "GPUPCG" || name == "ConjugateGradient")
         return std::unique_ptr<LinearSolver>(new PCGSolver(P, cg_max_it, cg_tol));
     return nullptr;

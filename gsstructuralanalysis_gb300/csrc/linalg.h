@@ -21,9 +21,12 @@ public:
     virtual int last_iterations() const { return 0; }
 };
 
+// Multifrontal LDL^T.  fp64 = false: FP32 fronts (FP32 or FP64-assembled values rounded), with
+// optional FP64 iterative refinement against the FP64 values; fp64 = true: FP64 fronts from the
+// FP64 values, vectors stay FP64 end to end (option "FrontPrecision" = 64).
 class MFSolver : public LinearSolver {
 public:
-    MFSolver(Problem& P, int refine, double refine_tol);
+    MFSolver(Problem& P, int refine, double refine_tol, bool fp64 = false);
     int compute_tangent() override;
     int factor_current(bool f64_for_refine);
     int solve(const double* d_b, double* d_x, int nrhs) override;
@@ -37,6 +40,7 @@ private:
     Problem& P_;
     int refine_;
     double tol_;
+    bool fp64_ = false;
     bool has64_ = false;
     int last_refine_its_ = 0;
     DevBuf<float> b32_, x32_;
@@ -59,6 +63,6 @@ private:
 };
 
 std::unique_ptr<LinearSolver> make_linear_solver(Problem& P, const std::string& name, int refine, double refine_tol,
-                                                 int cg_max_it, double cg_tol);
+                                                 int cg_max_it, double cg_tol, int front_precision = 32);
 
 }  // namespace klsa

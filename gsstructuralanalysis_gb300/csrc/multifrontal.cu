@@ -21,8 +21,9 @@ namespace {
 
 constexpr int NB = MF_NB;
 
-__global__ void mf_scatter_kernel(int64_t nnz, const int64_t* __restrict__ fpos, const float* __restrict__ vals,
-                                  float* __restrict__ pool) {
+template <class T>
+__global__ void mf_scatter_kernel(int64_t nnz, const int64_t* __restrict__ fpos, const T* __restrict__ vals,
+                                  T* __restrict__ pool) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < nnz) {
         int64_t p = fpos[i];
@@ -33,11 +34,12 @@ __global__ void mf_scatter_kernel(int64_t nnz, const int64_t* __restrict__ fpos,
 // Extend-add of 8 columns of a child's Schur complement into its parent's front: one warp per
 // column, lanes stride over the rows (4 independent read-modify-writes in flight per lane).
 constexpr int EA_COLS = 8;
+template <class T>
 __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restrict__ items, const int* __restrict__ f,
                                                             const int* __restrict__ k, const int* __restrict__ parent,
                                                             const int64_t* __restrict__ front_off,
                                                             const int64_t* __restrict__ map_off,
-                                                            const int* __restrict__ map, float* pool) {
+                                                            const int* __restrict__ map, T* pool) {
     int4 it = items[blockIdx.x];
     int c = it.x;
     int a = it.y + (threadIdx.x >> 5);
@@ -47,11 +49,11 @@ __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restri
     int par = parent[c];
     int fp = f[par];
     const int* mp = map + map_off[c];
-    const float* scol = pool + front_off[c] + (int64_t)(kc + a) * fc + kc;
-    float* dcol = pool + front_off[par] + (int64_t)mp[a] * fp;
+    const T* scol = pool + front_off[c] + (int64_t)(kc + a) * fc + kc;
+    T* dcol = pool + front_off[par] + (int64_t)mp[a] * fp;
     int b = a + lane;
     for (; b + 96 < hc; b += 128) {
-        float v0 = scol[b], v1 = scol[b + 32], v2 = scol[b + 64], v3 = scol[b + 96];
+        T v0 = scol[b], v1 = scol[b + 32], v2 = scol[b + 64], v3 = scol[b + 96];
         int m0 = mp[b], m1 = mp[b + 32], m2 = mp[b + 64], m3 = mp[b + 96];
         dcol[m0] += v0;
         dcol[m1] += v1;
@@ -61,127 +63,149 @@ __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restri
     for (; b < hc; b += 32) dcol[mp[b]] += scol[b];
 }
 
-// Diagonal tile (kk <= 64 pivots), 256 threads.  Every entry of the packed lower triangle of the
-// 64x64 tile (e = r(r+1)/2 + c) lives in a register of a fixed owner (thread e % 256, slot
-// e / 256); rows and columns beyond kk are padded with the identity.
-//   LDL^T, right-looking: step j, the owners of column j publish it to shared memory (double
-//   buffered), one barrier, then every thread applies -A(r,j) A(c,j) / d_j to its entries with
-//   c > j and scales its column-j entries to L(r,j).
-//   X = L^-1 (unit lower), same ownership: step j publishes row j of X, rows r > j subtract
-//   L(r,j) X(j,:).
-// Writes L (strict lower) and D (diagonal) into the front, D into Dvec and X into the tile's slot
-// of linv (row-major), which the panel GEMM and the triangular solves use.
-constexpr int DIAG_SLOTS = (NB * (NB + 1) / 2 + 255) / 256;
-__global__ void __launch_bounds__(256) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
-                                                      const int* __restrict__ k, const int* __restrict__ own,
-                                                      const int64_t* __restrict__ front_off,
-                                                      const int64_t* __restrict__ linv_off, float* pool, float* Dvec,
-                                                      float* linv, int* status) {
-    __shared__ float Ls[NB][NB + 1];
-    __shared__ float buf[2][NB];
+// Diagonal tile (kk <= 64 pivots), DIAG_THREADS threads.  Thread t owns a chunk of one column c
+// of the tile -- rows [r0, r0 + CH) with r0 >= c -- both of the tile A (becoming L and D) and of
+// X = L^-1 (unit lower); rows and columns beyond kk are padded with the identity.  Step j (one
+// barrier): the owners of column j publish A(:, j) and the owner of the pivot 1/d_j; the owners
+// of row j of X publish X(j, :).  Then columns c > j take the rank-1 update
+// A(r, c) -= A(r, j) A(c, j) / d_j, column j is scaled to L(:, j), and columns c <= j of X take
+// X(r, c) -= L(r, j) X(j, c) for r > j.  The chains of LDL^T and of the inverse advance in the
+// same 64 steps.  The update is branch-free (selects) with the chunk's column values loaded into
+// registers before use, and chunks are short so that 16 warps share the per-step latency.
+// Writes L (strict lower) and D into the front, D into Dvec and X into the tile's slot of linv
+// (row-major), which the panel GEMM and the triangular solves use.
+constexpr int DIAG_THREADS = 512;
+constexpr int DCH = 5;   // rows per chunk: sum_c ceil((64 - c) / 5) = 442 chunks <= 512 threads
+
+template <int CH>
+__device__ __forceinline__ void diag_chunk(int tid, int& c, int& r0) {
+    c = -1;
+    r0 = NB;
+    int t = tid;
+    for (int cc = 0; cc < NB; ++cc) {
+        const int nch = (NB - cc + CH - 1) / CH;
+        if (t < nch) {
+            c = cc;
+            r0 = cc + t * CH;
+            return;
+        }
+        t -= nch;
+    }
+}
+
+template <class T, int CH>
+__device__ __forceinline__ T sel_row(const T (&v)[CH], int k) {
+    T r = v[0];
+#pragma unroll
+    for (int q = 1; q < CH; ++q) r = (k == q) ? v[q] : r;
+    return r;
+}
+
+template <class T, int NT, int CH>
+__global__ void __launch_bounds__(NT) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
+                                                     const int* __restrict__ k, const int* __restrict__ own,
+                                                     const int64_t* __restrict__ front_off,
+                                                     const int64_t* __restrict__ linv_off, T* pool, T* Dvec, T* linv,
+                                                     int* status) {
+    __shared__ T col[2][NB];
+    __shared__ T xrow[2][NB];
+    __shared__ T sinv[2];
     __shared__ int bad;
     const int nd = items[blockIdx.x].x;
     const int fN = f[nd], kN = k[nd];
     const int c0 = t * NB;
     const int kk = min(NB, kN - c0);
-    float* F = pool + front_off[nd];
+    T* F = pool + front_off[nd];
     const int tid = threadIdx.x;
+    int c, r0;
+    diag_chunk<CH>(tid, c, r0);
+    T a[CH], x[CH];
+    int rc[CH];   // rows of the chunk clamped into the tile (slots beyond row 63 are never written back)
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        const int r = r0 + i;
+        const bool in = c >= 0 && r < NB;
+        a[i] = !in ? T(0) : (r < kk ? F[(int64_t)(c0 + c) * fN + c0 + r] : (r == c ? T(1) : T(0)));
+        x[i] = (in && r == c) ? T(1) : T(0);
+        rc[i] = min(r, NB - 1);
+    }
+    const int cc = c < 0 ? 0 : c;
     if (tid == 0) bad = 0;
-    // stage the tile, column-major walk (coalesced)
-    for (int e = tid; e < NB * NB; e += 256) {
-        const int c = e / NB, r = e % NB;
-        Ls[r][c] = (r < kk && c <= r) ? F[(int64_t)(c0 + c) * fN + c0 + r] : 0.f;
-    }
-    int rr[DIAG_SLOTS], cc[DIAG_SLOTS];
-    float v[DIAG_SLOTS];
-#pragma unroll
-    for (int q = 0; q < DIAG_SLOTS; ++q) {
-        const int e = tid + 256 * q;
-        int r = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);
-        while (r * (r + 1) / 2 > e) --r;
-        while ((r + 1) * (r + 2) / 2 <= e) ++r;
-        const bool live = e < NB * (NB + 1) / 2;
-        rr[q] = live ? r : -1;
-        cc[q] = live ? e - r * (r + 1) / 2 : NB;
-    }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < DIAG_SLOTS; ++q) {
-        const int r = rr[q], c = cc[q];
-        v[q] = (r < 0) ? 0.f : (r < kk ? Ls[r][c] : (r == c ? 1.f : 0.f));
-    }
     for (int j = 0; j < NB; ++j) {
-        float* b = buf[j & 1];
+        const int b = j & 1;
+        if (c == j) {
 #pragma unroll
-        for (int q = 0; q < DIAG_SLOTS; ++q)
-            if (cc[q] == j) b[rr[q]] = v[q];
-        __syncthreads();
-        float d = b[j];
-        if (!(fabsf(d) > 0.f) || !isfinite(d)) {
-            d = 1.f;
-            if (tid == 0) bad = 1;
+            for (int i = 0; i < CH; ++i)
+                if (r0 + i < NB) col[b][r0 + i] = a[i];
+            if (r0 == j) {
+                T d = a[0];
+                if (!(fabs(d) > T(0)) || !isfinite(d)) {
+                    if (j < kk) bad = 1;
+                    d = T(1);
+                }
+                sinv[b] = T(1) / d;
+            }
         }
-        const float inv = 1.f / d;
+        if (c >= 0 && c <= j && j >= r0 && j < r0 + CH) xrow[b][c] = sel_row<T, CH>(x, j - r0);
+        __syncthreads();
+        const T inv = sinv[b];
+        const T cv = col[b][cc], xr = xrow[b][cc];
+        T v[CH];
 #pragma unroll
-        for (int q = 0; q < DIAG_SLOTS; ++q) {
-            if (cc[q] > j && cc[q] < NB) v[q] -= b[rr[q]] * inv * b[cc[q]];
-            else if (cc[q] == j && rr[q] > j) v[q] *= inv;
+        for (int i = 0; i < CH; ++i) v[i] = col[b][rc[i]];
+        const bool upd_a = c > j, scale_a = c == j, upd_x = c >= 0 && c <= j;
+        const T fa = upd_a ? cv * inv : T(0);
+        const T xv = upd_x ? xr * inv : T(0);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+            const bool below = r0 + i > j;
+            const T an = fma(-v[i], fa, a[i]);
+            a[i] = upd_a ? an : ((scale_a && below) ? a[i] * inv : a[i]);
+            const T xn = fma(-v[i], xv, x[i]);
+            x[i] = (upd_x && below) ? xn : x[i];
         }
     }
-    // L and D back to shared memory (the front and the inverse read them from there)
+    T* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
 #pragma unroll
-    for (int q = 0; q < DIAG_SLOTS; ++q)
-        if (rr[q] >= 0) Ls[rr[q]][cc[q]] = v[q];
+    for (int i = 0; i < CH; ++i) {
+        const int r = r0 + i;
+        if (c >= 0 && r < NB) {
+            if (r < kk) F[(int64_t)(c0 + c) * fN + c0 + r] = a[i];
+            Li[r * NB + c] = r < kk ? x[i] : T(0);
+        }
+    }
+    if (c >= 0 && r0 == c && c < kk) Dvec[own[nd] + c0 + c] = a[0];
+    for (int e = tid; e < NB * NB; e += NT)
+        if (e % NB > e / NB) Li[e] = T(0);
     __syncthreads();
-    for (int e = tid; e < NB * NB; e += 256) {
-        const int c = e / NB, r = e % NB;
-        if (r < kk && c <= r) F[(int64_t)(c0 + c) * fN + c0 + r] = Ls[r][c];
-    }
-    if (tid < kk) Dvec[own[nd] + c0 + tid] = Ls[tid][tid];
-    // X = L^-1
-#pragma unroll
-    for (int q = 0; q < DIAG_SLOTS; ++q) v[q] = (rr[q] >= 0 && rr[q] == cc[q]) ? 1.f : 0.f;
-    for (int j = 0; j < NB; ++j) {
-        float* b = buf[j & 1];
-#pragma unroll
-        for (int q = 0; q < DIAG_SLOTS; ++q)
-            if (rr[q] == j) b[cc[q]] = v[q];
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < DIAG_SLOTS; ++q)
-            if (rr[q] > j && cc[q] <= j) v[q] -= Ls[rr[q]][j] * b[cc[q]];
-    }
-    float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-#pragma unroll
-    for (int q = 0; q < DIAG_SLOTS; ++q)
-        if (rr[q] >= 0) Li[rr[q] * NB + cc[q]] = rr[q] < kk ? v[q] : 0.f;
-    for (int e = tid; e < NB * NB; e += 256)
-        if (e % NB > e / NB) Li[e] = 0.f;
-    if (tid == 0 && bad && kk > 0) atomicExch(status, 1);
+    if (tid == 0 && bad) atomicExch(status, 1);
 }
 
 // Panel rows [r0, r0 + 64) below the diagonal tile: W = A21 X^T (X = L11^-1 from the diagonal
 // kernel), L21 = W D^-1 written in place and W kept for the trailing update.  A 64 x 64 x kk
 // product per CTA: thread (tx, ty) owns rows tx + 16 i and columns ty + 16 q.
+template <class T>
 __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                        const int* __restrict__ k, const int64_t* __restrict__ front_off,
                                                        const int64_t* __restrict__ linv_off,
-                                                       const int64_t* __restrict__ ws_off, float* pool,
-                                                       const float* __restrict__ linv, float* ws) {
-    __shared__ float As[NB][NB + 1];   // As[m][rr] = A21(r0 + rr, m)
-    __shared__ float Xs[NB][NB + 1];   // Xs[m][jj] = X(jj, m)
-    __shared__ float Ds[NB];
+                                                       const int64_t* __restrict__ ws_off, T* pool,
+                                                       const T* __restrict__ linv, T* ws) {
+    extern __shared__ unsigned char smem_raw[];
+    T(*As)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);              // As[m][rr] = A21(r0 + rr, m)
+    T(*Xs)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));   // Xs[m][jj] = X(jj, m)
+    T* Ds = reinterpret_cast<T*>(smem_raw + 2 * sizeof(T) * NB * (NB + 1));
     const int4 it = items[blockIdx.x];
     const int nd = it.x, r0 = it.y;
     const int fN = f[nd], kN = k[nd];
     const int c0 = t * NB;
     const int kk = min(NB, kN - c0);
-    float* F = pool + front_off[nd];
-    const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
+    T* F = pool + front_off[nd];
+    const T* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
     {
-        float va[16], vx[16];
+        T va[16], vx[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             const int m = lg + 4 * q;
@@ -196,13 +220,13 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
         if (threadIdx.x < NB) Ds[threadIdx.x] = threadIdx.x < kk ? F[(int64_t)(c0 + threadIdx.x) * fN + c0 + threadIdx.x] : 1.f;
     }
     __syncthreads();
-    float acc[4][4];
+    T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[i][q] = 0.f;
     for (int m = 0; m < kk; ++m) {
-        float a[4], b[4];
+        T a[4], b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = As[m][tx + 16 * i];
 #pragma unroll
@@ -210,14 +234,14 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(a[i], b[q], acc[i][q]);
+            for (int q = 0; q < 4; ++q) acc[i][q] = fma(a[i], b[q], acc[i][q]);
     }
-    float* W = ws + ws_off[nd];
+    T* W = ws + ws_off[nd];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int j = ty + 16 * q;
         if (j >= kk) continue;
-        const float dinv = 1.f / Ds[j];
+        const T dinv = 1.f / Ds[j];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int R = r0 + tx + 16 * i;
@@ -230,12 +254,14 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
 }
 
 // Trailing update of one 64x64 lower tile: A[R, C] -= W[R, :] L[C, :]^T.
+template <class T>
 __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                         const int* __restrict__ k, const int64_t* __restrict__ front_off,
-                                                        const int64_t* __restrict__ ws_off, float* pool,
-                                                        const float* __restrict__ ws) {
-    __shared__ float Ws[NB][NB + 1];   // Ws[m][rr] = W[R0+rr][m]
-    __shared__ float Ls[NB][NB + 1];   // Ls[m][cc] = L[C0+cc][c0+m]
+                                                        const int64_t* __restrict__ ws_off, T* pool,
+                                                        const T* __restrict__ ws) {
+    extern __shared__ unsigned char smem_raw[];
+    T(*Ws)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);                              // Ws[m][rr] = W[R0+rr][m]
+    T(*Ls)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));  // Ls[m][cc] = L[C0+cc][c0+m]
     int4 it = items[blockIdx.x];
     int nd = it.x;
     int fN = f[nd], kN = k[nd];
@@ -243,12 +269,12 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
     int kk = min(NB, kN - c0);
     int c1 = c0 + kk;
     int R0 = c1 + it.y * NB, C0 = c1 + it.z * NB;
-    float* F = pool + front_off[nd];
-    const float* W = ws + ws_off[nd];
+    T* F = pool + front_off[nd];
+    const T* W = ws + ws_off[nd];
     int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
     {
-        float vw[16], vl[16];
+        T vw[16], vl[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
             int m = lg + 4 * q;
@@ -262,13 +288,13 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
         }
     }
     __syncthreads();
-    float acc[4][4];
+    T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[i][q] = 0.f;
     for (int m = 0; m < kk; ++m) {
-        float a[4], b[4];
+        T a[4], b[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = Ws[m][tx + 16 * i];
 #pragma unroll
@@ -276,9 +302,9 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = fmaf(a[i], b[q], acc[i][q]);
+            for (int q = 0; q < 4; ++q) acc[i][q] = fma(a[i], b[q], acc[i][q]);
     }
-    float old[4][4];
+    T old[4][4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         int C = C0 + ty + 16 * q;
@@ -299,198 +325,318 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
     }
 }
 
-// Forward substitution of one node: children's update vectors, unit-lower solve of the own
-// block (inverse diagonal tiles staged in shared memory), update vector of the halo.  Row loops
-// are unrolled so that every thread keeps 16 independent loads of L in flight.
-constexpr int SOLVE_THREADS = 512;
+// ---- node inverses X = L11^-1 (k x k, row-major, lower) for the triangular solves -------------
+// Diagonal blocks: copies of the tile inverses written by the diagonal kernel.
+template <class T>
+__global__ void __launch_bounds__(256) mf_xdiag_kernel(const int4* __restrict__ items, const int* __restrict__ k,
+                                                       const int64_t* __restrict__ linv_off,
+                                                       const int64_t* __restrict__ xinv_off,
+                                                       const T* __restrict__ linv, T* __restrict__ xinv) {
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, bi = it.y, kN = k[nd];
+    const int c0 = bi * NB, kk = min(NB, kN - c0);
+    const T* Li = linv + linv_off[nd] + (int64_t)bi * NB * NB;
+    T* X = xinv + xinv_off[nd];
+    for (int e = threadIdx.x; e < NB * NB; e += 256) {
+        const int r = e / NB, c = e % NB;
+        if (r < kk && c < kk) X[(int64_t)(c0 + r) * kN + c0 + c] = Li[e];
+    }
+}
 
-template <int NR>
-__global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_kernel(const int4* __restrict__ items, int n,
-                                                     const int* __restrict__ f, const int* __restrict__ k,
-                                                     const int* __restrict__ own, const int* __restrict__ child0,
-                                                     const int* __restrict__ child1,
-                                                     const int64_t* __restrict__ front_off,
-                                                     const int64_t* __restrict__ linv_off,
-                                                     const int64_t* __restrict__ upd_off,
-                                                     const int64_t* __restrict__ map_off, const int* __restrict__ map,
-                                                     const float* __restrict__ pool, const float* __restrict__ linv,
-                                                     float* upd, const float* __restrict__ b, float* y) {
-    extern __shared__ float rhs[];   // fN * NR
-    __shared__ float Ls[NB][NB + 1];
-    __shared__ float yt[NR][NB];
-    int nd = items[blockIdx.x].x;
-    int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
-    const float* F = pool + front_off[nd];
+// Block row bi of X, block column bj < bi: X(bi, bj) = -X(bi, bi) sum_{m=bj}^{bi-1} L(bi, m) X(m, bj).
+// One CTA per output tile; thread (tx, ty) owns rows tx + 16 i and columns ty + 16 q.
+template <class T>
+__global__ void __launch_bounds__(256) mf_xoff_kernel(const int4* __restrict__ items, const int* __restrict__ f,
+                                                      const int* __restrict__ k, const int64_t* __restrict__ front_off,
+                                                      const int64_t* __restrict__ linv_off,
+                                                      const int64_t* __restrict__ xinv_off, const T* __restrict__ pool,
+                                                      const T* __restrict__ linv, T* __restrict__ xinv) {
+    extern __shared__ unsigned char smem_raw[];
+    T(*As)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);                               // As[q][r] = L(bi, m)(r, q)
+    T(*Bs)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));   // Bs[q][c] = X(m, bj)(q, c)
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, bi = it.y, bj = it.z;
+    const int fN = f[nd], kN = k[nd];
+    const int ri = bi * NB, kki = min(NB, kN - ri), cj = bj * NB;
+    const T* F = pool + front_off[nd];
+    T* X = xinv + xinv_off[nd];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[i][q] = T(0);
+    for (int bm = bj; bm < bi; ++bm) {
+        const int cm = bm * NB;
+        __syncthreads();
+        {
+            T va[16], vb[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int qq = lg + 4 * q;
+                va[q] = lt < kki ? F[(int64_t)(cm + qq) * fN + ri + lt] : T(0);   // L(ri + lt, cm + qq)
+                vb[q] = X[(int64_t)(cm + qq) * kN + cj + lt];                   // X(cm + qq, cj + lt)
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                As[lg + 4 * q][lt] = va[q];
+                Bs[lg + 4 * q][lt] = vb[q];
+            }
+        }
+        __syncthreads();
+        for (int q = 0; q < NB; ++q) {
+            T av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = As[q][tx + 16 * i];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bv[c] = Bs[q][ty + 16 * c];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[i][c] = fma(av[i], bv[c], acc[i][c]);
+        }
+    }
+    // S -> shared (Bs[r][c]), X(bi, bi) -> shared (As[r][q] = Xii(r, q)), out = -Xii S
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Bs[tx + 16 * i][ty + 16 * c] = acc[i][c];
+    const T* Li = linv + linv_off[nd] + (int64_t)bi * NB * NB;
+    for (int e = threadIdx.x; e < NB * NB; e += 256) As[e / NB][e % NB] = Li[e];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[i][c] = T(0);
+    for (int q = 0; q < NB; ++q) {
+        T av[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) av[i] = As[tx + 16 * i][q];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) bv[c] = Bs[q][ty + 16 * c];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[i][c] = fma(av[i], bv[c], acc[i][c]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = tx + 16 * i;
+        if (r < kki)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) X[(int64_t)(ri + r) * kN + cj + ty + 16 * c] = -acc[i][c];
+    }
+}
+
+// ---- triangular solves, five launches per level, many CTAs per front ---------------------------
+// Forward, leaves first: (1) gather b and the children's update vectors into the own part (y) and
+// the halo part (upd) of every node; (2) z_own = X r_own (row blocks); (3) u = r_halo - L21 z_own
+// (halo row blocks).  Backward, root first: (4) w = D^-1 z_own - L21^T x_halo (own column
+// blocks); (5) x_own = X^T w (own column blocks).  Vectors: n x NR, column stride n.
+constexpr int SOLVE_THREADS = 256;
+
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_gather_kernel(
+    const int4* __restrict__ items, int n, const int* __restrict__ f, const int* __restrict__ k,
+    const int* __restrict__ own, const int* __restrict__ child0, const int* __restrict__ child1,
+    const int64_t* __restrict__ upd_off, const int64_t* __restrict__ map_off, const int* __restrict__ map,
+    const T* __restrict__ b, T* __restrict__ y, T* upd) {
+    const int nd = items[blockIdx.x].x;
+    const int kN = k[nd], hN = f[nd] - kN, o = own[nd];
+    T* u = upd + upd_off[nd];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+        for (int r = threadIdx.x; r < kN; r += blockDim.x) y[o + r + (int64_t)n * q] = b[o + r + (int64_t)n * q];
+        for (int a = threadIdx.x; a < hN; a += blockDim.x) u[a + hN * q] = T(0);
+    }
+    const int chs[2] = {child0[nd], child1[nd]};
+    for (int s = 0; s < 2; ++s) {
+        __syncthreads();
+        const int c = chs[s];
+        if (c < 0) continue;
+        const int hc = f[c] - k[c];
+        const int* mp = map + map_off[c];
+        const T* uc = upd + upd_off[c];
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+            for (int a = threadIdx.x; a < hc; a += blockDim.x) {
+                const int pos = mp[a];
+                if (pos < kN) y[o + pos + (int64_t)n * q] += uc[a + hc * q];
+                else u[pos - kN + hN * q] += uc[a + hc * q];
+            }
+    }
+}
+
+// z_own(i) = sum_{m <= i} X(i, m) y_own(m); warp w handles rows rb*64 + w*8 .. +8, lanes over m.
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_own_kernel(
+    const int4* __restrict__ items, int n, const int* __restrict__ k, const int* __restrict__ own,
+    const int64_t* __restrict__ xinv_off, const T* __restrict__ xinv, const T* __restrict__ y, T* __restrict__ z) {
+    extern __shared__ unsigned char smem_raw[];
+    T* ys = reinterpret_cast<T*>(smem_raw);   // kN * NR
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, rb = it.y;
+    const int kN = k[nd], o = own[nd];
+    const int r1 = min(kN, (rb + 1) * NB);
 #pragma unroll
     for (int q = 0; q < NR; ++q)
-        for (int r = threadIdx.x; r < fN; r += blockDim.x) rhs[r + fN * q] = (r < kN) ? b[o + r + (int64_t)n * q] : 0.f;
+        for (int m = threadIdx.x; m < r1; m += blockDim.x) ys[m + kN * q] = y[o + m + (int64_t)n * q];
     __syncthreads();
-    int chs[2] = {child0[nd], child1[nd]};
-    for (int s = 0; s < 2; ++s) {
-        int c = chs[s];
-        if (c >= 0) {
-            int hc = f[c] - k[c];
-            const int* mp = map + map_off[c];
-            const float* u = upd + upd_off[c];
+    const T* X = xinv + xinv_off[nd];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int rr = 0; rr < 8; ++rr) {
+        const int i = rb * NB + warp * 8 + rr;
+        if (i >= kN) break;
+        const T* xr = X + (int64_t)i * kN;
+        T s[NR];
+#pragma unroll
+        for (int q = 0; q < NR; ++q) s[q] = T(0);
+        for (int m = lane; m <= i; m += 32) {
+            const T xv = xr[m];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) s[q] += xv * ys[m + kN * q];
+        }
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            T v = s[q];
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) z[o + i + (int64_t)n * q] = v;
+        }
+    }
+}
+
+// u(a) -= sum_j L21(a, j) z_own(j) for halo rows a of block ab; thread (al, g): row al, j = g mod 4.
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_halo_kernel(
+    const int4* __restrict__ items, int n, const int* __restrict__ f, const int* __restrict__ k,
+    const int* __restrict__ own, const int64_t* __restrict__ front_off, const int64_t* __restrict__ upd_off,
+    const T* __restrict__ pool, const T* __restrict__ z, T* upd) {
+    extern __shared__ unsigned char smem_raw[];
+    T* zs = reinterpret_cast<T*>(smem_raw);                                  // kN * NR
+    __shared__ T part[4][NR][NB];
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, ab = it.y;
+    const int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+        for (int m = threadIdx.x; m < kN; m += blockDim.x) zs[m + kN * q] = z[o + m + (int64_t)n * q];
+    __syncthreads();
+    const T* F = pool + front_off[nd];
+    const int al = threadIdx.x & 63, g = threadIdx.x >> 6;
+    const int a = ab * NB + al;
+    T s[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) s[q] = T(0);
+    if (a < hN) {
+        const T* col = F + kN + a;
+        int j = g;
+        for (; j + 12 < kN; j += 16) {
+            const T l0 = col[(int64_t)j * fN], l1 = col[(int64_t)(j + 4) * fN];
+            const T l2 = col[(int64_t)(j + 8) * fN], l3 = col[(int64_t)(j + 12) * fN];
 #pragma unroll
             for (int q = 0; q < NR; ++q)
-                for (int a = threadIdx.x; a < hc; a += blockDim.x) rhs[mp[a] + fN * q] += u[a + hc * q];
+                s[q] += l0 * zs[j + kN * q] + l1 * zs[j + 4 + kN * q] + l2 * zs[j + 8 + kN * q] +
+                        l3 * zs[j + 12 + kN * q];
         }
-        __syncthreads();
+        for (; j < kN; j += 4) {
+            const T l = col[(int64_t)j * fN];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) s[q] += l * zs[j + kN * q];
+        }
     }
-    int ntiles = (kN + NB - 1) / NB;
-    for (int t = 0; t < ntiles; ++t) {
-        int c0 = t * NB, kk = min(NB, kN - c0);
-        const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-        {
-            float v[NB * NB / SOLVE_THREADS];
 #pragma unroll
-            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) v[q] = Li[threadIdx.x + SOLVE_THREADS * q];
+    for (int q = 0; q < NR; ++q) part[g][q][al] = s[q];
+    __syncthreads();
+    if (g == 0 && a < hN) {
+        T* u = upd + upd_off[nd];
 #pragma unroll
-            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) {
-                int e = threadIdx.x + SOLVE_THREADS * q;
-                Ls[e / NB][e % NB] = v[q];
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x < NB * NR) {
-            int j = threadIdx.x % NB, q = threadIdx.x / NB;
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;   // Ls is zero above the diagonal
-            if (j < kk)
-                for (int m = 0; m < kk; m += 4) {
-                    a0 += Ls[j][m] * rhs[c0 + m + fN * q];
-                    if (m + 1 < kk) a1 += Ls[j][m + 1] * rhs[c0 + m + 1 + fN * q];
-                    if (m + 2 < kk) a2 += Ls[j][m + 2] * rhs[c0 + m + 2 + fN * q];
-                    if (m + 3 < kk) a3 += Ls[j][m + 3] * rhs[c0 + m + 3 + fN * q];
-                }
-            yt[q][j] = (a0 + a1) + (a2 + a3);
-        }
-        __syncthreads();
-        if (threadIdx.x < NB * NR) {
-            int j = threadIdx.x % NB, q = threadIdx.x / NB;
-            if (j < kk) rhs[c0 + j + fN * q] = yt[q][j];
-        }
-        // rows below the tile: rhs[r] -= L[r, c0:c0+kk] y_t
-        for (int r = c0 + kk + threadIdx.x; r < fN; r += blockDim.x) {
-            float acc[NR];
-#pragma unroll
-            for (int q = 0; q < NR; ++q) acc[q] = 0.f;
-            const float* col = F + (int64_t)c0 * fN + r;
-            int j = 0;
-            for (; j + 16 <= kk; j += 16) {
-                float l[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) l[u] = col[(int64_t)(j + u) * fN];
-#pragma unroll
-                for (int u = 0; u < 16; ++u)
-#pragma unroll
-                    for (int q = 0; q < NR; ++q) acc[q] += l[u] * yt[q][j + u];
-            }
-            for (; j < kk; ++j) {
-                float l = col[(int64_t)j * fN];
-#pragma unroll
-                for (int q = 0; q < NR; ++q) acc[q] += l * yt[q][j];
-            }
-#pragma unroll
-            for (int q = 0; q < NR; ++q) rhs[r + fN * q] -= acc[q];
-        }
-        __syncthreads();
-    }
-    float* u = upd + upd_off[nd];
-#pragma unroll
-    for (int q = 0; q < NR; ++q) {
-        for (int r = threadIdx.x; r < kN; r += blockDim.x) y[o + r + (int64_t)n * q] = rhs[r + fN * q];
-        for (int a = threadIdx.x; a < hN; a += blockDim.x) u[a + hN * q] = rhs[kN + a + fN * q];
+        for (int q = 0; q < NR; ++q)
+            u[a + hN * q] -= (part[0][q][al] + part[1][q][al]) + (part[2][q][al] + part[3][q][al]);
     }
 }
 
-// Backward substitution of one node: x_own = L11^-T (D^-1 y_own - L21^T x_halo), tile by tile
-// from the last; one warp per column of the tile, lanes stride over the rows below it.
-template <int NR>
-__global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_kernel(const int4* __restrict__ items, int n,
-                                                     const int* __restrict__ f, const int* __restrict__ k,
-                                                     const int* __restrict__ own,
-                                                     const int64_t* __restrict__ front_off,
-                                                     const int64_t* __restrict__ linv_off,
-                                                     const int64_t* __restrict__ halo_off, const int* __restrict__ halo,
-                                                     const float* __restrict__ pool, const float* __restrict__ linv,
-                                                     const float* __restrict__ Dvec, const float* __restrict__ y,
-                                                     float* x) {
-    extern __shared__ float xs[];   // fN * NR
-    __shared__ float Ls[NB][NB + 1];
-    __shared__ float zt[NR][NB];
-    int nd = items[blockIdx.x].x;
-    int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
-    const float* F = pool + front_off[nd];
+// w(j) = z(j) / D(j) - sum_a L21(a, j) x(halo a) for own columns j of block jb; warp per column.
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_z_kernel(
+    const int4* __restrict__ items, int n, const int* __restrict__ f, const int* __restrict__ k,
+    const int* __restrict__ own, const int64_t* __restrict__ front_off, const int64_t* __restrict__ halo_off,
+    const int* __restrict__ halo, const T* __restrict__ pool, const T* __restrict__ Dvec, const T* __restrict__ z,
+    const T* __restrict__ x, T* __restrict__ w) {
+    extern __shared__ unsigned char smem_raw[];
+    T* xs = reinterpret_cast<T*>(smem_raw);   // hN * NR
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, jb = it.y;
+    const int fN = f[nd], kN = k[nd], hN = fN - kN, o = own[nd];
     const int* hl = halo + halo_off[nd];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) {
-        for (int a = threadIdx.x; a < hN; a += blockDim.x) xs[kN + a + fN * q] = x[hl[a] + (int64_t)n * q];
-        for (int r = threadIdx.x; r < kN; r += blockDim.x) xs[r + fN * q] = y[o + r + (int64_t)n * q] / Dvec[o + r];
-    }
-    __syncthreads();
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-    int ntiles = (kN + NB - 1) / NB;
-    for (int t = ntiles - 1; t >= 0; --t) {
-        int c0 = t * NB, kk = min(NB, kN - c0), c1 = c0 + kk;
-        const float* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-        {
-            float v[NB * NB / SOLVE_THREADS];
-#pragma unroll
-            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) v[q] = Li[threadIdx.x + SOLVE_THREADS * q];
-#pragma unroll
-            for (int q = 0; q < NB * NB / SOLVE_THREADS; ++q) {
-                int e = threadIdx.x + SOLVE_THREADS * q;
-                Ls[e / NB][e % NB] = v[q];
-            }
-        }
-        for (int j = warp; j < kk; j += nwarp) {
-            const float* col = F + (int64_t)(c0 + j) * fN;
-            float s[NR];
-#pragma unroll
-            for (int q = 0; q < NR; ++q) s[q] = 0.f;
-            int r = c1 + lane;
-            for (; r + 96 < fN; r += 128) {
-                float l0 = col[r], l1 = col[r + 32], l2 = col[r + 64], l3 = col[r + 96];
-#pragma unroll
-                for (int q = 0; q < NR; ++q)
-                    s[q] += l0 * xs[r + fN * q] + l1 * xs[r + 32 + fN * q] + l2 * xs[r + 64 + fN * q] +
-                            l3 * xs[r + 96 + fN * q];
-            }
-            for (; r < fN; r += 32) {
-                float l = col[r];
-#pragma unroll
-                for (int q = 0; q < NR; ++q) s[q] += l * xs[r + fN * q];
-            }
-#pragma unroll
-            for (int q = 0; q < NR; ++q) {
-                float v = s[q];
-                for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-                if (lane == 0) zt[q][j] = xs[c0 + j + fN * q] - v;
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x < NB * NR) {
-            int j = threadIdx.x % NB, q = threadIdx.x / NB;
-            if (j < kk) {
-                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;   // Ls[m][j] = 0 for m < j
-                for (int m = 0; m < kk; m += 4) {
-                    a0 += Ls[m][j] * zt[q][m];
-                    if (m + 1 < kk) a1 += Ls[m + 1][j] * zt[q][m + 1];
-                    if (m + 2 < kk) a2 += Ls[m + 2][j] * zt[q][m + 2];
-                    if (m + 3 < kk) a3 += Ls[m + 3][j] * zt[q][m + 3];
-                }
-                xs[c0 + j + fN * q] = (a0 + a1) + (a2 + a3);
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
     for (int q = 0; q < NR; ++q)
-        for (int r = threadIdx.x; r < kN; r += blockDim.x) x[o + r + (int64_t)n * q] = xs[r + fN * q];
+        for (int a = threadIdx.x; a < hN; a += blockDim.x) xs[a + hN * q] = x[hl[a] + (int64_t)n * q];
+    __syncthreads();
+    const T* F = pool + front_off[nd];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int jj = 0; jj < 8; ++jj) {
+        const int j = jb * NB + warp * 8 + jj;
+        if (j >= kN) break;
+        const T* col = F + (int64_t)j * fN + kN;
+        T s[NR];
+#pragma unroll
+        for (int q = 0; q < NR; ++q) s[q] = T(0);
+        for (int a = lane; a < hN; a += 32) {
+            const T l = col[a];
+#pragma unroll
+            for (int q = 0; q < NR; ++q) s[q] += l * xs[a + hN * q];
+        }
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            T v = s[q];
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) w[o + j + (int64_t)n * q] = z[o + j + (int64_t)n * q] / Dvec[o + j] - v;
+        }
+    }
 }
 
-__global__ void mf_stability_kernel(int n, const float* __restrict__ D, double* out_min, unsigned long long* out_neg) {
+// x_own(j) = sum_{i >= j} X(i, j) w(i) for own columns j of block jb; thread (jl, g): column jl,
+// rows i = g mod 4 (row-major X: a row segment of 64 columns per load).
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_own_kernel(
+    const int4* __restrict__ items, int n, const int* __restrict__ k, const int* __restrict__ own,
+    const int64_t* __restrict__ xinv_off, const T* __restrict__ xinv, const T* __restrict__ w, T* __restrict__ x) {
+    extern __shared__ unsigned char smem_raw[];
+    T* ws = reinterpret_cast<T*>(smem_raw);   // kN * NR
+    __shared__ T part[4][NR][NB];
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x, jb = it.y;
+    const int kN = k[nd], o = own[nd];
+    const int j0 = jb * NB;
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+        for (int i = j0 + threadIdx.x; i < kN; i += blockDim.x) ws[i + kN * q] = w[o + i + (int64_t)n * q];
+    __syncthreads();
+    const T* X = xinv + xinv_off[nd];
+    const int jl = threadIdx.x & 63, g = threadIdx.x >> 6;
+    const int j = j0 + jl;
+    T s[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) s[q] = T(0);
+    if (j < kN)
+        for (int i = j0 + g; i < kN; i += 4) {
+            const T xv = (i >= j) ? X[(int64_t)i * kN + j] : T(0);
+#pragma unroll
+            for (int q = 0; q < NR; ++q) s[q] += xv * ws[i + kN * q];
+        }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) part[g][q][jl] = s[q];
+    __syncthreads();
+    if (g == 0 && j < kN)
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+            x[o + j + (int64_t)n * q] = (part[0][q][jl] + part[1][q][jl]) + (part[2][q][jl] + part[3][q][jl]);
+}
+
+template <class T>
+__global__ void mf_stability_kernel(int n, const T* __restrict__ D, double* out_min, unsigned long long* out_neg) {
     __shared__ double smin[256];
     __shared__ unsigned long long sneg[256];
     double mn = 1e300;
@@ -516,31 +662,36 @@ __global__ void mf_stability_kernel(int n, const float* __restrict__ D, double* 
     }
 }
 
+constexpr size_t gemm_smem(size_t elem) { return 2 * elem * NB * (NB + 1) + elem * NB; }
+
 }  // namespace
 
-Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, const std::vector<int>& cols,
-                           cudaStream_t stream)
+template <class T>
+MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr, const std::vector<int>& cols,
+                                cudaStream_t stream)
     : stream_(stream) {
-    n_ = T.nfree;
-    nnodes_ = (int)T.nodes.size();
-    flops_ = T.factor_flops();
+    n_ = Tr.nfree;
+    nnodes_ = (int)Tr.nodes.size();
+    flops_ = Tr.factor_flops();
     std::vector<int> f(nnodes_), k(nnodes_), own(nnodes_), parent(nnodes_), c0(nnodes_), c1(nnodes_);
     std::vector<int64_t> front_off(nnodes_), linv_off(nnodes_), ws_off(nnodes_), upd_off(nnodes_),
-        halo_off(nnodes_), map_off(nnodes_);
+        halo_off(nnodes_), map_off(nnodes_), xinv_off(nnodes_);
+    int64_t xo = 0;
     std::vector<int> halo_all, map_all;
     int64_t fo = 0, lo = 0, wo = 0, uo = 0;
     for (int i = 0; i < nnodes_; ++i) {
-        const NDNode& nd = T.nodes[i];
+        const NDNode& nd = Tr.nodes[i];
         f[i] = nd.f(); k[i] = nd.k; own[i] = nd.own_start; parent[i] = nd.parent;
         c0[i] = nd.child[0]; c1[i] = nd.child[1];
         front_off[i] = fo; fo += (int64_t)f[i] * f[i];
         linv_off[i] = lo; lo += (int64_t)((nd.k + NB - 1) / NB) * NB * NB;
+        xinv_off[i] = xo; xo += (int64_t)nd.k * nd.k;
         ws_off[i] = wo; wo += (int64_t)f[i] * NB;
         upd_off[i] = uo; uo += (int64_t)nd.h() * MF_MAX_RHS;
         halo_off[i] = (int64_t)halo_all.size();
         halo_all.insert(halo_all.end(), nd.halo.begin(), nd.halo.end());
         map_off[i] = (int64_t)map_all.size();
-        map_all.insert(map_all.end(), T.parent_map[i].begin(), T.parent_map[i].end());
+        map_all.insert(map_all.end(), Tr.parent_map[i].begin(), Tr.parent_map[i].end());
         max_f_ = std::max(max_f_, f[i]);
     }
     // CSR lower entries -> front positions
@@ -558,9 +709,9 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
                     for (int e = rowptr[R]; e < rowptr[R + 1]; ++e) {
                         int C = cols[e];
                         if (C > R) continue;
-                        int nd = T.node_of[C];
-                        int lc = C - T.nodes[nd].own_start;
-                        int lr = T.local_index(nd, R);
+                        int nd = Tr.node_of[C];
+                        int lc = C - Tr.nodes[nd].own_start;
+                        int lr = Tr.local_index(nd, R);
                         if (lr < 0) { bad[t] = 1; return; }
                         fpos[e] = front_off[nd] + (int64_t)lc * f[nd] + lr;
                     }
@@ -570,9 +721,9 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
             if (b) throw std::logic_error("multifrontal: matrix entry outside its front");
     }
     // levels and work lists
-    nlevels_ = T.max_height + 1;
+    nlevels_ = Tr.max_height + 1;
     level_nodes_.assign(nlevels_, {});
-    for (int i = 0; i < nnodes_; ++i) level_nodes_[T.nodes[i].height].push_back(i);
+    for (int i = 0; i < nnodes_; ++i) level_nodes_[Tr.nodes[i].height].push_back(i);
     std::vector<int4> items;
     struct Pending { int level, kind, slot, step; size_t begin, end; };
     std::vector<Pending> marks;
@@ -610,15 +761,50 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
                 if (k[nd] <= t * NB) continue;
                 int cc1 = t * NB + std::min(NB, k[nd] - t * NB);
                 int ntr = (f[nd] - cc1 + NB - 1) / NB;
-                for (int ti = 0; ti < ntr; ++ti)
-                    for (int tj = 0; tj <= ti; ++tj) items.push_back(make_int4(nd, ti, tj, 0));
+                for (int ti = 0; ti < ntr; ++ti) items.push_back(make_int4(nd, ti, 0, 0));
             }
             marks.push_back({L, 3, 0, t, b, items.size()});
+            b = items.size();
+            for (int nd : ln) {
+                if (k[nd] <= t * NB) continue;
+                int cc1 = t * NB + std::min(NB, k[nd] - t * NB);
+                int ntr = (f[nd] - cc1 + NB - 1) / NB;
+                for (int ti = 1; ti < ntr; ++ti)
+                    for (int tj = 1; tj <= ti; ++tj) items.push_back(make_int4(nd, ti, tj, 0));
+            }
+            marks.push_back({L, 5, 0, t, b, items.size()});
         }
         size_t b = items.size();
         for (int nd : ln) items.push_back(make_int4(nd, 0, 0, 0));
         marks.push_back({L, 4, 0, 0, b, items.size()});
-        for (int nd : ln) levels_[L].max_f = std::max(levels_[L].max_f, f[nd]);
+        b = items.size();
+        for (int nd : ln)
+            for (int rb = 0; rb * NB < k[nd]; ++rb) items.push_back(make_int4(nd, rb, 0, 0));
+        marks.push_back({L, 6, 0, 0, b, items.size()});
+        b = items.size();
+        for (int nd : ln)
+            for (int ab = 0; ab * NB < f[nd] - k[nd]; ++ab) items.push_back(make_int4(nd, ab, 0, 0));
+        marks.push_back({L, 7, 0, 0, b, items.size()});
+        int maxb = 0;
+        for (int nd : ln) maxb = std::max(maxb, (k[nd] + NB - 1) / NB);
+        levels_[L].xdiag.resize(maxb);
+        levels_[L].xoff.resize(maxb);
+        for (int bi = 0; bi < maxb; ++bi) {
+            b = items.size();
+            for (int nd : ln)
+                if (bi * NB < k[nd]) items.push_back(make_int4(nd, bi, 0, 0));
+            marks.push_back({L, 8, 0, bi, b, items.size()});
+            b = items.size();
+            for (int nd : ln)
+                if (bi * NB < k[nd])
+                    for (int bj = 0; bj < bi; ++bj) items.push_back(make_int4(nd, bi, bj, 0));
+            marks.push_back({L, 9, 0, bi, b, items.size()});
+        }
+        for (int nd : ln) {
+            levels_[L].max_f = std::max(levels_[L].max_f, f[nd]);
+            levels_[L].max_k = std::max(levels_[L].max_k, k[nd]);
+            levels_[L].max_h = std::max(levels_[L].max_h, f[nd] - k[nd]);
+        }
     }
     // algorithmic traffic and flops per factorisation
     for (int L = 0; L < nlevels_; ++L)
@@ -644,7 +830,12 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
             case 0: lv.ea[m.slot] = w; break;
             case 1: lv.steps[m.step].diag = w; break;
             case 2: lv.steps[m.step].panel = w; break;
-            case 3: lv.steps[m.step].update = w; break;
+            case 3: lv.steps[m.step].upd_next = w; break;
+            case 5: lv.steps[m.step].upd_rest = w; break;
+            case 6: lv.own_blocks = w; break;
+            case 7: lv.halo_blocks = w; break;
+            case 8: lv.xdiag[m.step] = w; break;
+            case 9: lv.xoff[m.step] = w; break;
             default: lv.nodes = w; break;
         }
     }
@@ -652,31 +843,55 @@ Multifrontal::Multifrontal(const NDTree& T, const std::vector<int>& rowptr, cons
         for (const Step& st : levels_[L].steps) {
             kernel_launches[0] += st.diag.count > 0;
             kernel_launches[1] += st.panel.count > 0;
-            kernel_launches[2] += st.update.count > 0;
+            kernel_launches[2] += (st.upd_next.count > 0) + (st.upd_rest.count > 0);
         }
     }
     d_f_.upload(f, stream_); d_k_.upload(k, stream_); d_own_.upload(own, stream_); d_parent_.upload(parent, stream_);
     d_child0_.upload(c0, stream_); d_child1_.upload(c1, stream_);
     d_front_off_.upload(front_off, stream_); d_linv_off_.upload(linv_off, stream_); d_ws_off_.upload(ws_off, stream_);
     d_upd_off_.upload(upd_off, stream_); d_halo_off_.upload(halo_off, stream_); d_map_off_.upload(map_off, stream_);
+    d_xinv_off_.upload(xinv_off, stream_);
+    xinv_.alloc(std::max<int64_t>(xo, 1));
     d_halo_.upload(halo_all, stream_); d_map_.upload(map_all, stream_);
     d_fpos_.upload(fpos, stream_);
     pool_.alloc(std::max<int64_t>(fo, 1));
     linv_.alloc(std::max<int64_t>(lo, 1));
-    ws_.alloc(std::max<int64_t>(wo, 1));
+    ws_half_ = wo;
+    ws_.alloc(std::max<int64_t>(2 * wo, 1));
+    KL_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+    KL_CUDA(cudaEventCreateWithFlags(&ev_panel_, cudaEventDisableTiming));
+    KL_CUDA(cudaEventCreateWithFlags(&ev_rest_, cudaEventDisableTiming));
     upd_.alloc(std::max<int64_t>(uo, 1));
     D_.alloc(std::max(n_, 1));
     y_.alloc((size_t)std::max(n_, 1) * MF_MAX_RHS);
+    z_.alloc((size_t)std::max(n_, 1) * MF_MAX_RHS);
+    KL_CUDA(cudaStreamCreateWithFlags(&inv_stream_, cudaStreamNonBlocking));
+    KL_CUDA(cudaEventCreateWithFlags(&ev_level_, cudaEventDisableTiming));
+    KL_CUDA(cudaEventCreateWithFlags(&ev_inv_, cudaEventDisableTiming));
     status_.alloc(1);
     status_.zero(stream_);
-    size_t smem = (size_t)max_f_ * MF_MAX_RHS * sizeof(float);
-    int smax = (int)std::max<size_t>(smem, 48 * 1024);
-    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    KL_CUDA(cudaFuncSetAttribute(mf_fwd_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
-    KL_CUDA(cudaFuncSetAttribute(mf_bwd_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+    int mk = 0, mh = 0;
+    for (const Level& lv : levels_) { mk = std::max(mk, lv.max_k); mh = std::max(mh, lv.max_h); }
+    const size_t smk = (size_t)mk * MF_MAX_RHS * sizeof(T), smh = (size_t)mh * MF_MAX_RHS * sizeof(T);
+    if (std::max(smk, smh) > (size_t)200 * 1024)
+        throw std::invalid_argument("multifrontal: separator too large for the shared-memory solve kernels");
+    const int ak = (int)std::max<size_t>(smk, 48 * 1024), ah = (int)std::max<size_t>(smh, 48 * 1024);
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_own_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_own_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_own_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_halo_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_halo_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_fwd_halo_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_z_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ah));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_z_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ah));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_z_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ah));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    const int gsm = (int)gemm_smem(sizeof(T));
+    KL_CUDA(cudaFuncSetAttribute(mf_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+    KL_CUDA(cudaFuncSetAttribute(mf_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+    KL_CUDA(cudaFuncSetAttribute(mf_xoff_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
     KL_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -692,8 +907,9 @@ bool graphs_enabled() {
 }  // namespace
 
 // Captures `launches` (a fixed launch sequence on stream_) into a graph once and replays it.
+template <class T>
 template <class Fn>
-void Multifrontal::replay(GraphSlot& slot, const void* key0, const void* key1, Fn&& launches) {
+void MultifrontalT<T>::replay(GraphSlot& slot, const void* key0, const void* key1, Fn&& launches) {
     if (g_timer.enabled || !graphs_enabled()) {
         launches();
         return;
@@ -724,28 +940,45 @@ void Multifrontal::replay(GraphSlot& slot, const void* key0, const void* key1, F
     count_launch(slot.kernels);
 }
 
-Multifrontal::~Multifrontal() {
+template <class T>
+MultifrontalT<T>::~MultifrontalT() {
     for (GraphSlot* s : {&fact_graph_, &solve_graph_[0], &solve_graph_[1], &solve_graph_[2]})
         if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (ev_panel_) cudaEventDestroy(ev_panel_);
+    if (ev_rest_) cudaEventDestroy(ev_rest_);
+    if (ev_level_) cudaEventDestroy(ev_level_);
+    if (ev_inv_) cudaEventDestroy(ev_inv_);
+    if (side_) cudaStreamDestroy(side_);
+    if (inv_stream_) cudaStreamDestroy(inv_stream_);
 }
 
-void Multifrontal::factorize_async(const float* d_vals) {
+template <class T>
+void MultifrontalT<T>::factorize_async(const T* d_vals) {
     if (!d_vals && nnz_ > 0) throw std::logic_error("multifrontal: no matrix values");
     replay(fact_graph_, d_vals, nullptr, [&] { factorize_launches(d_vals); });
 }
 
-void Multifrontal::factorize_launches(const float* d_vals) {
-    KL_CUDA(cudaMemsetAsync(pool_.get(), 0, pool_.size() * sizeof(float), stream_));
+template <class T>
+void MultifrontalT<T>::factorize_launches(const T* d_vals) {
+    KL_CUDA(cudaMemsetAsync(pool_.get(), 0, pool_.size() * sizeof(T), stream_));
     KL_CUDA(cudaMemsetAsync(status_.get(), 0, sizeof(int), stream_));
     if (nnz_ > 0) {
-        mf_scatter_kernel<<<ceil_div(nnz_, 256), 256, 0, stream_>>>(nnz_, d_fpos_.get(), d_vals, pool_.get());
+        mf_scatter_kernel<T><<<ceil_div(nnz_, 256), 256, 0, stream_>>>(nnz_, d_fpos_.get(), d_vals, pool_.get());
         count_launch();
     }
+    // Look-ahead: step t's update of the tiles beyond the next pivot block runs on side_,
+    // concurrently with step t+1's diagonal and panel; the next-block update waits for it.
+    bool rest_inflight = false;
+    auto join_rest = [&] {
+        if (rest_inflight) KL_CUDA(cudaStreamWaitEvent(stream_, ev_rest_, 0));
+        rest_inflight = false;
+    };
     for (int L = 0; L < nlevels_; ++L) {
         Level& lv = levels_[L];
+        join_rest();
         for (int s = 0; s < 2; ++s)
             if (lv.ea[s].count) {
-                mf_extend_add_kernel<<<lv.ea[s].count, 256, 0, stream_>>>(lv.ea[s].items, d_f_.get(), d_k_.get(),
+                mf_extend_add_kernel<T><<<lv.ea[s].count, 256, 0, stream_>>>(lv.ea[s].items, d_f_.get(), d_k_.get(),
                                                                           d_parent_.get(), d_front_off_.get(),
                                                                           d_map_off_.get(), d_map_.get(), pool_.get());
                 count_launch();
@@ -753,74 +986,126 @@ void Multifrontal::factorize_launches(const float* d_vals) {
         for (Step& st : lv.steps) {
             if (st.diag.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_diag_kernel<<<st.diag.count, 256, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
+                mf_diag_kernel<T, DIAG_THREADS, DCH><<<st.diag.count, DIAG_THREADS, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
                                                                    d_own_.get(), d_front_off_.get(),
                                                                    d_linv_off_.get(), pool_.get(), D_.get(),
                                                                    linv_.get(), status_.get());
                 g_timer.end(stream_, 5, evk);
                 count_launch();
             }
+            // block row st.t of the node inverses: needs this step's tile inverse and the panels
+            // of the earlier steps only, so it runs on inv_stream_ beside the remaining steps
+            if (st.t < (int)lv.xdiag.size() && lv.xdiag[st.t].count) {
+                KL_CUDA(cudaEventRecord(ev_level_, stream_));
+                KL_CUDA(cudaStreamWaitEvent(inv_stream_, ev_level_, 0));
+                mf_xdiag_kernel<T><<<lv.xdiag[st.t].count, 256, 0, inv_stream_>>>(
+                    lv.xdiag[st.t].items, d_k_.get(), d_linv_off_.get(), d_xinv_off_.get(), linv_.get(), xinv_.get());
+                count_launch();
+                if (lv.xoff[st.t].count) {
+                    mf_xoff_kernel<T><<<lv.xoff[st.t].count, 256, gemm_smem(sizeof(T)), inv_stream_>>>(
+                        lv.xoff[st.t].items, d_f_.get(), d_k_.get(), d_front_off_.get(), d_linv_off_.get(),
+                        d_xinv_off_.get(), pool_.get(), linv_.get(), xinv_.get());
+                    count_launch();
+                }
+            }
+            T* W = ws_.get() + (st.t & 1) * ws_half_;
             if (st.panel.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_panel_kernel<<<st.panel.count, 256, 0, stream_>>>(st.panel.items, st.t, d_f_.get(), d_k_.get(),
-                                                                     d_front_off_.get(), d_linv_off_.get(),
-                                                                     d_ws_off_.get(), pool_.get(), linv_.get(),
-                                                                     ws_.get());
+                mf_panel_kernel<T><<<st.panel.count, 256, gemm_smem(sizeof(T)), stream_>>>(
+                    st.panel.items, st.t, d_f_.get(), d_k_.get(), d_front_off_.get(), d_linv_off_.get(),
+                    d_ws_off_.get(), pool_.get(), linv_.get(), W);
                 g_timer.end(stream_, 6, evk);
                 count_launch();
             }
-            if (st.update.count) {
+            // the previous step's far update must finish before this step's updates start
+            join_rest();
+            if (st.upd_rest.count) {
+                KL_CUDA(cudaEventRecord(ev_panel_, stream_));
+                KL_CUDA(cudaStreamWaitEvent(side_, ev_panel_, 0));
+                cudaEvent_t evk = g_timer.begin(side_);
+                mf_update_kernel<T><<<st.upd_rest.count, 256, gemm_smem(sizeof(T)), side_>>>(
+                    st.upd_rest.items, st.t, d_f_.get(), d_k_.get(), d_front_off_.get(), d_ws_off_.get(), pool_.get(),
+                    W);
+                g_timer.end(side_, 4, evk);
+                count_launch();
+                KL_CUDA(cudaEventRecord(ev_rest_, side_));
+                rest_inflight = true;
+            }
+            if (st.upd_next.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_update_kernel<<<st.update.count, 256, 0, stream_>>>(st.update.items, st.t, d_f_.get(), d_k_.get(),
-                                                                       d_front_off_.get(), d_ws_off_.get(), pool_.get(),
-                                                                       ws_.get());
+                mf_update_kernel<T><<<st.upd_next.count, 256, gemm_smem(sizeof(T)), stream_>>>(
+                    st.upd_next.items, st.t, d_f_.get(), d_k_.get(), d_front_off_.get(), d_ws_off_.get(), pool_.get(),
+                    W);
                 g_timer.end(stream_, 4, evk);
                 count_launch();
             }
         }
     }
+    join_rest();
+    KL_CUDA(cudaEventRecord(ev_inv_, inv_stream_));
+    KL_CUDA(cudaStreamWaitEvent(stream_, ev_inv_, 0));
     KL_CHECK_LAUNCH();
 }
 
-int Multifrontal::read_status() {
+template <class T>
+int MultifrontalT<T>::read_status() {
     int st = 0;
     KL_CUDA(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
     KL_CUDA(cudaStreamSynchronize(stream_));
     return st ? ST_SOLVER_ERROR : ST_SUCCESS;
 }
 
-int Multifrontal::factorize(const float* d_vals, bool check_status) {
+template <class T>
+int MultifrontalT<T>::factorize(const T* d_vals, bool check_status) {
     factorize_async(d_vals);
     return check_status ? read_status() : ST_SUCCESS;
 }
 
+template <class T>
 template <int NR>
-void Multifrontal::solve_impl(const float* d_b, float* d_x) {
+void MultifrontalT<T>::solve_impl(const T* d_b, T* d_x) {
     for (int L = 0; L < nlevels_; ++L) {
         Level& lv = levels_[L];
-        size_t smem = (size_t)lv.max_f * NR * sizeof(float);
-        mf_fwd_kernel<NR><<<lv.nodes.count, SOLVE_THREADS, smem, stream_>>>(
+        const size_t smk = (size_t)lv.max_k * NR * sizeof(T);
+        mf_fwd_gather_kernel<T, NR><<<lv.nodes.count, SOLVE_THREADS, 0, stream_>>>(
             lv.nodes.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_child0_.get(), d_child1_.get(),
-            d_front_off_.get(), d_linv_off_.get(), d_upd_off_.get(), d_map_off_.get(), d_map_.get(), pool_.get(),
-            linv_.get(), upd_.get(), d_b, y_.get());
+            d_upd_off_.get(), d_map_off_.get(), d_map_.get(), d_b, y_.get(), upd_.get());
         count_launch();
+        if (lv.own_blocks.count) {
+            mf_fwd_own_kernel<T, NR><<<lv.own_blocks.count, SOLVE_THREADS, smk, stream_>>>(
+                lv.own_blocks.items, n_, d_k_.get(), d_own_.get(), d_xinv_off_.get(), xinv_.get(), y_.get(), z_.get());
+            count_launch();
+        }
+        if (lv.halo_blocks.count) {
+            mf_fwd_halo_kernel<T, NR><<<lv.halo_blocks.count, SOLVE_THREADS, smk, stream_>>>(
+                lv.halo_blocks.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_front_off_.get(), d_upd_off_.get(),
+                pool_.get(), z_.get(), upd_.get());
+            count_launch();
+        }
     }
     for (int L = nlevels_ - 1; L >= 0; --L) {
         Level& lv = levels_[L];
-        size_t smem = (size_t)lv.max_f * NR * sizeof(float);
-        mf_bwd_kernel<NR><<<lv.nodes.count, SOLVE_THREADS, smem, stream_>>>(
-            lv.nodes.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_front_off_.get(), d_linv_off_.get(),
-            d_halo_off_.get(), d_halo_.get(), pool_.get(), linv_.get(), D_.get(), y_.get(), d_x);
+        if (!lv.own_blocks.count) continue;
+        const size_t smk = (size_t)lv.max_k * NR * sizeof(T), smh = (size_t)lv.max_h * NR * sizeof(T);
+        mf_bwd_z_kernel<T, NR><<<lv.own_blocks.count, SOLVE_THREADS, smh, stream_>>>(
+            lv.own_blocks.items, n_, d_f_.get(), d_k_.get(), d_own_.get(), d_front_off_.get(), d_halo_off_.get(),
+            d_halo_.get(), pool_.get(), D_.get(), z_.get(), d_x, y_.get());
+        count_launch();
+        mf_bwd_own_kernel<T, NR><<<lv.own_blocks.count, SOLVE_THREADS, smk, stream_>>>(
+            lv.own_blocks.items, n_, d_k_.get(), d_own_.get(), d_xinv_off_.get(), xinv_.get(), y_.get(), d_x);
         count_launch();
     }
     KL_CHECK_LAUNCH();
 }
 
-void Multifrontal::enqueue_factorize(const float* d_vals) { factorize_launches(d_vals); }
+template <class T>
+void MultifrontalT<T>::enqueue_factorize(const T* d_vals) { factorize_launches(d_vals); }
 
-void Multifrontal::enqueue_solve(const float* d_b, float* d_x) { solve_impl<1>(d_b, d_x); }
+template <class T>
+void MultifrontalT<T>::enqueue_solve(const T* d_b, T* d_x) { solve_impl<1>(d_b, d_x); }
 
-void Multifrontal::solve(const float* d_b, float* d_x, int nrhs) {
+template <class T>
+void MultifrontalT<T>::solve(const T* d_b, T* d_x, int nrhs) {
     switch (nrhs) {
         case 1: replay(solve_graph_[0], d_b, d_x, [&] { solve_impl<1>(d_b, d_x); }); break;
         case 2: replay(solve_graph_[1], d_b, d_x, [&] { solve_impl<2>(d_b, d_x); }); break;
@@ -836,11 +1121,12 @@ void Multifrontal::solve(const float* d_b, float* d_x, int nrhs) {
     }
 }
 
-void Multifrontal::stability(double* min_d, int64_t* negatives) {
+template <class T>
+void MultifrontalT<T>::stability(double* min_d, int64_t* negatives) {
     const int blocks = 64;
     DevBuf<double> mn(blocks);
     DevBuf<unsigned long long> ng(blocks);
-    mf_stability_kernel<<<blocks, 256, 0, stream_>>>(n_, D_.get(), mn.get(), ng.get());
+    mf_stability_kernel<T><<<blocks, 256, 0, stream_>>>(n_, D_.get(), mn.get(), ng.get());
     count_launch();
     KL_CHECK_LAUNCH();
     std::vector<double> hm(blocks);
@@ -854,5 +1140,8 @@ void Multifrontal::stability(double* min_d, int64_t* negatives) {
     *min_d = m;
     *negatives = (int64_t)s;
 }
+
+template class MultifrontalT<float>;
+template class MultifrontalT<double>;
 
 }  // namespace klsa

@@ -337,12 +337,18 @@ Problem::Problem(const klsa_patch_desc& d) {
 
 Problem::~Problem() {
     mf.reset();
+    mf64.reset();
     if (stream) cudaStreamDestroy(stream);
 }
 
 Multifrontal& Problem::solver() {
     if (!mf) mf.reset(new Multifrontal(tree, rowptr, cols, stream));
     return *mf;
+}
+
+Multifrontal64& Problem::solver64() {
+    if (!mf64) mf64.reset(new Multifrontal64(tree, rowptr, cols, stream));
+    return *mf64;
 }
 
 double Problem::flops_tangent() const {

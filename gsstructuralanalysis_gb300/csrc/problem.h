@@ -54,6 +54,7 @@ struct Problem {
     DevBuf<double> d_tmp_int;
 
     std::unique_ptr<Multifrontal> mf;
+    std::unique_ptr<Multifrontal64> mf64;
 
     explicit Problem(const klsa_patch_desc& d);
     ~Problem();
@@ -65,7 +66,8 @@ struct Problem {
     void internal_force(double* d_out);                 // Fint(u), internal order, FP64
     void internal_force_elements(double* elemR);        // element forces of u into elemR (nel*d), no allocation
     void mass_f64();                                    // d_vals64 = M
-    Multifrontal& solver();                             // lazily built
+    Multifrontal& solver();                             // lazily built (FP32 fronts)
+    Multifrontal64& solver64();                         // lazily built (FP64 fronts)
 
     // public <-> internal permutations of nv vectors (device)
     void pub_to_int(const double* d_pub, double* d_int, int nv = 1);

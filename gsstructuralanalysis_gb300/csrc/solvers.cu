@@ -21,7 +21,8 @@ inline double sgn(double x) { return (double)((x > 0) - (x < 0)); }
 std::unique_ptr<LinearSolver> solver_from_options(Problem& P, const Options& opt, const std::string& def) {
     std::string name = opt.str("Solver", def);
     auto s = make_linear_solver(P, name, (int)opt.integer("Refinement", 0), opt.real("RefineTol", 1e-12),
-                                (int)opt.integer("CGMaxIterations", 0), opt.real("CGTolerance", 1e-10));
+                                (int)opt.integer("CGMaxIterations", 0), opt.real("CGTolerance", 1e-10),
+                                (int)opt.integer("FrontPrecision", 32));
     if (!s) throw std::invalid_argument("unknown Solver '" + name + "'");
     return s;
 }
@@ -650,8 +651,11 @@ void ALMGPU::step_impl() {
     else predictor();
     compute_residual();
     compute_residual_norms();
-    if (quasi_ && !ut_valid_) {
-        // quasiNewtonPredictor: keep the predictor's tangent
+    if (quasi_) {
+        // quasiNewtonPredictor (gsALMCrisfield.hpp:56-63, gsALMRiks.hpp:38-45,
+        // gsALMLoadControl.hpp:23-29): the Jacobian at the predicted point U + DU, kept for the
+        // iterations; u_t and u_bar follow from it in iteration()
+        compute_jacobian();
     }
     stabilityPrev_ = stability_;
     for (num_it_ = 1; num_it_ < maxIt_; ++num_it_) {

@@ -213,7 +213,9 @@ int64_t klsa_batch_instance_ndof(klsa_batch* b, int i);
  * (kind 0 tangent / 1 internal force, degree, blocks per SM, ms) per trial, up to cap rows;
  * returns the number of rows. */
 int klsa_batch_autotune(klsa_batch* b, double* log, int cap);
-/* Options as gsStaticNewton ("tol", "tolF", "tolU", "maxIt", "Relaxation") plus "LoadFactor". */
+/* Options as gsStaticNewton ("tol", "tolF", "tolU", "maxIt", "Relaxation") plus "LoadFactor" and
+ * "Refinement" (sweeps of iterative refinement of each Newton step against the assembled
+ * tangent, default 1). */
 int klsa_batch_newton_create(klsa_batch* b, const klsa_options* opt, klsa_batch_newton** out);
 int klsa_batch_newton_destroy(klsa_batch_newton* s);
 /* solve() of every instance -> Success when all converged, else NotConverged; per-instance

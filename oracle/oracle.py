@@ -434,6 +434,14 @@ class _ALMBase:
     def compute_ubar(self):
         self.deltaUbar = self.solve_system(-self.resVec)
 
+    def quasi_newton_predictor(self):
+        """quasiNewtonPredictor (gsALMCrisfield.hpp:56-63, gsALMRiks.hpp:38-45): the Jacobian at the
+        predicted point, kept for the iterations; LoadControl needs no u_t (gsALMLoadControl.hpp:23-29)."""
+        self.compute_jacobian()
+        if not isinstance(self, ALMLoadControl):
+            self.compute_ut()
+        self.compute_ubar()
+
     def compute_ut(self):
         self.deltaUt = self.solve_system(self.F)
 
@@ -448,10 +456,15 @@ class _ALMBase:
             self.predictor()
         self.compute_residual()
         self.compute_residual_norms()
+        quasi = bool(self.opts["Quasi"])
+        interval = int(self.opts["QuasiIterations"])
+        if quasi:
+            self.quasi_newton_predictor()
         self.stabilityPrev = self.stability
         for it in range(1, self.maxIt):
             self.num_iterations = it
-            self.quasi_newton_iteration()
+            if (not quasi) or (interval > 0 and it % interval == 0):
+                self.quasi_newton_iteration()
             self.iteration()
             if int(self.opts["BifurcationMethod"]) in (0, 1):
                 self.compute_stability(jacobian=False)

@@ -121,3 +121,49 @@ def test_static_newton_load_ramp_through_snap(lib, oracle_mod):
         U = st.solution()
         assert np.linalg.norm(U - ref.U) / np.linalg.norm(ref.U) < 1e-6, k
         assert np.linalg.norm(L * F - oa.fint(U)) <= 1e-7 * np.linalg.norm(L * F), k
+
+
+def test_fp64_fronts(lib, oracle_mod):
+    """FrontPrecision 64: the multifrontal LDL^T in FP64 (no refinement) solves the linear plate to
+    FP64 accuracy, and the Newton corrector with it is the exact Newton of the oracle (same
+    iteration count, same converged point)."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.flat_plate(m=8, p=2)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    st = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "FrontPrecision": 64})
+    assert st.solveLinear() == 0
+    ur = spla.spsolve(oa.linear().tocsc(), oa.force())
+    assert np.linalg.norm(st.solution() - ur) / np.linalg.norm(ur) < 1e-12
+    prob = P.cylindrical_panel(m=6, p=3, load=800.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    st = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "FrontPrecision": 64, "tol": 1e-10, "maxIt": 30})
+    assert st.solve() == 0
+    ref = oracle_mod.StaticNewton(oa.linear(), oa.force(), oa.jacobian, oa.residual, dict(tol=1e-10, maxIt=30))
+    assert ref.solve() == 0
+    assert np.linalg.norm(st.solution() - ref.U) / np.linalg.norm(ref.U) < 1e-9
+    assert st.iterations() == ref.num_iterations
+
+
+@pytest.mark.parametrize("method", ["Crisfield", "Riks", "LoadControl"])
+def test_quasi_newton_adaptive_length(lib, oracle_mod, method):
+    """Quasi-Newton corrector (Jacobian refreshed every QuasiIterations) with adaptive arc length
+    (gsALMBase.hpp:106-117, 376-387) against the oracle step by step."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=8, p=2, load=1e5 if method == "Riks" else 1.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    length = {"Crisfield": 0.004, "Riks": 0.003, "LoadControl": 100.0}[method]
+    opts = dict(Length=length, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=60, Quasi=1, QuasiIterations=2,
+                AdaptiveLength=1, AdaptiveIterations=4, BifurcationMethod=-1)
+    cls = {"Crisfield": G.ALMCrisfield, "Riks": G.ALMRiks, "LoadControl": G.ALMLoadControl}[method]
+    rcls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks,
+            "LoadControl": oracle_mod.ALMLoadControl}[method]
+    alm = cls(gp, opts)
+    alm.initialize()
+    ref = rcls(oa.jacobian, oa.al_residual, oa.force(), opts)
+    for k in range(5):
+        assert alm.step() == 0
+        assert ref.step() == 0
+        assert abs(alm.getLength() - ref.arcLength) <= 1e-12 * ref.arcLength, k
+        U, L = alm.solutionU(), alm.solutionL()
+        assert np.linalg.norm(U - ref.U) / np.linalg.norm(ref.U) < 1e-6, k
+        assert abs(L - ref.L) / abs(ref.L) < 1e-6, k
