@@ -354,8 +354,15 @@ def roofline(prof, stats, args):
                      "gbs": byts / t / 1e9, "tflops": fl / t / 1e12, "bytes_per_launch": byts}
     dom = max(detail, key=lambda k: detail[k]["ms_total_per_step"])
     ach = detail[dom]["gbs"]
+    # DRAM traffic per launch from one ncu capture (profiles/arclength_50k_launches_and_mf_diag_kernel.md):
+    # top-level single-front tiles of mf_diag_kernel read 23-25 KB and write 0 B of DRAM (results stay in
+    # L2) against 48 KB algorithmic; the live average above spans multi-front launches, so the captured
+    # launches are reported beside it rather than as this average's traffic.
+    capture = {"kernel": "mf_diag_kernel", "launches": "top-level single-front tiles (timed launches 35-37)",
+               "dram_bytes_per_launch": 25344, "algorithmic_bytes_per_launch": 49152,
+               "source": "profiles/arclength_50k_launches_and_mf_diag_kernel.md"}
     return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-            "traffic": None, "peak_source": src,
+            "traffic": None, "traffic_capture": capture, "peak_source": src,
             "note": "multifrontal kernels are bound by the latency of the pivot-tile chain, not by HBM or FLOP rate; "
                     "per-kernel bandwidth and FLOP rates in detail",
             "factorization_ms": raw["factorization"][0] / fac_n,
@@ -756,6 +763,10 @@ def run_eigen(args):
     Bm = gp.jacobian(uL, 1) - KL
     rb = [float(np.linalg.norm(KL @ v - lam * (Bm @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(bv, bvec)]
     rm = [float(np.linalg.norm(KL @ v - lam * (M @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(mv, mvec)]
+    # Rayleigh quotients of the returned vectors in FP64: second-order accurate in the vector error,
+    # so their agreement with the returned eigenvalues bounds the eigenvalue error
+    qb = [float(abs((v @ (KL @ v)) / (v @ (Bm @ v)) - lam) / abs(lam)) for lam, v in zip(bv, bvec)]
+    qm = [float(abs((v @ (KL @ v)) / (v @ (M @ v)) - lam) / abs(lam)) for lam, v in zip(mv, mvec)]
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = eigen_cpu_baseline()
@@ -769,6 +780,7 @@ def run_eigen(args):
                    "ndof_free": gp.ndof, "nnz": gp.nnz, "status": [int(st1), int(st2)],
                    "buckling_values": bv.tolist(), "modal_values": mv.tolist(),
                    "max_rel_residual_buckling": max(rb), "max_rel_residual_modal": max(rm),
+                   "max_rayleigh_rel_diff_buckling": max(qb), "max_rayleigh_rel_diff_modal": max(qm),
                    "l2": "inputs larger than L2 (fronts %.1f GB)" % (gp.stats()["front_bytes"] / 1e9)},
         "e2e": {"value": value, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 8 * gp.ndof * 2 * EIG_NEV},

@@ -63,52 +63,53 @@ __global__ void __launch_bounds__(256) mf_extend_add_kernel(const int4* __restri
     for (; b < hc; b += 32) dcol[mp[b]] += scol[b];
 }
 
-// Diagonal tile (kk <= 64 pivots), DIAG_THREADS threads.  Thread t owns a chunk of one column c
-// of the tile -- rows [r0, r0 + CH) with r0 >= c -- both of the tile A (becoming L and D) and of
-// X = L^-1 (unit lower); rows and columns beyond kk are padded with the identity.  Step j (one
-// barrier): the owners of column j publish A(:, j) and the owner of the pivot 1/d_j; the owners
-// of row j of X publish X(j, :).  Then columns c > j take the rank-1 update
-// A(r, c) -= A(r, j) A(c, j) / d_j, column j is scaled to L(:, j), and columns c <= j of X take
-// X(r, c) -= L(r, j) X(j, c) for r > j.  The chains of LDL^T and of the inverse advance in the
-// same 64 steps.  The update is branch-free (selects) with the chunk's column values loaded into
-// registers before use, and chunks are short so that 16 warps share the per-step latency.
+// Diagonal tile (kk <= 64 pivots), 288 threads.  Thread t owns one row r of the tile and the 8
+// columns [8q, 8q + 8) of it that lie on or below the diagonal (q = 0..7, rows r >= 8q: 64 + 56 +
+// ... + 8 = 288 owners), both of A (becoming L and D) and of X = L^-1 (unit lower); rows and
+// columns beyond kk are padded with the identity.  Step j (one barrier): the owners of column j
+// publish A(:, j), the owner of the pivot its reciprocal, the owners of row j of X publish
+// X(j, :).  Then every thread updates its 8 entries:
+//   A(r, c) -= L(r, j) A(c, j) for c > j,   A(r, j) = L(r, j) = A(r, j) / d_j,
+//   X(r, c) -= L(r, j) X(j, c) for c <= j < r.
+// A thread reads one value of column j for its row and two 16-byte words of the column / row
+// buffers that its whole column group shares, so the shared-memory traffic per step stays small.
 // Writes L (strict lower) and D into the front, D into Dvec and X into the tile's slot of linv
 // (row-major), which the panel GEMM and the triangular solves use.
-constexpr int DIAG_THREADS = 512;
-constexpr int DCH = 5;   // rows per chunk: sum_c ceil((64 - c) / 5) = 442 chunks <= 512 threads
+constexpr int DIAG_THREADS = 288;
 
-template <int CH>
-__device__ __forceinline__ void diag_chunk(int tid, int& c, int& r0) {
-    c = -1;
-    r0 = NB;
-    int t = tid;
-    for (int cc = 0; cc < NB; ++cc) {
-        const int nch = (NB - cc + CH - 1) / CH;
-        if (t < nch) {
-            c = cc;
-            r0 = cc + t * CH;
-            return;
-        }
-        t -= nch;
-    }
+// 1/d from the fast intrinsic quotient refined by Newton's iteration r <- r (2 - d r), with the
+// exact quotient outside the range where the intrinsic is accurate.
+__device__ __forceinline__ float pivot_recip(float d) {
+    const float ad = fabsf(d);
+    if (!(ad > 1e-30f && ad < 1e30f)) return 1.0f / d;
+    const float r = __fdividef(1.0f, d);
+    return r * (2.0f - d * r);
+}
+__device__ __forceinline__ double pivot_recip(double d) {
+    const double ad = fabs(d);
+    if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+    double r = (double)__fdividef(1.0f, (float)d);
+    r = r * (2.0 - d * r);
+    return r * (2.0 - d * r);
 }
 
-template <class T, int CH>
-__device__ __forceinline__ T sel_row(const T (&v)[CH], int k) {
+template <class T>
+__device__ __forceinline__ T sel8(const T (&v)[8], int k) {
     T r = v[0];
 #pragma unroll
-    for (int q = 1; q < CH; ++q) r = (k == q) ? v[q] : r;
+    for (int q = 1; q < 8; ++q) r = (k == q) ? v[q] : r;
     return r;
 }
 
-template <class T, int NT, int CH>
-__global__ void __launch_bounds__(NT) mf_diag_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
-                                                     const int* __restrict__ k, const int* __restrict__ own,
-                                                     const int64_t* __restrict__ front_off,
-                                                     const int64_t* __restrict__ linv_off, T* pool, T* Dvec, T* linv,
-                                                     int* status) {
-    __shared__ T col[2][NB];
-    __shared__ T xrow[2][NB];
+template <class T>
+__global__ void __launch_bounds__(DIAG_THREADS) mf_diag_kernel(const int4* __restrict__ items, int t,
+                                                               const int* __restrict__ f, const int* __restrict__ k,
+                                                               const int* __restrict__ own,
+                                                               const int64_t* __restrict__ front_off,
+                                                               const int64_t* __restrict__ linv_off, T* pool, T* Dvec,
+                                                               T* linv, int* status) {
+    __shared__ __align__(16) T col[2][NB];
+    __shared__ __align__(16) T xrow[2][NB];
     __shared__ T sinv[2];
     __shared__ int bad;
     const int nd = items[blockIdx.x].x;
@@ -117,66 +118,71 @@ __global__ void __launch_bounds__(NT) mf_diag_kernel(const int4* __restrict__ it
     const int kk = min(NB, kN - c0);
     T* F = pool + front_off[nd];
     const int tid = threadIdx.x;
-    int c, r0;
-    diag_chunk<CH>(tid, c, r0);
-    T a[CH], x[CH];
-    int rc[CH];   // rows of the chunk clamped into the tile (slots beyond row 63 are never written back)
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-        const int r = r0 + i;
-        const bool in = c >= 0 && r < NB;
-        a[i] = !in ? T(0) : (r < kk ? F[(int64_t)(c0 + c) * fN + c0 + r] : (r == c ? T(1) : T(0)));
-        x[i] = (in && r == c) ? T(1) : T(0);
-        rc[i] = min(r, NB - 1);
+    // owner map: column group q and row r (rows 8q..63 of group q)
+    int q = 0, base = 0;
+    while (q < 7 && tid >= base + (NB - 8 * q)) {
+        base += NB - 8 * q;
+        ++q;
     }
-    const int cc = c < 0 ? 0 : c;
+    const int r = 8 * q + (tid - base);
+    const int cb = 8 * q;
+    T a[8], x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int c = cb + e;
+        a[e] = (c > r) ? T(0) : (r < kk ? F[(int64_t)(c0 + c) * fN + c0 + r] : (r == c ? T(1) : T(0)));
+        x[e] = (r == c) ? T(1) : T(0);
+    }
     if (tid == 0) bad = 0;
     __syncthreads();
     for (int j = 0; j < NB; ++j) {
         const int b = j & 1;
-        if (c == j) {
-#pragma unroll
-            for (int i = 0; i < CH; ++i)
-                if (r0 + i < NB) col[b][r0 + i] = a[i];
-            if (r0 == j) {
-                T d = a[0];
+        if ((j >> 3) == q && r >= j) {
+            const T v = sel8(a, j & 7);
+            col[b][r] = v;
+            if (r == j) {
+                T d = v;
                 if (!(fabs(d) > T(0)) || !isfinite(d)) {
                     if (j < kk) bad = 1;
                     d = T(1);
                 }
-                sinv[b] = T(1) / d;
+                sinv[b] = pivot_recip(d);
             }
         }
-        if (c >= 0 && c <= j && j >= r0 && j < r0 + CH) xrow[b][c] = sel_row<T, CH>(x, j - r0);
+        if (r == j) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) xrow[b][cb + e] = x[e];
+        }
         __syncthreads();
         const T inv = sinv[b];
-        const T cv = col[b][cc], xr = xrow[b][cc];
-        T v[CH];
+        const T l = col[b][r] * inv;   // L(r, j) for r > j
+        T cv[8], xv[8];
 #pragma unroll
-        for (int i = 0; i < CH; ++i) v[i] = col[b][rc[i]];
-        const bool upd_a = c > j, scale_a = c == j, upd_x = c >= 0 && c <= j;
-        const T fa = upd_a ? cv * inv : T(0);
-        const T xv = upd_x ? xr * inv : T(0);
+        for (int e = 0; e < 8; ++e) {
+            cv[e] = col[b][cb + e];
+            xv[e] = xrow[b][cb + e];
+        }
+        const bool below = r > j;
 #pragma unroll
-        for (int i = 0; i < CH; ++i) {
-            const bool below = r0 + i > j;
-            const T an = fma(-v[i], fa, a[i]);
-            a[i] = upd_a ? an : ((scale_a && below) ? a[i] * inv : a[i]);
-            const T xn = fma(-v[i], xv, x[i]);
-            x[i] = (upd_x && below) ? xn : x[i];
+        for (int e = 0; e < 8; ++e) {
+            const int c = cb + e;
+            const T an = fma(-l, cv[e], a[e]);
+            a[e] = (c > j && c <= r) ? an : ((c == j && below) ? a[e] * inv : a[e]);
+            const T xn = fma(-l, xv[e], x[e]);
+            x[e] = (c <= j && below) ? xn : x[e];
         }
     }
     T* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
 #pragma unroll
-    for (int i = 0; i < CH; ++i) {
-        const int r = r0 + i;
-        if (c >= 0 && r < NB) {
-            if (r < kk) F[(int64_t)(c0 + c) * fN + c0 + r] = a[i];
-            Li[r * NB + c] = r < kk ? x[i] : T(0);
+    for (int e = 0; e < 8; ++e) {
+        const int c = cb + e;
+        if (c <= r) {
+            if (r < kk) F[(int64_t)(c0 + c) * fN + c0 + r] = a[e];
+            Li[r * NB + c] = r < kk ? x[e] : T(0);
         }
     }
-    if (c >= 0 && r0 == c && c < kk) Dvec[own[nd] + c0 + c] = a[0];
-    for (int e = tid; e < NB * NB; e += NT)
+    if (r >= cb && r < cb + 8 && r < kk) Dvec[own[nd] + c0 + r] = sel8(a, r - cb);
+    for (int e = tid; e < NB * NB; e += DIAG_THREADS)
         if (e % NB > e / NB) Li[e] = T(0);
     __syncthreads();
     if (tid == 0 && bad) atomicExch(status, 1);
@@ -986,7 +992,7 @@ void MultifrontalT<T>::factorize_launches(const T* d_vals) {
         for (Step& st : lv.steps) {
             if (st.diag.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_diag_kernel<T, DIAG_THREADS, DCH><<<st.diag.count, DIAG_THREADS, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
+                mf_diag_kernel<T><<<st.diag.count, DIAG_THREADS, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
                                                                    d_own_.get(), d_front_off_.get(),
                                                                    d_linv_off_.get(), pool_.get(), D_.get(),
                                                                    linv_.get(), status_.get());
