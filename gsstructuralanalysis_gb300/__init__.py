@@ -71,6 +71,10 @@ SIGNATURES = {
     "klsa_alm_initialize": (_c_int, [_c_vp, _c_int]),
     "klsa_alm_compute_stability": (_c_int, [_c_vp, _c_int, _c_dbl]),
     "klsa_alm_stability": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_alm_is_bifurcation": (_c_int, [_c_vp, _c_int]),
+    "klsa_alm_compute_singular_point": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_int, _c_int, _c_int]),
+    "klsa_alm_switch_branch": (_c_int, [_c_vp]),
+    "klsa_alm_solution_v": (_c_int, [_c_vp, _c_vp]),
     "klsa_alm_step": (_c_int, [_c_vp]),
     "klsa_alm_set_length": (_c_int, [_c_vp, _c_dbl]),
     "klsa_alm_reduce_length": (_c_int, [_c_vp, _c_dbl]),
@@ -412,6 +416,22 @@ class _ALM:
         v = ctypes.c_int64()
         _check(_lib.klsa_alm_stability(self.h, None, None, None, ctypes.byref(v)))
         return v.value
+
+    def isBifurcation(self, jacobian=False):
+        return bool(_check(_lib.klsa_alm_is_bifurcation(self.h, 1 if jacobian else 0)))
+
+    def computeSingularPoint(self, U, L, switchBranch=False, jacobian=False, testPoint=True):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        return _check(_lib.klsa_alm_compute_singular_point(self.h, _ptr(U), float(L), int(bool(switchBranch)),
+                                                           int(bool(jacobian)), int(bool(testPoint))))
+
+    def switchBranch(self):
+        _check(_lib.klsa_alm_switch_branch(self.h))
+
+    def solutionV(self):
+        V = np.zeros(self.problem.ndof)
+        _check(_lib.klsa_alm_solution_v(self.h, _ptr(V)))
+        return V
 
     def step(self):
         return _check(_lib.klsa_alm_step(self.h))

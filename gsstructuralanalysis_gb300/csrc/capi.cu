@@ -428,6 +428,38 @@ int klsa_alm_solution(klsa_alm* a, double* U, double* L) {
         return KLSA_SUCCESS;
     });
 }
+int klsa_alm_is_bifurcation(klsa_alm* a, int jacobian) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return a->A->is_bifurcation(jacobian != 0) ? 1 : 0; });
+}
+int klsa_alm_compute_singular_point(klsa_alm* a, const double* U, double L, int switch_branch, int jacobian,
+                                    int test_point) {
+    if (!a || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->v, P.nfree);
+        P.upload_pub(U, a->v.get());
+        return a->A->compute_singular_point(a->v.get(), L, switch_branch != 0, jacobian != 0, test_point != 0);
+    });
+}
+int klsa_alm_switch_branch(klsa_alm* a) {
+    if (!a) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        a->A->switch_branch();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_solution_v(klsa_alm* a, double* V) {
+    if (!a || !V) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!a->A->V()) {
+            g_err = "no singular-point vector computed";
+            return KLSA_INVALID_ARGUMENT;
+        }
+        a->prob->P->download_pub(a->A->V(), V);
+        return KLSA_SUCCESS;
+    });
+}
 int klsa_alm_info(klsa_alm* a, double* out) {
     if (!a || !out) return KLSA_INVALID_ARGUMENT;
     out[0] = a->A->iterations();

@@ -179,6 +179,14 @@ void ALMGPU::apply_options() {
     // gsALMBase.hpp:39, 72-78: Eigenvalue by default; Determinant needs the LDL^T solver
     bifurcation_ = (int)opt_.integer("BifurcationMethod", 1);
     if (bifurcation_ == 0 && !S_->has_ldlt()) bifurcation_ = 1;
+    // singular-point options (gsALMBase.hpp:26-45, 60-90)
+    tolerance_ = opt_.real("Tol", 1e-6);
+    tau_ = opt_.real("Perturbation", 1e3);
+    spFail_ = (int)opt_.integer("SingularPointFailure", 1);
+    spTestTol_ = opt_.real("SingularPointTestTol", 1e-6);
+    spTestIt_ = (int)opt_.integer("SingularPointTestIt", 5);
+    spTolE_ = opt_.real("SingularPointComputeTolE", 1e-10);
+    spTolB_ = opt_.real("SingularPointComputeTolB", 0.0);
 }
 
 void ALMGPU::set_length(double l) {
@@ -260,8 +268,7 @@ void ALMGPU::compute_jacobian() {
     P_.set_displacement(x_.get());
     ++n_jac;
     if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
-    if (bifurcation_ == 1)
-        KL_CUDA(cudaMemcpyAsync(xjac_.get(), x_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+    KL_CUDA(cudaMemcpyAsync(xjac_.get(), x_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
     ut_valid_ = false;
     fact_stale_ = false;
 }
@@ -688,6 +695,221 @@ int ALMGPU::step() {
     } catch (const Fail& f) {
         return f.code;
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// singular points (gsALMBase.hpp:421-512, 628-852).  The extended system differentiates the
+// Jacobian by a forward difference with eps = 1e-8, which cancels to noise unless u_t solves
+// K u_t = F to FP64 working accuracy: these solves use FP64 fronts.
+// ------------------------------------------------------------------------------------------
+void ALMGPU::factor64_at(const double* d_x) {
+    if (!S64_) {
+        S64_.reset(new MFSolver(P_, 0, 0.0, true));
+        for (DevBuf<double>* b : {&V_, &DV_, &dV_, &ut64_, &ub64_, &h1_, &h2_, &Vt_, &Vb_, &W_}) {
+            b->alloc(n_);
+            b->zero(P_.stream);
+        }
+        Kv_.alloc(P_.nnz);
+    }
+    P_.set_displacement(d_x);
+    ++n_jac;
+    if (S64_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+}
+
+namespace {
+double dnorm(const double* x, int n, cudaStream_t s) {
+    double d;
+    const double* a[1] = {x};
+    vec::multidot(1, a, a, n, &d, s);
+    return std::sqrt(d);
+}
+}  // namespace
+
+bool ALMGPU::test_singular_point(bool jacobian) {
+    cudaStream_t s = P_.stream;
+    if (jacobian)
+        KL_CUDA(cudaMemcpyAsync(xjac_.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    // the current Jacobian, in FP64 fronts (gsALMBase.hpp:631-640)
+    factor64_at(xjac_.get());
+    std::vector<double> ones(n_, 1.0 / std::sqrt((double)n_));
+    KL_CUDA(cudaMemcpyAsync(V_.get(), ones.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < spTestIt_; ++k) {
+        if (S64_->solve(V_.get(), W_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        const double nv = dnorm(W_.get(), n_, s);
+        vec::lincomb(1.0 / nv, W_.get(), 0.0, W_.get(), V_.get(), n_, s);
+    }
+    double dot;
+    const double* a[1] = {V_.get()};
+    const double* b[1] = {P_.d_F.get()};
+    vec::multidot(1, a, b, n_, &dot, s);
+    return std::fabs(dot) < spTestTol_;
+}
+
+bool ALMGPU::is_bifurcation(bool jacobian) {
+    try {
+        return test_singular_point(jacobian);
+    } catch (const Fail&) {
+        return false;
+    }
+}
+
+void ALMGPU::extended_system_iteration() {
+    cudaStream_t s = P_.stream;
+    compute_residual();   // R at (U + DU, L + DL)
+    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, s);
+    factor64_at(x_.get());
+    KL_CUDA(cudaMemcpyAsync(Kv_.get(), P_.d_vals64.get(), sizeof(double) * P_.nnz, cudaMemcpyDeviceToDevice, s));
+    if (S64_->solve(P_.d_F.get(), ut64_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    vec::lincomb(-1.0, R_.get(), 0.0, R_.get(), tmp_.get(), n_, s);
+    if (S64_->solve(tmp_.get(), ub64_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    const double eps = 1e-8;
+    vec::lincomb(1.0, V_.get(), 1.0, DV_.get(), W_.get(), n_, s);
+    // K_eps at x + eps W (FP64 values only; the factorisation of K stays)
+    vec::lincomb(1.0, x_.get(), eps, W_.get(), tmp_.get(), n_, s);
+    P_.set_displacement(tmp_.get());
+    P_.tangent_f64();
+    ++n_jac;
+    // h1 = (K_eps u_t - F) / eps,  h2 = K W + (K_eps u_bar + R) / eps
+    spmv_vals(P_, P_.d_vals64.get(), ut64_.get(), h1_.get());
+    vec::lincomb(1.0 / eps, h1_.get(), -1.0 / eps, P_.d_F.get(), h1_.get(), n_, s);
+    spmv_vals(P_, P_.d_vals64.get(), ub64_.get(), h2_.get());
+    vec::axpby(1.0 / eps, R_.get(), 1.0 / eps, h2_.get(), n_, s);
+    spmv_vals(P_, Kv_.get(), W_.get(), tmp_.get());
+    vec::axpby(1.0, tmp_.get(), 1.0, h2_.get(), n_, s);
+    vec::lincomb(-1.0, h1_.get(), 0.0, h1_.get(), tmp_.get(), n_, s);
+    if (S64_->solve(tmp_.get(), Vt_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    vec::lincomb(-1.0, h2_.get(), 0.0, h2_.get(), tmp_.get(), n_, s);
+    if (S64_->solve(tmp_.get(), Vb_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+    double d[3];
+    const double* xs[3] = {W_.get(), W_.get(), W_.get()};
+    const double* ys[3] = {W_.get(), Vb_.get(), Vt_.get()};
+    vec::multidot(3, xs, ys, n_, d, s);
+    const double nW = std::sqrt(d[0]);
+    dL_ = -(d[1] / nW + nW - 1.0) / (d[2] / nW);
+    vec::lincomb(dL_, ut64_.get(), 1.0, ub64_.get(), dU_.get(), n_, s);
+    vec::lincomb(dL_, Vt_.get(), 1.0, Vb_.get(), dV_.get(), n_, s);
+}
+
+bool ALMGPU::extended_system_solve(double tol) {
+    cudaStream_t s = P_.stream;
+    factor64_at(U_.get());
+    for (DevBuf<double>* b : {&DV_, &DU_, &dV_, &dU_}) b->zero(s);
+    DL_ = dL_ = 0.0;
+    for (num_it_ = 0; num_it_ < maxIt_; ++num_it_) {
+        extended_system_iteration();
+        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
+        DL_ += dL_;
+        vec::axpby(1.0, dV_.get(), 1.0, DV_.get(), n_, s);
+        vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, s);
+        factor64_at(x_.get());
+        vec::lincomb(1.0, V_.get(), 1.0, DV_.get(), W_.get(), n_, s);
+        spmv_vals(P_, P_.d_vals64.get(), W_.get(), tmp_.get());
+        residueKTPhi_ = dnorm(tmp_.get(), n_, s);
+        compute_residual();
+        compute_residual_norms();
+        if (residueKTPhi_ < tol) {
+            vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
+            L_ += DL_;
+            return true;
+        }
+        if (num_it_ == maxIt_ - 1) {
+            if (spFail_ == 1) {
+                vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
+                L_ += DL_;
+            } else {
+                for (DevBuf<double>* b : {&DV_, &DU_, &dV_, &dU_}) b->zero(s);
+                DL_ = dL_ = 0.0;
+            }
+            return false;
+        }
+    }
+    return true;
+}
+
+bool ALMGPU::bisection_solve(double tol) {
+    cudaStream_t s = P_.stream;
+    DevBuf<double> Uold(n_);
+    KL_CUDA(cudaMemcpyAsync(Uold.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    double Lold = L_;
+    const double dL = arcLength_;
+    const bool adaptive = adaptive_;
+    adaptive_ = false;
+    bool converged = false;
+    stability_impl(true, -1e2);
+    const double reference = indicator_;
+    stability_impl(false, -1e2);
+    int64_t fa = negatives_;
+    for (int k = 1; k < maxIt_; ++k) {
+        KL_CUDA(cudaMemcpyAsync(U_.get(), Uold.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        L_ = Lold;
+        const int status = step();
+        stability_impl(true, -1e2);
+        const int64_t fb = negatives_;
+        if (fa == fb && status == ST_SUCCESS) {
+            KL_CUDA(cudaMemcpyAsync(Uold.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+            Lold = L_;
+            fa = fb;
+        } else {
+            arcLength_ = arcLength_ / 2.0;
+        }
+        stability_impl(false, -1e2);
+        if (std::fabs(indicator_ / reference) < tol) {
+            converged = true;
+            break;
+        }
+    }
+    arcLength_ = dL;
+    adaptive_ = adaptive;
+    // null vector of the last Jacobian by inverse iteration (gsALMBase.hpp:820-836)
+    factor64_at(xjac_.get());
+    std::vector<double> ones(n_, 1.0 / std::sqrt((double)n_));
+    KL_CUDA(cudaMemcpyAsync(V_.get(), ones.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, s));
+    DevBuf<double> Vold(n_);
+    Vold.zero(s);
+    for (int k = 0; k < 5; ++k) {
+        if (S64_->solve(V_.get(), W_.get(), 1) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
+        const double nv = dnorm(W_.get(), n_, s);
+        vec::lincomb(1.0 / nv, W_.get(), 0.0, W_.get(), V_.get(), n_, s);
+        vec::lincomb(1.0, V_.get(), -1.0, Vold.get(), tmp_.get(), n_, s);
+        if (dnorm(tmp_.get(), n_, s) < tolerance_) {
+            converged = true;
+            break;
+        }
+        KL_CUDA(cudaMemcpyAsync(Vold.get(), V_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    }
+    return converged;
+}
+
+int ALMGPU::compute_singular_point(const double* d_U, double L, bool switch_branch_after, bool jacobian,
+                                   bool test_point) {
+    try {
+        const bool test = test_point ? test_singular_point(jacobian) : true;
+        KL_CUDA(cudaMemcpyAsync(U_.get(), d_U, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+        L_ = L;
+        if (test) {
+            if (!S64_) factor64_at(U_.get());
+            if (spTolB_ != 0.0) bisection_solve(spTolB_);
+            const bool converged = extended_system_solve(spTolE_);
+            if (switch_branch_after && (converged || spFail_ == 1)) switch_branch();
+            stability_ = stabilityPrev_;
+        }
+        return ST_SUCCESS;
+    } catch (const Fail& f) {
+        return f.code;
+    }
+}
+
+void ALMGPU::switch_branch() {
+    // gsALMBase.hpp:839-852
+    cudaStream_t s = P_.stream;
+    if (!S64_) return;
+    const double nv = dnorm(V_.get(), n_, s);
+    vec::lincomb(1.0 / nv, V_.get(), 0.0, V_.get(), V_.get(), n_, s);
+    const double xi = dnorm(V_.get(), n_, s) / tau_;
+    vec::lincomb(xi, V_.get(), 0.0, V_.get(), DU_.get(), n_, s);
+    vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
+    DLold_ = 0.0;
+    DUold_.zero(s);
 }
 
 }  // namespace klsa

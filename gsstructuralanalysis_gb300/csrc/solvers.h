@@ -83,6 +83,11 @@ public:
     bool stability_change() const { return stability_ * stabilityPrev_ < 0; }
     int64_t negatives() const { return negatives_; }
     int bifurcation_method() const { return bifurcation_; }
+    // singular points (gsALMBase.hpp:421-512, 628-852); U in internal order on the device
+    bool is_bifurcation(bool jacobian);
+    int compute_singular_point(const double* d_U, double L, bool switch_branch, bool jacobian, bool test_point);
+    void switch_branch();
+    const double* V() const { return V_.get(); }
     void set_length(double l);
     double reduce_length(double fac) { arcLength_ *= fac; return arcLength_; }
     double length() const { return arcLength_; }
@@ -127,6 +132,11 @@ private:
     void lambdas_crisfield();
     void consistent_predictor(const double* prevU, double prevL);
     void stability_impl(bool jacobian, double shift);
+    bool test_singular_point(bool jacobian);
+    void factor64_at(const double* d_x);   // FP64 tangent at x, FP64 fronts
+    bool extended_system_solve(double tol);
+    void extended_system_iteration();
+    bool bisection_solve(double tol);
 
     Problem& P_;
     Method method_;
@@ -162,6 +172,14 @@ private:
     double indicator_ = 0.0;
     int64_t negatives_ = 0;
     bool fact_stale_ = false;      // the eigenvalue indicator reused the factorisation workspace
+    // singular points: options, FP64 solver and extended-system vectors
+    double tau_ = 1e3, tolerance_ = 1e-6, spTestTol_ = 1e-6, spTolE_ = 1e-10, spTolB_ = 0.0;
+    int spFail_ = 1, spTestIt_ = 5;
+    std::unique_ptr<LinearSolver> S64_;
+    DevBuf<double> V_, DV_, dV_, ut64_, ub64_, h1_, h2_, Vt_, Vb_, W_, Kv_;
+    double residueKTPhi_ = 0.0;
+public:
+    double residue_ktphi() const { return residueKTPhi_; }
 };
 
 }  // namespace klsa

@@ -142,6 +142,17 @@ int klsa_alm_compute_stability(klsa_alm* a, int jacobian, double shift);
    stabilityChange() (gsALMBase.hpp:624-627) and the number of negative entries of the
    stability vector (inertia of the Jacobian for "Determinant"). Any out pointer may be NULL. */
 int klsa_alm_stability(klsa_alm* a, double* indicator, int* stability, int* change, int64_t* negatives);
+/* Singular points (gsALMBase.hpp:421-512, 628-852), with the options "SingularPointFailure",
+ * "SingularPointTestTol", "SingularPointTestIt", "SingularPointComputeTolE",
+ * "SingularPointComputeTolB" (bisection stage when nonzero), "Perturbation" and "Tol".
+ * isBifurcation(bool jacobian) (gsALMBase.h:237): 1 bifurcation, 0 limit point, < 0 error.
+ * computeSingularPoint(U, L, switchBranch, jacobian, testPoint) (gsALMBase.h:234) -> gsStatus.
+ * switchBranch() (gsALMBase.h:257).  solutionV() (gsALMBase.h:169): the null vector. */
+int klsa_alm_is_bifurcation(klsa_alm* a, int jacobian);
+int klsa_alm_compute_singular_point(klsa_alm* a, const double* U, double L, int switch_branch, int jacobian,
+                                    int test_point);
+int klsa_alm_switch_branch(klsa_alm* a);
+int klsa_alm_solution_v(klsa_alm* a, double* V);
 int klsa_alm_step(klsa_alm* a);                           /* step() -> gsStatus */
 int klsa_alm_set_length(klsa_alm* a, double length);      /* setLength */
 int klsa_alm_reduce_length(klsa_alm* a, double factor);   /* reduceLength */

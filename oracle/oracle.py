@@ -311,7 +311,9 @@ class _ALMBase:
         self.F = np.asarray(F, dtype=np.float64)
         self.opts = dict(MaxIter=100, Tol=1e-6, TolF=1e-3, TolU=1e-6, Length=1e-2, AdaptiveLength=False,
                          AdaptiveIterations=10, Quasi=False, QuasiIterations=-1, BifurcationMethod=1,
-                         Relaxation=1.0, Scaling=-1.0, AngleMethod=0)
+                         Relaxation=1.0, Scaling=-1.0, AngleMethod=0, Perturbation=1e3, SingularPointFailure=1,
+                         SingularPointTestTol=1e-6, SingularPointTestIt=5, SingularPointComputeTolE=1e-10,
+                         SingularPointComputeTolB=0.0)
         if options:
             self.opts.update(options)
         self.solver = SuperLUSolver()
@@ -372,6 +374,145 @@ class _ALMBase:
 
     def stability_change(self):
         return self.stability * self.stabilityPrev < 0
+
+    # ---- singular points (gsALMBase.hpp:421-512, 628-728, 839-852) ---------------------------
+    def is_bifurcation(self, jacobian=False):
+        """_testSingularPoint: a few inverse iterations from the normalised ones vector; the point is
+        a bifurcation when the approximate null vector is orthogonal to the load."""
+        if jacobian:
+            K = self.jacobian(self.U)
+            self.counts["jac"] += 1
+            self.solver.compute(K)
+            self.jacMat = K
+        n = self.numDof
+        V = np.ones(n) / np.sqrt(n)
+        self.solver.compute(self.jacMat)
+        for _ in range(int(self.opts["SingularPointTestIt"])):
+            V = self.solver.solve(V)
+            V = V / np.linalg.norm(V)
+        self.V = V
+        return abs(float(V @ self.F)) < float(self.opts["SingularPointTestTol"])
+
+    def compute_singular_point(self, U, L, switch_branch=False, jacobian=False, test_point=True):
+        return _status_of(lambda: self._compute_singular_point(U, L, switch_branch, jacobian, test_point))
+
+    def _compute_singular_point(self, U, L, switch_branch, jacobian, test_point):
+        test = self.is_bifurcation(jacobian) if test_point else True
+        self.U = np.asarray(U, dtype=np.float64).copy()
+        self.L = float(L)
+        if test:
+            if float(self.opts["SingularPointComputeTolB"]) != 0:
+                self._bisection_solve(self.U, self.L, float(self.opts["SingularPointComputeTolB"]))
+            converged = self._extended_system_solve(self.U, self.L, float(self.opts["SingularPointComputeTolE"]))
+            if switch_branch and (converged or int(self.opts["SingularPointFailure"]) == 1):
+                self.switch_branch()
+            self.stability = self.stabilityPrev
+
+    def _extended_system_solve(self, U, L, tol):
+        self.U, self.L = U.copy(), L
+        K = self.jacobian(self.U)
+        self.solver.compute(K)
+        self.jacMat = K
+        n = self.numDof
+        self.DeltaV = np.zeros(n); self.DeltaU = np.zeros(n); self.DeltaL = 0.0
+        self.deltaV = np.zeros(n); self.deltaU = np.zeros(n); self.deltaL = 0.0
+        for it in range(self.maxIt):
+            self.num_iterations = it
+            self._extended_system_iteration()
+            self.DeltaU = self.DeltaU + self.deltaU
+            self.DeltaL += self.deltaL
+            self.DeltaV = self.DeltaV + self.deltaV
+            K = self.jacobian(self.U + self.DeltaU)
+            self.solver.compute(K)
+            self.jacMat = K
+            self.residueKTPhi = float(np.linalg.norm(K @ (self.V + self.DeltaV)))
+            self.resVec = self.res(self.U + self.DeltaU, self.L + self.DeltaL)
+            self.compute_residual_norms()
+            if self.residueKTPhi < tol:
+                self.U = self.U + self.DeltaU
+                self.L += self.DeltaL
+                return True
+            if it == self.maxIt - 1:
+                if int(self.opts["SingularPointFailure"]) == 1:
+                    self.U = self.U + self.DeltaU
+                    self.L += self.DeltaL
+                else:
+                    self.DeltaV = np.zeros(n); self.DeltaU = np.zeros(n); self.DeltaL = 0.0
+                    self.deltaV = np.zeros(n); self.deltaU = np.zeros(n); self.deltaL = 0.0
+                return False
+        return True
+
+    def _extended_system_iteration(self):
+        x = self.U + self.DeltaU
+        R = self.res(x, self.L + self.DeltaL)
+        K = self.jacobian(x)
+        self.solver.compute(K)
+        ut = self.solver.solve(self.F)
+        ubar = self.solver.solve(-R)
+        eps = 1e-8
+        W = self.V + self.DeltaV
+        Keps = self.jacobian(x + eps * W)
+        h1 = (Keps @ ut) / eps - self.F / eps
+        h2 = K @ W + (Keps @ ubar + R) / eps
+        Vt = self.solver.solve(-h1)
+        Vbar = self.solver.solve(-h2)
+        nW = float(np.linalg.norm(W))
+        Wn = W / nW
+        self.deltaL = -(float(Wn @ Vbar) + nW - 1.0) / float(Wn @ Vt)
+        self.deltaU = self.deltaL * ut + ubar
+        self.deltaV = self.deltaL * Vt + Vbar
+
+    def _bisection_solve(self, U, L, tol):
+        """_bisectionSolve (gsALMBase.hpp:758-837): arc-length steps from the last point with the same
+        number of negative pivots, halving the length when the count changes, until the indicator
+        drops below tol of its start value; then the null vector by inverse iteration."""
+        self.U, self.L = U.copy(), L
+        U_old, L_old = self.U.copy(), self.L
+        dL = self.arcLength
+        adaptive = self.adaptive
+        self.adaptive = False
+        converged = False
+        self.compute_stability(jacobian=True)
+        reference = self.indicator
+        self.compute_stability(jacobian=False)
+        fa = self.negatives
+        for _ in range(1, self.maxIt):
+            self.U, self.L = U_old.copy(), L_old
+            status = self.step()
+            self.compute_stability(jacobian=True)
+            fb = self.negatives
+            if fa == fb and status == 0:
+                U_old, L_old = self.U.copy(), self.L
+                fa = fb
+            else:
+                self.arcLength = self.arcLength / 2.0
+            self.compute_stability(jacobian=False)
+            if abs(self.indicator / reference) < tol:
+                converged = True
+                break
+        self.arcLength = dL
+        self.adaptive = adaptive
+        n = self.numDof
+        self.V = np.ones(n) / np.sqrt(n)
+        Vold = np.zeros(n)
+        for _ in range(5):
+            self.solver.compute(self.jacMat)
+            self.V = self.solver.solve(self.V)
+            self.V = self.V / np.linalg.norm(self.V)
+            if np.linalg.norm(self.V - Vold) < float(self.opts["Tol"]):
+                converged = True
+                break
+            Vold = self.V.copy()
+        return converged
+
+    def switch_branch(self):
+        """switchBranch (gsALMBase.hpp:839-852): perturb U along the null vector by |V| / tau."""
+        self.V = self.V / np.linalg.norm(self.V)
+        xi = float(np.linalg.norm(self.V)) / float(self.opts["Perturbation"])
+        self.DeltaU = xi * self.V
+        self.U = self.U + self.DeltaU
+        self.DeltaLold = 0.0
+        self.DeltaUold = np.zeros(self.numDof)
 
     def apply_options(self):
         o = self.opts

@@ -167,3 +167,42 @@ def test_quasi_newton_adaptive_length(lib, oracle_mod, method):
         U, L = alm.solutionU(), alm.solutionL()
         assert np.linalg.norm(U - ref.U) / np.linalg.norm(ref.U) < 1e-6, k
         assert abs(L - ref.L) / abs(ref.L) < 1e-6, k
+
+
+@pytest.mark.parametrize("tolB", [0.0, 0.1])
+def test_singular_point_and_branch_switch(lib, oracle_mod, tolB):
+    """At the limit point of the roof (stability change of the Determinant indicator): the
+    singular-point test (a limit point, not a bifurcation), the extended-system Newton for the
+    critical point (with and without the bisection stage) and switchBranch, against the oracle
+    (gsALMBase.hpp:421-512, 628-852).  The critical load factor is converged to FP64 accuracy."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=8, p=2, load=1.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    opts = dict(Length=0.004, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=8, BifurcationMethod=0,
+                SingularPointComputeTolB=tolB)
+    alm = G.ALMCrisfield(gp, opts)
+    alm.initialize()
+    ref = oracle_mod.ALMCrisfield(oa.jacobian, oa.al_residual, oa.force(), opts)
+    ref.initialize()
+    found = False
+    for k in range(12):
+        Uold, Lold = alm.solutionU(), alm.solutionL()
+        Uref, Lref = ref.U.copy(), ref.L
+        assert alm.step() == 0 and ref.step() == 0
+        assert alm.stabilityChange() == ref.stability_change(), k
+        if ref.stability_change():
+            found = True
+            assert alm.isBifurcation(False) == ref.is_bifurcation(False)
+            assert alm.computeSingularPoint(Uold, Lold, False, False, False) == 0
+            assert ref.compute_singular_point(Uref, Lref, False, False, False) == 0
+            U, L = alm.solutionU(), alm.solutionL()
+            assert abs(L - ref.L) <= 1e-8 * abs(ref.L)
+            assert np.linalg.norm(U - ref.U) <= 1e-6 * np.linalg.norm(ref.U)
+            if tolB == 0.0:
+                # without the bisection stage both use the null vector of the same Jacobian (with it,
+                # the number of bisection steps depends on min D, which differs with the ordering)
+                alm.switchBranch()
+                ref.switch_branch()
+                assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-6 * np.linalg.norm(ref.U)
+            break
+    assert found
