@@ -756,7 +756,7 @@ def run_eigen(args):
     # size-independent check in FP64 on the host: relative eigen-residuals of every pair
     KL = gp.jacobian(np.zeros(gp.ndof), 1)
     M = gp.mass()
-    sn = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "Refinement": 20, "RefineTol": 1e-14})
+    sn = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "FrontPrecision": 64, "Refinement": 4, "RefineTol": 1e-15})
     sn.setLoad(EIG_SCALING)
     sn.solveLinear()
     uL = sn.solution()

@@ -108,9 +108,12 @@ __global__ void __launch_bounds__(DIAG_THREADS) mf_diag_kernel(const int4* __res
                                                                const int64_t* __restrict__ front_off,
                                                                const int64_t* __restrict__ linv_off, T* pool, T* Dvec,
                                                                T* linv, int* status) {
-    __shared__ __align__(16) T col[2][NB];
-    __shared__ __align__(16) T xrow[2][NB];
-    __shared__ T sinv[2];
+    // published per pivot pair (j, j+1), double-buffered by pair parity: columns j and j+1 of A
+    // (rows >= j) and rows j, j+1 of X
+    __shared__ __align__(16) T col0s[2][NB];
+    __shared__ __align__(16) T col1s[2][NB];
+    __shared__ __align__(16) T xr0s[2][NB];
+    __shared__ __align__(16) T xr1s[2][NB];
     __shared__ int bad;
     const int nd = items[blockIdx.x].x;
     const int fN = f[nd], kN = k[nd];
@@ -134,42 +137,95 @@ __global__ void __launch_bounds__(DIAG_THREADS) mf_diag_kernel(const int4* __res
         x[e] = (r == c) ? T(1) : T(0);
     }
     if (tid == 0) bad = 0;
-    __syncthreads();
-    for (int j = 0; j < NB; ++j) {
-        const int b = j & 1;
-        if ((j >> 3) == q && r >= j) {
-            const T v = sel8(a, j & 7);
-            col[b][r] = v;
-            if (r == j) {
-                T d = v;
-                if (!(fabs(d) > T(0)) || !isfinite(d)) {
-                    if (j < kk) bad = 1;
-                    d = T(1);
+    // pivot pairs, one barrier each (the pair two steps back used the same buffers, and every
+    // thread has passed the previous pair's barrier since reading them); pivots beyond kk are the
+    // identity padding (an odd kk pairs its last pivot with a padding pivot)
+    for (int jq = 0; jq * 8 < kk; ++jq) {
+#pragma unroll
+        for (int jj = 0; jj < 8; jj += 2) {
+            const int j = jq * 8 + jj;
+            if (j < kk) {
+                const int pb = (jj >> 1) & 1;
+                T* col0 = col0s[pb];
+                T* col1 = col1s[pb];
+                T* xr0 = xr0s[pb];
+                T* xr1 = xr1s[pb];
+                if (jq == q && r >= j) {
+                    col0[r] = a[jj];
+                    col1[r] = a[jj + 1];
                 }
-                sinv[b] = pivot_recip(d);
+                if (r == j) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) xr0[cb + e] = x[e];
+                }
+                if (r == j + 1) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) xr1[cb + e] = x[e];
+                }
+                __syncthreads();
+                // the 2x2 pivot block, rebuilt by every thread
+                T d0 = col0[j];
+                const T e10 = col0[j + 1], f11 = col1[j + 1];
+                if (!(fabs(d0) > T(0)) || !isfinite(d0)) {
+                    if (tid == 0) bad = 1;
+                    d0 = T(1);
+                }
+                const T inv0 = pivot_recip(d0);
+                const T l10 = e10 * inv0;
+                T d1 = f11 - l10 * e10;
+                if (!(fabs(d1) > T(0)) || !isfinite(d1)) {
+                    if (tid == 0 && j + 1 < kk) bad = 1;
+                    d1 = T(1);
+                }
+                const T inv1 = pivot_recip(d1);
+                // own row: L(r, j), column j+1 after the column-j update, L(r, j+1)
+                const T lr0 = col0[r] * inv0;
+                const T ar1 = col1[r] - lr0 * e10;
+                const T lr1 = ar1 * inv1;
+                const T g = inv0 * e10;
+                if (q > jq) {
+                    // every column right of the pair: rank-2 update only
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const T cv0 = col0[cb + e], cv1 = col1[cb + e];
+                        const T an = a[e] - lr0 * cv0 - lr1 * (cv1 - cv0 * g);
+                        a[e] = (cb + e <= r) ? an : a[e];
+                    }
+                } else if (q < jq) {
+                    // every column left of the pair: only X changes, in the rows below it
+                    if (r > j) {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            const T xv0 = xr0[cb + e], xv1 = xr1[cb + e];
+                            const T xn2 = x[e] - lr0 * xv0 - lr1 * (xv1 - l10 * xv0);
+                            const T xn1 = x[e] - l10 * xv0;
+                            x[e] = (r > j + 1) ? xn2 : xn1;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        const int c = cb + e;
+                        const T cv0 = col0[c], cv1 = col1[c], xv0 = xr0[c], xv1 = xr1[c];
+                        // A: rank-2 update of c > j+1, columns j and j+1 become L, the pivot
+                        // (j+1, j+1) d1
+                        const T an = a[e] - lr0 * cv0 - lr1 * (cv1 - cv0 * g);
+                        T av = a[e];
+                        if (c > j + 1 && c <= r) av = an;
+                        else if (c == j && r > j) av = lr0;
+                        else if (c == j + 1 && r > j + 1) av = lr1;
+                        else if (c == j + 1 && r == j + 1) av = d1;
+                        a[e] = av;
+                        // X: rows below the pair take both steps, row j+1 the first
+                        const T xn2 = x[e] - lr0 * xv0 - lr1 * (xv1 - l10 * xv0);
+                        const T xn1 = x[e] - l10 * xv0;
+                        T xv = x[e];
+                        if (c <= j + 1 && r > j + 1) xv = xn2;
+                        else if (c <= j && r == j + 1) xv = xn1;
+                        x[e] = xv;
+                    }
+                }
             }
-        }
-        if (r == j) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) xrow[b][cb + e] = x[e];
-        }
-        __syncthreads();
-        const T inv = sinv[b];
-        const T l = col[b][r] * inv;   // L(r, j) for r > j
-        T cv[8], xv[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            cv[e] = col[b][cb + e];
-            xv[e] = xrow[b][cb + e];
-        }
-        const bool below = r > j;
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int c = cb + e;
-            const T an = fma(-l, cv[e], a[e]);
-            a[e] = (c > j && c <= r) ? an : ((c == j && below) ? a[e] * inv : a[e]);
-            const T xn = fma(-l, xv[e], x[e]);
-            x[e] = (c <= j && below) ? xn : x[e];
         }
     }
     T* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
