@@ -244,6 +244,20 @@ __global__ void __launch_bounds__(DIAG_THREADS) mf_diag_kernel(const int4* __res
     if (tid == 0 && bad) atomicExch(status, 1);
 }
 
+// Four consecutive shared-memory values (16-byte aligned) in one or two vector loads.
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+    const double2 x = *reinterpret_cast<const double2*>(p);
+    const double2 y = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
+
+// Staged 64-wide tiles use rows padded to NBP = 68 elements, keeping the vectors aligned.
+constexpr int NBP = NB + 4;
+
 // Panel rows [r0, r0 + 64) below the diagonal tile: W = A21 X^T (X = L11^-1 from the diagonal
 // kernel), L21 = W D^-1 written in place and W kept for the trailing update.  A 64 x 64 x kk
 // product per CTA: thread (tx, ty) owns rows tx + 16 i and columns ty + 16 q.
@@ -253,7 +267,7 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
                                                        const int64_t* __restrict__ linv_off,
                                                        const int64_t* __restrict__ ws_off, T* pool,
                                                        const T* __restrict__ linv, T* ws) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T(*As)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);              // As[m][rr] = A21(r0 + rr, m)
     T(*Xs)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));   // Xs[m][jj] = X(jj, m)
     T* Ds = reinterpret_cast<T*>(smem_raw + 2 * sizeof(T) * NB * (NB + 1));
@@ -315,33 +329,34 @@ __global__ void __launch_bounds__(256) mf_panel_kernel(const int4* __restrict__ 
     }
 }
 
-// Trailing update of one 64x64 lower tile: A[R, C] -= W[R, :] L[C, :]^T.
+// Trailing update of one 64x64 lower tile: A[R, C] -= W[R, :] L[C, :]^T.  Thread (tx, ty) owns
+// rows 4tx..4tx+3 and columns 4ty..4ty+3; per k step two 16-byte shared loads feed 16 FMAs.
 template <class T>
 __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__ items, int t, const int* __restrict__ f,
                                                         const int* __restrict__ k, const int64_t* __restrict__ front_off,
                                                         const int64_t* __restrict__ ws_off, T* pool,
                                                         const T* __restrict__ ws) {
-    extern __shared__ unsigned char smem_raw[];
-    T(*Ws)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);                              // Ws[m][rr] = W[R0+rr][m]
-    T(*Ls)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));  // Ls[m][cc] = L[C0+cc][c0+m]
-    int4 it = items[blockIdx.x];
-    int nd = it.x;
-    int fN = f[nd], kN = k[nd];
-    int c0 = t * NB;
-    int kk = min(NB, kN - c0);
-    int c1 = c0 + kk;
-    int R0 = c1 + it.y * NB, C0 = c1 + it.z * NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T(*Ws)[NBP] = reinterpret_cast<T(*)[NBP]>(smem_raw);                          // Ws[m][rr] = W[R0+rr][m]
+    T(*Ls)[NBP] = reinterpret_cast<T(*)[NBP]>(smem_raw + sizeof(T) * NB * NBP);   // Ls[m][cc] = L[C0+cc][c0+m]
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x;
+    const int fN = f[nd], kN = k[nd];
+    const int c0 = t * NB;
+    const int kk = min(NB, kN - c0);
+    const int c1 = c0 + kk;
+    const int R0 = c1 + it.y * NB, C0 = c1 + it.z * NB;
     T* F = pool + front_off[nd];
     const T* W = ws + ws_off[nd];
-    int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lt = threadIdx.x & 63, lg = threadIdx.x >> 6;
     {
         T vw[16], vl[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-            int m = lg + 4 * q;
-            vw[q] = (m < kk && R0 + lt < fN) ? W[(int64_t)m * fN + R0 + lt] : 0.f;
-            vl[q] = (m < kk && C0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + C0 + lt] : 0.f;
+            const int m = lg + 4 * q;
+            vw[q] = (m < kk && R0 + lt < fN) ? W[(int64_t)m * fN + R0 + lt] : T(0);
+            vl[q] = (m < kk && C0 + lt < fN) ? F[(int64_t)(c0 + m) * fN + C0 + lt] : T(0);
         }
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
@@ -354,35 +369,34 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[i][q] = 0.f;
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+#pragma unroll 4
     for (int m = 0; m < kk; ++m) {
         T a[4], b[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = Ws[m][tx + 16 * i];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) b[q] = Ls[m][ty + 16 * q];
+        ld4(&Ws[m][4 * tx], a);
+        ld4(&Ls[m][4 * ty], b);
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][q] = fma(a[i], b[q], acc[i][q]);
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     T old[4][4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        int C = C0 + ty + 16 * q;
+    for (int j = 0; j < 4; ++j) {
+        const int C = C0 + 4 * ty + j;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            int R = R0 + tx + 16 * i;
-            old[i][q] = (C < fN && R < fN && R >= C) ? F[(int64_t)C * fN + R] : 0.f;
+            const int R = R0 + 4 * tx + i;
+            old[i][j] = (C < fN && R < fN && R >= C) ? F[(int64_t)C * fN + R] : T(0);
         }
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        int C = C0 + ty + 16 * q;
+    for (int j = 0; j < 4; ++j) {
+        const int C = C0 + 4 * ty + j;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            int R = R0 + tx + 16 * i;
-            if (C < fN && R < fN && R >= C) F[(int64_t)C * fN + R] = old[i][q] - acc[i][q];
+            const int R = R0 + 4 * tx + i;
+            if (C < fN && R < fN && R >= C) F[(int64_t)C * fN + R] = old[i][j] - acc[i][j];
         }
     }
 }
@@ -413,7 +427,7 @@ __global__ void __launch_bounds__(256) mf_xoff_kernel(const int4* __restrict__ i
                                                       const int64_t* __restrict__ linv_off,
                                                       const int64_t* __restrict__ xinv_off, const T* __restrict__ pool,
                                                       const T* __restrict__ linv, T* __restrict__ xinv) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T(*As)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw);                               // As[q][r] = L(bi, m)(r, q)
     T(*Bs)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(smem_raw + sizeof(T) * NB * (NB + 1));   // Bs[q][c] = X(m, bj)(q, c)
     const int4 it = items[blockIdx.x];
@@ -536,7 +550,7 @@ template <class T, int NR>
 __global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_own_kernel(
     const int4* __restrict__ items, int n, const int* __restrict__ k, const int* __restrict__ own,
     const int64_t* __restrict__ xinv_off, const T* __restrict__ xinv, const T* __restrict__ y, T* __restrict__ z) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* ys = reinterpret_cast<T*>(smem_raw);   // kN * NR
     const int4 it = items[blockIdx.x];
     const int nd = it.x, rb = it.y;
@@ -575,7 +589,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_fwd_halo_kernel(
     const int4* __restrict__ items, int n, const int* __restrict__ f, const int* __restrict__ k,
     const int* __restrict__ own, const int64_t* __restrict__ front_off, const int64_t* __restrict__ upd_off,
     const T* __restrict__ pool, const T* __restrict__ z, T* upd) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* zs = reinterpret_cast<T*>(smem_raw);                                  // kN * NR
     __shared__ T part[4][NR][NB];
     const int4 it = items[blockIdx.x];
@@ -626,7 +640,7 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_z_kernel(
     const int* __restrict__ own, const int64_t* __restrict__ front_off, const int64_t* __restrict__ halo_off,
     const int* __restrict__ halo, const T* __restrict__ pool, const T* __restrict__ Dvec, const T* __restrict__ z,
     const T* __restrict__ x, T* __restrict__ w) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* xs = reinterpret_cast<T*>(smem_raw);   // hN * NR
     const int4 it = items[blockIdx.x];
     const int nd = it.x, jb = it.y;
@@ -665,7 +679,7 @@ template <class T, int NR>
 __global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_own_kernel(
     const int4* __restrict__ items, int n, const int* __restrict__ k, const int* __restrict__ own,
     const int64_t* __restrict__ xinv_off, const T* __restrict__ xinv, const T* __restrict__ w, T* __restrict__ x) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T* ws = reinterpret_cast<T*>(smem_raw);   // kN * NR
     __shared__ T part[4][NR][NB];
     const int4 it = items[blockIdx.x];
@@ -724,7 +738,7 @@ __global__ void mf_stability_kernel(int n, const T* __restrict__ D, double* out_
     }
 }
 
-constexpr size_t gemm_smem(size_t elem) { return 2 * elem * NB * (NB + 1) + elem * NB; }
+constexpr size_t gemm_smem(size_t elem) { return 2 * elem * NB * NBP + elem * NB; }
 
 }  // namespace
 
