@@ -167,7 +167,7 @@ def run_ours(args):
         paths = [learned.generate_path(G, learned.imperfect_problem(base, modes, s), ALM_OPTS, nsteps_path)
                  for s in range(args.train_paths)]
         t1 = time.perf_counter()
-        tp = learned.train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3)
+        tp = learned.train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=1e-3, chunk=5)
         train_info = {"paths": args.train_paths, "points_per_path": nsteps_path, "samples": tp.nsamples,
                       "path_generation_s": t1 - t0, "training_s": tp.seconds["train"], "alpha": tp.alpha,
                       "best_epoch": tp.best_epoch, "val_rel_error_vs_extrapolation": tp.val_rel_error}
@@ -354,13 +354,26 @@ def roofline(prof, stats, args):
                      "gbs": byts / t / 1e9, "tflops": fl / t / 1e12, "bytes_per_launch": byts}
     dom = max(detail, key=lambda k: detail[k]["ms_total_per_step"])
     ach = detail[dom]["gbs"]
-    # DRAM traffic per launch from one ncu capture (profiles/arclength_50k_launches_and_mf_diag_kernel.md):
-    # top-level single-front tiles of mf_diag_kernel read 23-25 KB and write 0 B of DRAM (results stay in
-    # L2) against 48 KB algorithmic; the live average above spans multi-front launches, so the captured
-    # launches are reported beside it rather than as this average's traffic.
-    capture = {"kernel": "mf_diag_kernel", "launches": "top-level single-front tiles (timed launches 35-37)",
-               "dram_bytes_per_launch": 25344, "algorithmic_bytes_per_launch": 49152,
-               "source": "profiles/arclength_50k_launches_and_mf_diag_kernel.md"}
+    # DRAM traffic per launch from ncu captures (profiles/arclength_50k_launches_diag_update.md).
+    # The first three timed mf_update_kernel launches (bottom levels, 957-1710 tiles) read 27-47 MB
+    # of DRAM against at most 64 KB algorithmic per tile; mid-level launches of 21, 7 and 15 tiles
+    # read 533, 257 and 404 KB and wrote 0 B: the written tiles stay in L2, and the panel blocks are read from
+    # L2 by the tiles that share them.  Top-level single-front mf_diag_kernel tiles read 45 KB and
+    # wrote 0 B against 48 KB algorithmic.  The live averages above span every level's launch shape,
+    # so the captured launches are reported beside them rather than as their traffic.
+    capture = [
+        {"kernel": "mf_update_kernel", "launches": "first three timed launches (1710, 1056, 957 tiles, bottom levels)",
+         "dram_bytes_per_launch": [46553344 + 123392, 38491136 + 2048, 26986240],
+         "algorithmic_bytes_upper_bound": [1710 * 65536, 1056 * 65536, 957 * 65536],
+         "source": "profiles/arclength_50k_launches_diag_update.md"},
+        {"kernel": "mf_update_kernel", "launches": "timed launches 60-62 (21, 7, 15 tiles)",
+         "dram_bytes_per_launch": [532736, 256512, 404480],
+         "algorithmic_bytes_per_launch": [21 * 65536, 7 * 65536, 15 * 65536],
+         "source": "profiles/arclength_50k_launches_diag_update.md"},
+        {"kernel": "mf_diag_kernel", "launches": "top-level single-front tiles (timed launches 35-37)",
+         "dram_bytes_per_launch": [45056, 45056, 44544], "algorithmic_bytes_per_launch": [49152] * 3,
+         "source": "profiles/arclength_50k_launches_diag_update.md"},
+    ]
     return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
             "traffic": None, "traffic_capture": capture, "peak_source": src,
             "note": "multifrontal kernels are bound by the latency of the pivot-tile chain, not by HBM or FLOP rate; "
@@ -813,7 +826,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
-    ap.add_argument("--train-paths", type=int, default=6)
+    ap.add_argument("--train-paths", type=int, default=16)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
