@@ -99,6 +99,15 @@ SIGNATURES = {
     "klsa_alm_step_learned": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
+    "klsa_dynamic_create": (_c_int, [_c_vp, _c_char_p, _c_int, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_dynamic_destroy": (_c_int, [_c_vp]),
+    "klsa_dynamic_set_load_table": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int]),
+    "klsa_dynamic_set_state": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_dynamic_state": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "klsa_dynamic_step": (_c_int, [_c_vp, _c_dbl]),
+    "klsa_dynamic_set_time": (_c_int, [_c_vp, _c_dbl]),
+    "klsa_dynamic_time": (_c_dbl, [_c_vp]),
+    "klsa_dynamic_iterations": (_c_int, [_c_vp]),
     "klsa_batch_create": (_c_int, [_c_vp, _c_int, ctypes.POINTER(_c_vp)]),
     "klsa_batch_destroy": (_c_int, [_c_vp]),
     "klsa_batch_info": (_c_int, [_c_vp, _c_vp]),
@@ -519,6 +528,70 @@ def modal(problem: Problem, nev: int, shift: float = 0.0, options: dict | None =
     vecs = np.zeros((nev, problem.ndof)) if vectors else None
     st = _check(_lib.klsa_modal(problem.h, o.h, int(nev), float(shift), _ptr(vals), _ptr(vecs)))
     return st, vals, vecs
+
+
+class Dynamic:
+    """gsDynamicSolvers time integrators on the device: ``method`` is "Newmark", "Bathe", "Wilson",
+    "ExplicitEuler", "ImplicitEuler" or "RK4"; ``nonlinear`` is the reference's _NL flag.  Vectors
+    are in the public free-dof order."""
+
+    def __init__(self, problem: Problem, method: str, nonlinear: bool = True, options: dict | None = None):
+        self.problem = problem
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_dynamic_create(problem.h, method.encode(), 1 if nonlinear else 0, self.opts.h,
+                                        ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_dynamic_destroy(self.h)
+            self.h = None
+
+    def setLoadTable(self, t, f):
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        _check(_lib.klsa_dynamic_set_load_table(self.h, _ptr(t), _ptr(f), len(t)))
+
+    def _set(self, U=None, V=None, A=None):
+        c = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (U, V, A)]
+        _check(_lib.klsa_dynamic_set_state(self.h, *(_ptr(x) for x in c)))
+
+    def setU(self, U):
+        self._set(U=U)
+
+    def setV(self, V):
+        self._set(V=V)
+
+    def setA(self, A):
+        self._set(A=A)
+
+    def _get(self, which):
+        out = [None, None, None]
+        out[which] = np.zeros(self.problem.ndof)
+        _check(_lib.klsa_dynamic_state(self.h, *(_ptr(x) for x in out)))
+        return out[which]
+
+    def solutionU(self):
+        return self._get(0)
+
+    def solutionV(self):
+        return self._get(1)
+
+    def solutionA(self):
+        return self._get(2)
+
+    def step(self, dt: float | None = None):
+        return _check(_lib.klsa_dynamic_step(self.h, float(dt) if dt is not None else 0.0))
+
+    def setTime(self, t):
+        _check(_lib.klsa_dynamic_set_time(self.h, float(t)))
+
+    def time(self):
+        return float(_lib.klsa_dynamic_time(self.h))
+
+    def iterations(self):
+        return int(_lib.klsa_dynamic_iterations(self.h))
 
 
 class MLP:

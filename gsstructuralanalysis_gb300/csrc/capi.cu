@@ -6,6 +6,7 @@
 
 #include "../../include/klshell_gb300.h"
 #include "batch.h"
+#include "dynamics.h"
 #include "eigen.h"
 #include "linalg.h"
 #include "mlp.h"
@@ -40,6 +41,10 @@ struct klsa_alm {
     klsa_problem* prob;
     std::unique_ptr<ALMGPU> A;
     DevBuf<double> v;
+};
+struct klsa_dynamic {
+    klsa_problem* prob;
+    std::unique_ptr<DynamicGPU> D;
 };
 struct klsa_mlp {
     std::unique_ptr<MLP> net;
@@ -704,6 +709,77 @@ int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shif
     if (!prob || !values || nev < 1) return KLSA_INVALID_ARGUMENT;
     return guarded([&] { return modal_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, values, vectors); });
 }
+
+// ---- time integrators ----------------------------------------------------------------------
+int klsa_dynamic_create(klsa_problem* prob, const char* method, int nonlinear, const klsa_options* opt,
+                        klsa_dynamic** out) {
+    if (!prob || !method || !out) return KLSA_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guarded([&] {
+        DynamicGPU::Method m;
+        std::string s(method);
+        if (s == "Newmark") m = DynamicGPU::Newmark;
+        else if (s == "Bathe") m = DynamicGPU::Bathe;
+        else if (s == "Wilson") m = DynamicGPU::Wilson;
+        else if (s == "ExplicitEuler") m = DynamicGPU::ExplicitEuler;
+        else if (s == "ImplicitEuler") m = DynamicGPU::ImplicitEuler;
+        else if (s == "RK4") m = DynamicGPU::RK4;
+        else {
+            g_err = "unknown time integrator " + s;
+            return KLSA_INVALID_ARGUMENT;
+        }
+        std::unique_ptr<klsa_dynamic> h(new klsa_dynamic);
+        h->prob = prob;
+        h->D.reset(new DynamicGPU(*prob->P, m, nonlinear != 0, opt ? opt->o : Options()));
+        *out = h.release();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_dynamic_destroy(klsa_dynamic* d) {
+    return guarded([&] {
+        delete d;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_dynamic_set_load_table(klsa_dynamic* d, const double* t, const double* f, int n) {
+    if (!d || n < 0 || (n > 0 && (!t || !f))) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        d->D->set_load_table(std::vector<double>(t, t + n), std::vector<double>(f, f + n));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_dynamic_set_state(klsa_dynamic* d, const double* U, const double* V, const double* A) {
+    if (!d) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *d->prob->P;
+        if (U) P.upload_pub(U, d->D->U());
+        if (V) P.upload_pub(V, d->D->V());
+        if (A) P.upload_pub(A, d->D->A());
+        KL_CUDA(cudaStreamSynchronize(P.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_dynamic_state(klsa_dynamic* d, double* U, double* V, double* A) {
+    if (!d) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *d->prob->P;
+        if (U) P.download_pub(d->D->U(), U);
+        if (V) P.download_pub(d->D->V(), V);
+        if (A) P.download_pub(d->D->A(), A);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_dynamic_step(klsa_dynamic* d, double dt) {
+    if (!d) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return d->D->step(dt > 0.0 ? dt : d->D->default_dt()); });
+}
+int klsa_dynamic_set_time(klsa_dynamic* d, double t) {
+    if (!d) return KLSA_INVALID_ARGUMENT;
+    d->D->set_time(t);
+    return KLSA_SUCCESS;
+}
+double klsa_dynamic_time(klsa_dynamic* d) { return d ? d->D->time() : 0.0; }
+int klsa_dynamic_iterations(klsa_dynamic* d) { return d ? d->D->iterations() : -1; }
 
 }  // extern "C"
 

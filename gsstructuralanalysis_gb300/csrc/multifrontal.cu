@@ -1031,6 +1031,7 @@ MultifrontalT<T>::~MultifrontalT() {
 template <class T>
 void MultifrontalT<T>::factorize_async(const T* d_vals) {
     if (!d_vals && nnz_ > 0) throw std::logic_error("multifrontal: no matrix values");
+    ++generation_;
     replay(fact_graph_, d_vals, nullptr, [&] { factorize_launches(d_vals); });
 }
 
@@ -1175,7 +1176,10 @@ void MultifrontalT<T>::solve_impl(const T* d_b, T* d_x) {
 }
 
 template <class T>
-void MultifrontalT<T>::enqueue_factorize(const T* d_vals) { factorize_launches(d_vals); }
+void MultifrontalT<T>::enqueue_factorize(const T* d_vals) {
+    ++generation_;
+    factorize_launches(d_vals);
+}
 
 template <class T>
 void MultifrontalT<T>::enqueue_solve(const T* d_b, T* d_x) { solve_impl<1>(d_b, d_x); }

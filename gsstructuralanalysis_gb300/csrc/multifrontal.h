@@ -53,6 +53,8 @@ public:
     void enqueue_solve(const T* d_b, T* d_x);
 
     int n() const { return n_; }
+    // number of factorisations enqueued so far (identifies the factor the fronts hold)
+    uint64_t generation() const { return generation_; }
     double flops() const { return flops_; }
     int64_t front_bytes() const { return (int64_t)pool_.size() * 4; }
     // algorithmic bytes / flops of one factorisation per kernel kind (0 diag, 1 panel, 2 update),
@@ -63,6 +65,7 @@ public:
     const std::vector<int>& level_nodes(int lvl) const { return level_nodes_[lvl]; }
 
 private:
+    uint64_t generation_ = 0;
     struct GraphSlot {
         cudaGraphExec_t exec = nullptr;
         const void* key0 = nullptr;

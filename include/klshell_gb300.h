@@ -206,6 +206,38 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
                double* vectors);
 
+/* ---- time integrators (gsDynamicSolvers/gsDynamicBase.h:185-260 and the integrators) ----
+ * method: "Newmark" (gsDynamicNewmark.hpp), "Bathe" (gsDynamicBathe.hpp), "Wilson"
+ * (gsDynamicWilson.hpp), "ExplicitEuler" (gsDynamicExplicitEuler.hpp), "ImplicitEuler"
+ * (gsDynamicImplicitEuler.hpp), "RK4" (gsDynamicRK4.hpp).  nonlinear selects the reference's
+ * _NL template flag: 1 = tangent K(U) and residual R(U,t) = f(t) F - Fint(U) (the Mass,
+ * Damping, Jacobian, TResidual constructor), 0 = constant stiffness K_L and force f(t) F (the
+ * Mass, Damping, Stiffness, TForce constructor).  M is the consistent mass.  Options: "DT" (1e-2),
+ * "MaxIter" (100), "TolF" (1e-3), "TolU" (1e-6), "Quasi" (0), "QuasiIterations" (1), "alpha",
+ * "delta", "gamma" (Newmark 0.25/0.5, Bathe 0.25/0.5/0.5, Wilson 0.25/0.5/1.4), "Solver"
+ * (a direct solver: SimplicialLDLT), plus, without a reference key, "DampingMass" and
+ * "DampingStiffness" (Rayleigh damping C = cM M + cK K_L; the reference takes C from a Damping_t
+ * callback, zero in its tutorials) and "FrontPrecision" (64, or 32 with FP64 refinement).
+ * ImplicitEuler solves its block system exactly where the reference runs GMRES on it. */
+typedef struct klsa_dynamic klsa_dynamic;
+int klsa_dynamic_create(klsa_problem* prob, const char* method, int nonlinear, const klsa_options* opt,
+                        klsa_dynamic** out);
+int klsa_dynamic_destroy(klsa_dynamic* d);
+/* Load factor f(t): piecewise linear through (t[i], f[i]), t non-decreasing, constant beyond the
+ * ends; n = 0 restores f = 1 (the TForce_t / TResidual_t callbacks of the reference). */
+int klsa_dynamic_set_load_table(klsa_dynamic* d, const double* t, const double* f, int n);
+/* setU / setV / setA and solutionU / solutionV / solutionA (public free-dof order; a NULL
+ * pointer leaves that field unchanged / unread). */
+int klsa_dynamic_set_state(klsa_dynamic* d, const double* U, const double* V, const double* A);
+int klsa_dynamic_state(klsa_dynamic* d, double* U, double* V, double* A);
+/* step(dt) (gsDynamicBase.h:196-208), dt <= 0: the "DT" option.  Returns the gsStatus of the step;
+ * the time advances by dt in every case. */
+int klsa_dynamic_step(klsa_dynamic* d, double dt);
+int klsa_dynamic_set_time(klsa_dynamic* d, double t);
+double klsa_dynamic_time(klsa_dynamic* d);
+/* Newton iterations of the last step (1 for the explicit and linear integrators) */
+int klsa_dynamic_iterations(klsa_dynamic* d);
+
 /* ---- batched Newton solves of many patches (no counterpart in the reference) ------------
  * Equivalent to one gsStaticNewton::solve() per instance (gsStaticNewton.hpp:101-193), each
  * with its own assembler; here all instances share every launch: a persistent assembly kernel
