@@ -1,0 +1,107 @@
+"""XML problem input (gsstructuralanalysis_gb300/xmlio.py) on CPU: files in the reference's
+gsFileData layout, elevated and refined as the reference's XML solvers do, give exactly the
+problems built directly in gsstructuralanalysis_gb300.problems; unsupported content is rejected."""
+import os
+
+import numpy as np
+import pytest
+
+from gsstructuralanalysis_gb300 import problems as P
+from gsstructuralanalysis_gb300 import xmlio as X
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "xml")
+
+
+def test_plate_elevated_and_refined_matches_direct_construction():
+    r = X.read(os.path.join(GOLD, "plate_clamped.xml"), elevate=1, refine=3)
+    q = r.problem
+    ref = P.flat_plate(m=8, p=2, E=1e7, t=0.01, rho=1.0, bc="clamped", pressure=1.0)
+    assert (q.p, q.n1, q.n2) == (ref.p, ref.n1, ref.n2)
+    np.testing.assert_allclose(q.knots1, ref.knots1, atol=1e-15)
+    np.testing.assert_allclose(q.ctrl, ref.ctrl, atol=1e-14)
+    assert np.array_equal(q.fixed, ref.fixed)
+    np.testing.assert_array_equal(q.surface_load, ref.surface_load)
+    assert (q.E, q.nu, q.t, q.rho) == (ref.E, ref.nu, ref.t, ref.rho)
+    assert r.options[91] == {"tol": 1e-10, "maxIt": 30, "Relaxation": 1.0, "Solver": "SimplicialLDLT"}
+
+
+def test_roof_refined_matches_direct_construction():
+    r = X.read(os.path.join(GOLD, "roof_point_load.xml"), refine=4)
+    q = r.problem
+    ref = P.cylindrical_panel(m=16, p=2, load=1.0)
+    assert (q.p, q.n1, q.n2) == (2, 18, 18)
+    np.testing.assert_allclose(q.ctrl, ref.ctrl, atol=1e-14)
+    assert np.array_equal(q.fixed, ref.fixed)
+    np.testing.assert_array_equal(q.point_loads, ref.point_loads)
+    np.testing.assert_array_equal(r.reference_points, [[0.5], [0.5]])
+    assert list(r.reference_patches) == [0]
+    assert r.options[93]["Length"] == 5e-3 and r.options[93]["AdaptiveLength"] is False
+    assert r.options[93]["BifurcationMethod"] == -1
+
+
+def test_roof_assembles_like_direct_construction(oracle_mod):
+    q = X.read(os.path.join(GOLD, "roof_point_load.xml"), refine=2).problem
+    ref = P.cylindrical_panel(m=4, p=2, load=1.0)
+    a, b = oracle_mod.OracleAssembler(q), oracle_mod.OracleAssembler(ref)
+    x = np.random.default_rng(0).normal(size=a.nfree) * 1e-3
+    Ka, Kb = a.jacobian(x), b.jacobian(x)
+    assert abs(Ka - Kb).max() <= 1e-12 * abs(Kb).max()
+    np.testing.assert_allclose(a.force(), b.force(), atol=1e-15)
+
+
+def test_degree_elevation_reproduces_the_surface():
+    """Elevation and refinement keep the surface: points evaluated on the coarse and the fine
+    nets agree."""
+    r0 = X.read(os.path.join(GOLD, "roof_point_load.xml")).problem
+    r1 = X.read(os.path.join(GOLD, "roof_point_load.xml"), elevate=2, refine=1).problem
+    assert r1.p == 4
+    uv = np.random.default_rng(1).random((20, 2))
+
+    def ev(q):
+        B1 = P.bspline_basis_matrix(q.knots1, q.p, uv[:, 0])
+        B2 = P.bspline_basis_matrix(q.knots2, q.p, uv[:, 1])
+        C = q.ctrl.reshape(q.n2, q.n1, 3)
+        return np.einsum("ki,kj,jic->kc", B1, B2, C)
+    np.testing.assert_allclose(ev(r1), ev(r0), atol=1e-13)
+
+
+def test_expressions():
+    assert X.eval_constant("2*2*(3+1)*(1+0.5)") == 24.0
+    assert X.eval_constant("2^3") == 8.0
+    assert X.eval_constant("-1e-2") == -0.01
+    with pytest.raises(NotImplementedError):
+        X.eval_constant("x*2")
+    with pytest.raises(NotImplementedError):
+        X.eval_constant("__import__('os')")
+
+
+def _edit(tmp_path, name, old, new):
+    src = open(os.path.join(GOLD, name)).read()
+    assert old in src
+    f = tmp_path / name
+    f.write_text(src.replace(old, new))
+    return str(f)
+
+
+def test_neumann_edge_load_and_corner_values(tmp_path):
+    f = _edit(tmp_path, "roof_point_load.xml", '<bc type="Dirichlet" function="0" unknown="0" component="-1" name="straight">\n  </bc>',
+              '<Function type="FunctionExpr" dim="3" index="1"><c>0</c><c>0</c><c>-5</c></Function>\n'
+              '  <bc type="Dirichlet" function="0" unknown="0" component="-1" name="straight">\n  </bc>\n'
+              '  <bc type="Neumann" function="1" unknown="0">\n    0 2\n  </bc>\n'
+              '  <cv patch="0" corner="1" component="0">0.0</cv>')
+    q = X.read(f, refine=1).problem
+    np.testing.assert_array_equal(q.edge_loads, [[1, 0, 0, -5]])
+    assert q.fixed.reshape(3, -1)[0, 0]
+
+
+@pytest.mark.parametrize("old,new,what", [
+    ('type="Linear3"', 'type="NeoHookean3"', "material"),
+    ('<Function type="FunctionExpr" dim="3" index="0">0</Function>\n  <bc',
+     '<Function type="FunctionExpr" dim="3" index="0">0.1</Function>\n  <bc', "inhomogeneous"),
+    ('<patches type="id_range">5 5</patches>', '<patches type="id_range">5 6</patches>', "patches"),
+    ('<Matrix rows="2" cols="1" id="30" tag="Loads">', '<Function type="FunctionExpr" id="22" tag="Loads" dim="3">1</Function>\n<Matrix rows="2" cols="1" id="30" tag="Loads">', "pressure"),
+])
+def test_unsupported_content_is_rejected(tmp_path, old, new, what):
+    f = _edit(tmp_path, "roof_point_load.xml", old, new)
+    with pytest.raises(NotImplementedError, match=what):
+        X.read(f)
