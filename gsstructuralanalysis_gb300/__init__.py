@@ -81,6 +81,18 @@ SIGNATURES = {
     "klsa_alm_get_length": (_c_dbl, [_c_vp]),
     "klsa_alm_set_solution": (_c_int, [_c_vp, _c_vp, _c_dbl]),
     "klsa_alm_set_solution_step": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_alm_set_previous": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_alm_distance": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
+    "klsa_apalm_create": (_c_int, [_c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
+    "klsa_apalm_destroy": (_c_int, [_c_vp]),
+    "klsa_apalm_initialize": (_c_int, [_c_vp]),
+    "klsa_apalm_add_start": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_dbl]),
+    "klsa_apalm_serial_solve": (_c_int, [_c_vp, _c_int]),
+    "klsa_apalm_parallel_solve": (_c_int, [_c_vp]),
+    "klsa_apalm_solve": (_c_int, [_c_vp, _c_int]),
+    "klsa_apalm_branches": (_c_int, [_c_vp]),
+    "klsa_apalm_solutions": (_c_int, [_c_vp, _c_int]),
+    "klsa_apalm_solution": (_c_int, [_c_vp, _c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_alm_set_initial_guess": (_c_int, [_c_vp, _c_vp, _c_dbl]),
     "klsa_alm_solution": (_c_int, [_c_vp, _c_vp, _c_vp]),
     "klsa_alm_info": (_c_int, [_c_vp, _c_vp]),
@@ -462,6 +474,16 @@ class _ALM:
         DU = np.ascontiguousarray(DU, dtype=np.float64)
         _check(_lib.klsa_alm_set_solution_step(self.h, _ptr(DU), float(DL)))
 
+    def setPrevious(self, Uprev, Lprev):
+        Uprev = np.ascontiguousarray(Uprev, dtype=np.float64)
+        _check(_lib.klsa_alm_set_previous(self.h, _ptr(Uprev), float(Lprev)))
+
+    def distance(self, DU, DL):
+        DU = np.ascontiguousarray(DU, dtype=np.float64)
+        out = ctypes.c_double()
+        _check(_lib.klsa_alm_distance(self.h, _ptr(DU), float(DL), ctypes.byref(out)))
+        return out.value
+
     def setInitialGuess(self, U, L):
         U = np.ascontiguousarray(U, dtype=np.float64)
         _check(_lib.klsa_alm_set_initial_guess(self.h, _ptr(U), float(L)))
@@ -528,6 +550,64 @@ def modal(problem: Problem, nev: int, shift: float = 0.0, options: dict | None =
     vecs = np.zeros((nev, problem.ndof)) if vectors else None
     st = _check(_lib.klsa_modal(problem.h, o.h, int(nev), float(shift), _ptr(vals), _ptr(vecs)))
     return st, vals, vecs
+
+
+class APALM:
+    """gsAPALM over an arc-length object (ALMCrisfield or ALMRiks): serialSolve / parallelSolve /
+    solve and the flat solutions, times and levels per branch (public free-dof order)."""
+
+    def __init__(self, alm: "_ALM", options: dict | None = None):
+        self.alm = alm
+        self.opts = Options(options)
+        h = _c_vp()
+        _check(_lib.klsa_apalm_create(alm.h, self.opts.h, ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.klsa_apalm_destroy(self.h)
+            self.h = None
+
+    def initialize(self):
+        _check(_lib.klsa_apalm_initialize(self.h))
+
+    def addStart(self, U, L, dL):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(_lib.klsa_apalm_add_start(self.h, _ptr(U), float(L), float(dL)))
+
+    def serialSolve(self, nsteps=10):
+        _check(_lib.klsa_apalm_serial_solve(self.h, int(nsteps)))
+
+    def parallelSolve(self):
+        _check(_lib.klsa_apalm_parallel_solve(self.h))
+
+    def solve(self, nsteps=10):
+        _check(_lib.klsa_apalm_solve(self.h, int(nsteps)))
+
+    def nBranches(self):
+        return _check(_lib.klsa_apalm_branches(self.h))
+
+    def _branch(self, branch, want_u=True):
+        n = _check(_lib.klsa_apalm_solutions(self.h, int(branch)))
+        U = np.zeros((n, self.alm.problem.ndof)) if want_u else None
+        L, t = np.zeros(n), np.zeros(n)
+        lv = np.zeros(n, dtype=np.int32)
+        for k in range(n):
+            Lk, tk, lk = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+            _check(_lib.klsa_apalm_solution(self.h, int(branch), k, _ptr(U[k]) if want_u else None,
+                                            ctypes.byref(Lk), ctypes.byref(tk), ctypes.byref(lk)))
+            L[k], t[k], lv[k] = Lk.value, tk.value, lk.value
+        return U, L, t, lv
+
+    def getFlatSolutions(self, branch=0):
+        U, L, _, _ = self._branch(branch)
+        return list(zip(U, L))
+
+    def getFlatTimes(self, branch=0):
+        return self._branch(branch, want_u=False)[2]
+
+    def getFlatLevels(self, branch=0):
+        return self._branch(branch, want_u=False)[3]
 
 
 class Dynamic:

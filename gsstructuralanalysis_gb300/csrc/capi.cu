@@ -5,6 +5,7 @@
 #include <string>
 
 #include "../../include/klshell_gb300.h"
+#include "apalm.h"
 #include "batch.h"
 #include "dynamics.h"
 #include "eigen.h"
@@ -41,6 +42,10 @@ struct klsa_alm {
     klsa_problem* prob;
     std::unique_ptr<ALMGPU> A;
     DevBuf<double> v;
+};
+struct klsa_apalm {
+    klsa_alm* alm;
+    std::unique_ptr<APALM> A;
 };
 struct klsa_dynamic {
     klsa_problem* prob;
@@ -405,6 +410,27 @@ int klsa_alm_set_solution(klsa_alm* a, const double* U, double L) {
         return KLSA_SUCCESS;
     });
 }
+int klsa_alm_set_previous(klsa_alm* a, const double* Uprev, double Lprev) {
+    if (!a || !Uprev) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->prob->x, P.nfree);
+        P.upload_pub(Uprev, a->prob->x.get());
+        a->A->set_previous(a->prob->x.get(), Lprev);
+        KL_CUDA(cudaStreamSynchronize(P.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_alm_distance(klsa_alm* a, const double* DU, double DL, double* out) {
+    if (!a || !DU || !out) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *a->prob->P;
+        ensure(a->prob->x, P.nfree);
+        P.upload_pub(DU, a->prob->x.get());
+        *out = a->A->distance(a->prob->x.get(), DL);
+        return KLSA_SUCCESS;
+    });
+}
 int klsa_alm_set_solution_step(klsa_alm* a, const double* DU, double DL) {
     if (!a || !DU) return KLSA_INVALID_ARGUMENT;
     return guarded([&] {
@@ -708,6 +734,81 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values, double* vectors) {
     if (!prob || !values || nev < 1) return KLSA_INVALID_ARGUMENT;
     return guarded([&] { return modal_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, values, vectors); });
+}
+
+// ---- adaptive parallel arc-length method -----------------------------------------------------
+int klsa_apalm_create(klsa_alm* alm, const klsa_options* opt, klsa_apalm** out) {
+    if (!alm || !out) return KLSA_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guarded([&] {
+        std::unique_ptr<klsa_apalm> h(new klsa_apalm);
+        h->alm = alm;
+        h->A.reset(new APALM(*alm->A, opt ? opt->o : Options()));
+        *out = h.release();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_destroy(klsa_apalm* ap) {
+    return guarded([&] {
+        delete ap;
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_initialize(klsa_apalm* ap) {
+    if (!ap) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ap->A->initialize();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_add_start(klsa_apalm* ap, const double* U, double L, double dL) {
+    if (!ap || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *ap->alm->prob->P;
+        ensure(ap->alm->prob->x, P.nfree);
+        P.upload_pub(U, ap->alm->prob->x.get());
+        ap->A->add_start(ap->alm->prob->x.get(), L, dL);
+        KL_CUDA(cudaStreamSynchronize(P.stream));
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_serial_solve(klsa_apalm* ap, int nsteps) {
+    if (!ap) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ap->A->serial_solve(nsteps);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_parallel_solve(klsa_apalm* ap) {
+    if (!ap) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ap->A->parallel_solve();
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_solve(klsa_apalm* ap, int nsteps) {
+    if (!ap) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ap->A->solve(nsteps);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_apalm_branches(klsa_apalm* ap) { return ap ? ap->A->branches() : KLSA_INVALID_ARGUMENT; }
+int klsa_apalm_solutions(klsa_apalm* ap, int branch) {
+    if (!ap || branch < 0 || branch >= ap->A->branches()) return KLSA_INVALID_ARGUMENT;
+    return ap->A->solutions(branch);
+}
+int klsa_apalm_solution(klsa_apalm* ap, int branch, int k, double* U, double* L, double* time, int* level) {
+    if (!ap || branch < 0 || branch >= ap->A->branches() || k < 0 || k >= ap->A->solutions(branch))
+        return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        const APSolution& s = ap->A->solution(branch, k);
+        if (U) ap->alm->prob->P->download_pub(s.U->get(), U);
+        if (L) *L = s.L;
+        if (time) *time = ap->A->time(branch, k);
+        if (level) *level = ap->A->level(branch, k);
+        return KLSA_SUCCESS;
+    });
 }
 
 // ---- time integrators ----------------------------------------------------------------------

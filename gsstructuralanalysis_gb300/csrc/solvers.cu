@@ -257,6 +257,21 @@ void ALMGPU::set_solution_step(const double* d_DU, double DL) {
     DLold_ = DL;
 }
 
+void ALMGPU::set_previous(const double* d_Uprev, double Lprev) {
+    KL_CUDA(cudaMemcpyAsync(Uprev_.get(), d_Uprev, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
+    Lprev_ = Lprev;
+    vec::lincomb(1.0, U_.get(), -1.0, Uprev_.get(), DUold_.get(), n_, P_.stream);
+    DLold_ = L_ - Lprev_;
+}
+
+double ALMGPU::distance(const double* d_DU, double DL) {
+    double uu = 0.0;
+    vec::multidot(1, &d_DU, &d_DU, n_, &uu, P_.stream);
+    if (method_ == Crisfield) return std::sqrt(uu + phi_ * phi_ * FF_ * DL * DL);
+    if (method_ == Riks) return std::sqrt(phi_ * uu + (1.0 - phi_) * DL * DL);
+    throw std::invalid_argument("distance: not defined for this arc-length method");
+}
+
 void ALMGPU::set_initial_guess(const double* d_U, double L) {
     KL_CUDA(cudaMemcpyAsync(Uguess_.get(), d_U, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
     Lguess_ = L;

@@ -94,6 +94,13 @@ public:
     void set_solution(const double* d_U, double L);
     void set_solution_step(const double* d_DU, double DL);
     void set_initial_guess(const double* d_U, double L);
+    // gsALMBase::setPrevious (gsALMBase.h:185-191): Uprev, Lprev and DUold = U - Uprev, DLold = L - Lprev
+    void set_previous(const double* d_Uprev, double Lprev);
+    // distance of a path increment in the method's norm: gsALMCrisfield.h:79-83
+    // sqrt(DU.DU + phi^2 F.F DL^2), gsALMRiks.h:81-84 sqrt(phi |DU|^2 + (1 - phi) DL^2); the
+    // other methods have none (gsALMBase.h:211-214) and throw
+    double distance(const double* d_DU, double DL);
+    Method method() const { return method_; }
     const double* U() const { return U_.get(); }
     double L() const { return L_; }
     const double* Uprev() const { return Uprev_.get(); }
@@ -113,6 +120,7 @@ public:
     int max_iter() const { return maxIt_; }
     void set_max_iter(int it) { maxIt_ = it; }
     Problem& problem() { return P_; }
+    bool quasi() const { return quasi_; }
     // per-step work counters
     int n_jac = 0, n_res = 0, n_solve = 0;
 

@@ -159,6 +159,9 @@ int klsa_alm_reduce_length(klsa_alm* a, double factor);   /* reduceLength */
 double klsa_alm_get_length(klsa_alm* a);
 int klsa_alm_set_solution(klsa_alm* a, const double* U, double L);      /* setSolution */
 int klsa_alm_set_solution_step(klsa_alm* a, const double* DU, double DL); /* setSolutionStep */
+int klsa_alm_set_previous(klsa_alm* a, const double* Uprev, double Lprev);  /* setPrevious (gsALMBase.h:185-191) */
+/* distance(DeltaU, DeltaL) of Crisfield (gsALMCrisfield.h:79-83) and Riks (gsALMRiks.h:81-84) */
+int klsa_alm_distance(klsa_alm* a, const double* DU, double DL, double* out);
 int klsa_alm_set_initial_guess(klsa_alm* a, const double* U, double L);  /* setInitialGuess */
 int klsa_alm_solution(klsa_alm* a, double* U, double* L);  /* solutionU / solutionL */
 /* out: [iterations, residueF, residueU, phi, converged, Lprev, DeltaL_old] */
@@ -205,6 +208,24 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 /* Modal (gsModalSolver.h:46-51): eigenpairs of K v = omega^2 M v about ``shift``. */
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
                double* vectors);
+
+/* ---- adaptive parallel arc-length method (gsALMSolvers/gsAPALM.hpp, gsAPALMData.hpp) -----
+ * Over an arc-length object of method Crisfield or Riks (the methods with a distance).  The jobs
+ * run in queue order on the device solver: the schedule of a one-process reference run.  Options:
+ * "MaxIt" (1000), "SubIntervals" (2), "SingularPoint" (0), "BranchLengthMultiplier" (1),
+ * "BifLengthMultiplier" (0.1), and the data options "MaxLevel" (5) and "Tolerance" (0.1). */
+typedef struct klsa_apalm klsa_apalm;
+int klsa_apalm_create(klsa_alm* alm, const klsa_options* opt, klsa_apalm** out);
+int klsa_apalm_destroy(klsa_apalm* ap);
+int klsa_apalm_initialize(klsa_apalm* ap);                           /* initialize(): start at (0, 0) */
+int klsa_apalm_add_start(klsa_apalm* ap, const double* U, double L, double dL);   /* _initStart */
+int klsa_apalm_serial_solve(klsa_apalm* ap, int nsteps);             /* serialSolve(Nsteps) */
+int klsa_apalm_parallel_solve(klsa_apalm* ap);                       /* parallelSolve() */
+int klsa_apalm_solve(klsa_apalm* ap, int nsteps);                    /* solve(Nsteps) */
+int klsa_apalm_branches(klsa_apalm* ap);
+int klsa_apalm_solutions(klsa_apalm* ap, int branch);                /* points of getFlatSolutions(branch) */
+/* point k of branch b: U (public order, may be NULL), L, curve time (getFlatTimes), level (getFlatLevels) */
+int klsa_apalm_solution(klsa_apalm* ap, int branch, int k, double* U, double* L, double* time, int* level);
 
 /* ---- time integrators (gsDynamicSolvers/gsDynamicBase.h:185-260 and the integrators) ----
  * method: "Newmark" (gsDynamicNewmark.hpp), "Bathe" (gsDynamicBathe.hpp), "Wilson"

@@ -531,6 +531,15 @@ class _ALMBase:
     def set_initial_guess(self, Ug, Lg):
         self.Uguess = np.asarray(Ug, dtype=np.float64).copy(); self.Lguess = float(Lg)
 
+    def set_previous(self, Uprev, Lprev):
+        """gsALMBase::setPrevious (gsALMBase.h:185-191)."""
+        self.Uprev = np.asarray(Uprev, dtype=np.float64).copy(); self.Lprev = float(Lprev)
+        self.DeltaUold = self.U - self.Uprev
+        self.DeltaLold = self.L - self.Lprev
+
+    def distance(self, DU, DL):
+        raise NotImplementedError("gsALMBase::distance has no implementation (gsALMBase.h:211-214)")
+
     def reduce_length(self, fac):
         self.arcLength *= fac
         return self.arcLength
@@ -629,6 +638,10 @@ class _ALMBase:
 
 class ALMCrisfield(_ALMBase):
     """gsALMCrisfield restated (gsALMCrisfield.hpp:22-427); AngleMethod 0 (Step) and 1 (Iteration)."""
+
+    def distance(self, DU, DL):
+        """gsALMCrisfield.h:79-83."""
+        return float(np.sqrt(float(DU @ DU) + self.phi ** 2 * float(self.F @ self.F) * DL ** 2))
 
     def apply_options(self):
         super().apply_options()
@@ -785,6 +798,10 @@ class ALMCrisfield(_ALMBase):
 
 class ALMRiks(_ALMBase):
     """gsALMRiks restated (gsALMRiks.hpp:40-170)."""
+
+    def distance(self, DU, DL):
+        """gsALMRiks.h:81-84."""
+        return float(np.sqrt(self.phi * float(DU @ DU) + (1.0 - self.phi) * DL ** 2))
 
     def initiate_step(self):
         self.DeltaU = np.zeros(self.numDof); self.deltaU = np.zeros(self.numDof)
