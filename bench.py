@@ -826,7 +826,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
-    ap.add_argument("--train-paths", type=int, default=16)
+    ap.add_argument("--train-paths", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
