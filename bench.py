@@ -134,6 +134,13 @@ class ClockSampler:
         return out
 
 
+def alm_options(mode, frozen):
+    """Crisfield options of an arm: the reference's for the plain predictor; the guess arms add
+    FrozenIterations (the first corrector iterations after a placed guess reuse the held
+    factorisation)."""
+    return dict(ALM_OPTS, FrozenIterations=int(frozen)) if (mode != "plain" and frozen) else dict(ALM_OPTS)
+
+
 def step_with_retry(alm, G):
     """One accepted point; on non-convergence halve the length and retry (benchmark_Roof.cpp:420-431)."""
     for _ in range(MAX_RETRIES):
@@ -175,16 +182,24 @@ def run_ours(args):
     gp = G.Problem(prob)
     stats = gp.stats()
 
-    def run_path(mode, timed=True):
-        alm = G.ALMCrisfield(gp, ALM_OPTS)
+    def make_arm(mode, frozen):
+        """A fresh Crisfield path and its step function.  The guess modes place the predicted point
+        and, with frozen > 0, start the corrector on the factorisation the solver already holds
+        (FrozenIterations); the plain mode is the reference's tangent predictor."""
+        alm = G.ALMCrisfield(gp, alm_options(mode, frozen))
         alm.initialize()
         pred = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
+        gmi = frozen + 4 if (frozen and pred is not None) else 6
 
         def one():
             if pred is None:
                 return step_with_retry(alm, G)
-            st, _ = pred.step(alm, guess_max_iter=6)
+            st, _ = pred.step(alm, guess_max_iter=gmi)
             return st == G.SUCCESS or step_with_retry(alm, G)
+        return alm, pred, one
+
+    def run_path(mode, frozen=args.frozen_it):
+        alm, pred, one = make_arm(mode, frozen)
 
         for _ in range(args.warmup):
             one()
@@ -224,27 +239,23 @@ def run_ours(args):
         return
     compare = {}
     if mode == "learned":
-        for other in ("plain", "extrapolation"):
-            r = run_path(other)
-            compare[other] = {"points_per_s": world * r["pts"] / (reduce_max(r["ms"], world) / 1e3),
-                              "jacobians_per_point": r["jac_per_point"]}
-        compare["learned"] = {"points_per_s": value, "jacobians_per_point": main["jac_per_point"]}
+        arms = [("plain", "plain", 0), ("extrapolation", "extrapolation", args.frozen_it)]
+        if args.frozen_it:
+            arms.append(("learned_full_newton", "learned", 0))
+        for name, m, fz in arms:
+            r = run_path(m, fz)
+            compare[name] = {"points_per_s": world * r["pts"] / (reduce_max(r["ms"], world) / 1e3),
+                             "jacobians_per_point": r["jac_per_point"], "frozen_iterations": fz}
+        compare["learned"] = {"points_per_s": value, "jacobians_per_point": main["jac_per_point"],
+                              "frozen_iterations": args.frozen_it}
         compare["learned_over_plain"] = value / compare["plain"]["points_per_s"]
         compare["final_load_factor_plain_vs_learned"] = None
 
     # e2e: the same steps again through the C-ABI with host vectors in and out every step
-    alm2 = G.ALMCrisfield(gp, ALM_OPTS)
-    alm2.initialize()
-    pred2 = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
+    alm2, pred2, one2 = make_arm(mode, args.frozen_it)
     U = np.zeros(gp.ndof)
     L = 0.0
     pin_bytes = 8 * gp.ndof
-
-    def one2():
-        if pred2 is None:
-            return step_with_retry(alm2, G)
-        st, _ = pred2.step(alm2, guess_max_iter=6)
-        return st == G.SUCCESS or step_with_retry(alm2, G)
 
     for _ in range(args.warmup):
         alm2.setSolution(U, L)
@@ -265,7 +276,7 @@ def run_ours(args):
     if compare:
         compare["final_load_factor_plain_vs_learned"] = [float(L), float(L_end)]
 
-    prof = profile_phases(G, gp, args)
+    prof = profile_phases(G, gp, args, lambda: make_arm(mode, args.frozen_it)[::2])
     roof = roofline(prof, stats, args)
     info = alm.info()
     cpu = None
@@ -296,17 +307,17 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def profile_phases(G, gp, args, nsteps=None):
+def profile_phases(G, gp, args, make_arm, nsteps=None):
+    """Per-phase device times of the measured arm (serialised launches with CUDA events)."""
     nsteps = nsteps or min(args.steps, 20)
-    alm = G.ALMCrisfield(gp, ALM_OPTS)
-    alm.initialize()
+    alm, one = make_arm()
     for _ in range(args.warmup):
-        step_with_retry(alm, G)
+        one()
     gp.sync()
     G.profile_reset()
     G.profile_enable(True)
     for _ in range(nsteps):
-        step_with_retry(alm, G)
+        one()
     gp.sync()
     G.profile_enable(False)
     ph = G.profile_read()
@@ -827,6 +838,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
     ap.add_argument("--train-paths", type=int, default=32)
+    ap.add_argument("--frozen-it", type=int, default=1,
+                    help="corrector iterations on the held factorisation after a placed guess (0: full Newton)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")

@@ -167,6 +167,11 @@ int MFSolver::factor_current(bool f64_for_refine) {
     return P_.solver().read_status();
 }
 
+uint64_t MFSolver::generation() const {
+    if (fp64_) return P_.mf64 ? P_.mf64->generation() : 0;
+    return P_.mf ? P_.mf->generation() : 0;
+}
+
 int MFSolver::compute_tangent() {
     cudaEvent_t ev = g_timer.begin(P_.stream);
     if (refine_ > 0 || fp64_) P_.tangent_f64();

@@ -19,6 +19,8 @@ public:
     virtual bool has_ldlt() const { return false; }
     virtual void stability(double* min_d, int64_t* neg) { *min_d = 0; *neg = 0; }
     virtual int last_iterations() const { return 0; }
+    // identifies the factorisation the solver currently holds (0: none / not a factorisation)
+    virtual uint64_t generation() const { return 0; }
 };
 
 // Multifrontal LDL^T.  fp64 = false: FP32 fronts (FP32 or FP64-assembled values rounded), with
@@ -33,6 +35,7 @@ public:
     bool has_ldlt() const override { return true; }
     void stability(double* min_d, int64_t* neg) override;
     int last_iterations() const override { return last_refine_its_; }
+    uint64_t generation() const override;
     void set_refine(int r) { refine_ = r; }
 
 private:

@@ -172,6 +172,7 @@ void ALMGPU::apply_options() {
     desiredIt_ = (int)opt_.integer("AdaptiveIterations", 10);
     quasi_ = opt_.integer("Quasi", 0) != 0;
     quasiInterval_ = (int)opt_.integer("QuasiIterations", -1);
+    frozen_it_ = (int)opt_.integer("FrozenIterations", 0);
     relax_ = opt_.real("Relaxation", 1.0);
     phi_ = opt_.real("Scaling", -1.0);
     phi_user_ = phi_ != -1.0;
@@ -210,6 +211,7 @@ void ALMGPU::stability_impl(bool jacobian, double shift) {
         if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
         ut_valid_ = false;
         fact_stale_ = false;
+        jac_gen_ = S_->generation();
     }
     if (bifurcation_ == 0) {
         // Determinant (gsALMBase.hpp:557-569): D of the current LDL^T factorisation
@@ -286,6 +288,7 @@ void ALMGPU::compute_jacobian() {
     KL_CUDA(cudaMemcpyAsync(xjac_.get(), x_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
     ut_valid_ = false;
     fact_stale_ = false;
+    jac_gen_ = S_->generation();
 }
 
 void ALMGPU::compute_residual() {
@@ -596,6 +599,7 @@ void ALMGPU::iteration() {
         ++n_jac;
         if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
         fact_stale_ = false;
+        jac_gen_ = S_->generation();
     }
     if (method_ == Crisfield) {
         solve_ut_ubar(!ut_valid_);
@@ -669,6 +673,9 @@ void ALMGPU::step_impl() {
         vec::multidot(1, a, a, n_, &d, P_.stream);
         use_guess = d != 0 && (Lguess_ - L_) != 0;
     }
+    // frozen tangent: a placed guess, and the fronts still hold this solver's last Jacobian
+    const bool frozen = use_guess && guess_place_ && frozen_it_ > 0 && S_->has_ldlt() && !fact_stale_ &&
+                        jac_gen_ != 0 && jac_gen_ == S_->generation();
     if (use_guess) predictor_guess();
     else predictor();
     compute_residual();
@@ -681,7 +688,9 @@ void ALMGPU::step_impl() {
     }
     stabilityPrev_ = stability_;
     for (num_it_ = 1; num_it_ < maxIt_; ++num_it_) {
-        if (!quasi_ || (quasiInterval_ > 0 && num_it_ % quasiInterval_ == 0)) quasi_newton_iteration();
+        bool refresh = !quasi_ || (quasiInterval_ > 0 && num_it_ % quasiInterval_ == 0);
+        if (frozen && num_it_ <= frozen_it_) refresh = false;
+        if (refresh) quasi_newton_iteration();
         iteration();
         stability_impl(false, -1e2);   // gsALMBase.hpp:390
         compute_residual();

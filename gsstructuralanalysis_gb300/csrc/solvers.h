@@ -117,6 +117,12 @@ public:
     // from the guessed point itself (DU = Uguess - U, DL = Lguess - L) instead of using the guess
     // only for the direction of the tangent predictor (gsALMCrisfield.hpp:167-191).
     void set_guess_place(bool on) { guess_place_ = on; }
+    // Frozen tangent after a placed guess (no reference counterpart; option "FrozenIterations",
+    // default 0 = off): the first N corrector iterations of a step that starts from a placed guess
+    // solve with the factorisation the solver already holds (the last Jacobian of an earlier
+    // step, a modified-Newton corrector), then the iteration returns to a fresh Jacobian per
+    // iteration.  Used only while the problem's fronts still hold that Jacobian.
+    void set_frozen_iterations(int n) { frozen_it_ = n; }
     int max_iter() const { return maxIt_; }
     void set_max_iter(int it) { maxIt_ = it; }
     Problem& problem() { return P_; }
@@ -163,6 +169,8 @@ private:
     bool adaptive_ = false;
     int desiredIt_ = 10;
     bool quasi_ = false;
+    int frozen_it_ = 0;
+    uint64_t jac_gen_ = 0;   // generation of the factorisation of the last Jacobian
     int quasiInterval_ = -1;
     double phi_ = -1;
     bool phi_user_ = false;

@@ -77,3 +77,42 @@ def test_learned_predictor_same_path_fewer_tangents(lib):
         assert results[mode][2] >= 20                     # the guess is used on most steps
         assert results[mode][1] < results["plain"][1]     # fewer tangent assemblies/factorisations
     print({k: (v[1], v[2]) for k, v in results.items()})
+
+
+def test_frozen_tangent_corrector_same_points(lib, oracle_mod):
+    """FrozenIterations: after a placed guess the corrector first iterates on the factorisation
+    the solver already holds.  The points are the points of the full-Newton run (same path, same
+    arc length), each meets the reference's force criterion when its residual is evaluated by the
+    oracle, and far fewer Jacobians are assembled and factorised."""
+    import gsstructuralanalysis_gb300 as G
+    opts = dict(Length=0.0025, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
+    base = P.cylindrical_panel(m=12, p=2, load=1.0)
+    modes, _, st = learned.buckling_modes(G, base, nmodes=3, shift=-0.5)
+    assert st == 0
+    paths = _paths(G, [0, 1, 2], modes, opts, 40)
+    tp = learned.train(G, paths, nm=16, hidden=64, epochs=300, batch=64, lr=2e-3)
+    test_prob = learned.imperfect_problem(base, modes, 1000)
+    oa = oracle_mod.OracleAssembler(test_prob)
+    F = oa.force()
+    runs = {}
+    for frozen in (0, 1, 2):
+        gp = G.Problem(test_prob)
+        alm = G.ALMCrisfield(gp, dict(opts, FrozenIterations=frozen) if frozen else opts)
+        alm.initialize()
+        pred = learned.make_predictor(G, gp, tp, use_net=True)
+        pts = []
+        for _ in range(30):
+            st, _ = pred.step(alm, guess_max_iter=frozen + 4 if frozen else 6)
+            if st != 0:
+                assert alm.step() == 0
+            U, L = alm.solutionU(), alm.solutionL()
+            pts.append((U, L))
+            R = oa.al_residual(U, L)
+            assert np.linalg.norm(R) <= 1e-8 * abs(L) * np.linalg.norm(F) * (1 + 1e-6)
+        runs[frozen] = (pts, alm.info()["n_jac"])
+    for frozen in (1, 2):
+        for (U, L), (Ur, Lr) in zip(runs[frozen][0], runs[0][0]):
+            assert abs(L - Lr) <= 1e-6 * abs(Lr)
+            assert np.linalg.norm(U - Ur) <= 1e-5 * np.linalg.norm(Ur)
+        assert runs[frozen][1] < 0.7 * runs[0][1]
+    print({k: v[1] for k, v in runs.items()})
