@@ -293,6 +293,9 @@ def run_ours(args):
                    "arc_length": ALM_OPTS["Length"], "TolF": 1e-8, "TolU": 1e-6,
                    "solver": "SimplicialLDLT -> nested-dissection multifrontal LDL^T (FP32 fronts)",
                    "l2": "inputs larger than L2 (multifrontal fronts %.0f MB)" % (stats["front_bytes"] / 1e6),
+                   "corrector": ("Crisfield; after a placed guess the first %d iteration(s) reuse the held "
+                                 "factorisation (FrozenIterations), then a fresh Jacobian per iteration"
+                                 % args.frozen_it) if (mode != "plain" and args.frozen_it) else "Crisfield, full Newton",
                    "final_load_factor": L_end, "jacobians_per_point": main["jac_per_point"],
                    "setup_s": t_setup, "training": train_info, "compare": compare,
                    "parallelism": f"replicas x{world}"},
