@@ -167,3 +167,52 @@ def test_assembly_error_status(oracle_mod):
     fint, jac, F = _truss()
     newton = oracle_mod.StaticNewton(jac(np.zeros(2)), F, jac, lambda x: None, dict(tol=1e-10))
     assert newton.solve() == oracle_mod.ASSEMBLY_ERROR
+
+
+def test_svk_membrane_uniaxial_stretch(oracle_mod):
+    """Nonlinear pin of the membrane part, the edge loads and gsStaticNewton: a flat SVK sheet
+    (nu = 0) pulled by a dead line load q on its right edge stretches uniformly to lambda with
+    t E lambda (lambda^2 - 1) / 2 = q (first Piola stress of the Green-Lagrange strain).  The
+    displacement field (lambda - 1) x lies in the spline space, so the discrete solution is exact."""
+    lam, E, t = 1.2, 1e3, 0.01
+    q = t * E * lam * (lam ** 2 - 1) / 2
+    prob = P.flat_plate(m=4, p=2, E=E, t=t, nu=0.0, pressure=0.0)
+    n, ncp = prob.n1, prob.ncp
+    ii = np.arange(ncp) % n
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[0, ii == 0] = True          # x on the left edge
+    fixed[1, 0] = True                # y at one corner
+    fixed[2, :] = True                # flat: no out-of-plane motion
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, q, 0.0, 0.0]])
+    A = oracle_mod.OracleAssembler(prob)
+    N = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(tol=1e-12, maxIt=50))
+    assert N.solve() == 0
+    u = A.to_full(N.U).reshape(3, ncp)
+    np.testing.assert_allclose(u[0], (lam - 1) * prob.ctrl[:, 0], atol=1e-10)
+    assert np.abs(u[1]).max() < 1e-10
+
+
+def test_plate_buckling_under_uniaxial_compression(oracle_mod):
+    """Pin of the geometric stiffness (second variation of the membrane strain): a simply
+    supported square plate under a uniform compressive edge load q buckles at
+    q_cr = 4 pi^2 D / b^2 (one half-wave each way).  The gsBucklingSolver pencil
+    K_L v = lambda B v, B = K(u_L) - K_L with u_L = K_L^-1 (s F), is the linear geometric
+    stiffness of the load s F for a small reference load s; the critical load is -lambda s."""
+    E, nu, t = 1.0, 0.3, 0.01
+    prob = P.flat_plate(m=8, p=3, E=E, nu=nu, t=t, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True              # w = 0 on the boundary (simple support)
+    fixed[0, ii == 0] = True          # x held on the loaded opposite edge
+    fixed[1, 0] = True                # y at one corner: free Poisson expansion
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, -1.0, 0.0, 0.0]])
+    A = oracle_mod.OracleAssembler(prob)
+    D = E * t ** 3 / (12 * (1 - nu ** 2))
+    expected = 4 * np.pi ** 2 * D
+    s = 1e-8                          # pre-buckling strain s q / (E t) = 1e-6
+    lam, _, _ = oracle_mod.buckling_dense(A.linear(), A.force(), A.jacobian, nev=1, shift=-expected / s, scaling=s)
+    assert abs(-lam[0] * s / expected - 1) < 1e-4      # 1.8e-5 at 8x8 cubic elements
