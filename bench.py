@@ -45,8 +45,8 @@ def workload_problem(m=None, p=None):
 
 
 def profiler_range(on):
-    """Mark the timed region for a profiler started with --profile-from-start off (driver API
-    cuProfilerStart/Stop on the current context); a no-op when the driver library is absent."""
+    """Mark the timed region for a profiler started with --profile-from-start off (CUDA driver
+    API cuProfilerStart/Stop on the current context); a no-op when libcuda is absent."""
     try:
         import ctypes
         cu = ctypes.CDLL("libcuda.so.1")
