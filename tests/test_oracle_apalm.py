@@ -45,3 +45,18 @@ def test_apalm_restatement(oracle_mod):
     np.testing.assert_allclose(b.times[0], a.times[0], rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose([s[1] for s in b.solutions[0]], [s[1] for s in a.solutions[0]], rtol=1e-9)
     assert list(b.levels[0]) == list(a.levels[0])
+
+
+def test_apalm_over_riks(oracle_mod):
+    """APALM over Riks measures its intervals in Riks's norm (gsALMRiks.h:81-84): the corrected
+    sub-steps cover every interval (the check in gsAPALMData::submit) and the times grow."""
+    from gsstructuralanalysis_gb300 import problems as P
+    prob = P.cylindrical_panel(m=5, p=2, load=1e5)
+    oa = oracle_mod.OracleAssembler(prob)
+    alm = oracle_mod.ALMRiks(oa.jacobian, oa.al_residual, oa.force(),
+                             dict(Length=0.003, TolF=1e-8, TolU=1e-6, MaxIter=30, BifurcationMethod=-1))
+    a = AP.APALM(alm, dict(SubIntervals=2, MaxLevel=1, Tolerance=1e-4, MaxIt=20))
+    a.initialize()
+    a.solve(4)
+    t, lv = np.array(a.times[0]), np.array(a.levels[0])
+    assert len(t) >= 7 and np.all(np.diff(t) > 0) and lv.max() == 1
