@@ -1,11 +1,11 @@
 // noalloc.cu -- ALResidual (R = Fint(x) - lambda F) that allocates no device memory.
 //
-// Who needs it: callers that cannot call cudaMalloc at the point where they need a residual,
-// e.g. code running inside a captured CUDA graph region or under a host framework that owns
-// the device memory pool and forbids allocations outside it.  The regular klsa_al_residual
-// grows its element-force buffer and staging vectors with cudaMalloc on first use; this variant
-// takes caller-owned device vectors and keeps its only scratch -- the per-element internal
-// forces -- in a fixed file-scope device array.
+// Who needs it: callers that must not allocate device memory at the point where they need a
+// residual -- a host framework that owns the whole device memory pool and forbids allocations
+// outside it, or a service whose device footprint is fixed when it starts.  The regular
+// klsa_al_residual grows its element-force buffer and staging vectors with cudaMalloc on first
+// use; this variant takes caller-owned device vectors and keeps its only scratch -- the
+// per-element internal forces -- in a fixed file-scope device array.
 //
 // Limits and sharing
 //   * scratch: NOALLOC_SCRATCH_DOUBLES doubles (8 MiB) per GPU that loads the library, held
@@ -13,8 +13,14 @@
 //   * every call shares the array and it keeps the last call's contents; each call overwrites
 //     every entry it reads, so nothing needs clearing.  Calls that overlap on the GPU (two host
 //     threads, or two problems' streams) race on the array: serialise them.
+//   * the call writes the problem's full-layout displacement vector (P.d_ufull), which the
+//     problem's other entry points and solvers also write: no other call on the same problem
+//     may overlap it.
+//   * the kernels go to the problem's stream, which waits for no other stream: the caller
+//     completes every pending write to d_x first.  The call synchronises that stream before it
+//     returns.
 //   * the first call on a device resolves the array's device address with
-//     cudaGetSymbolAddress (once per device); make that first call before any stream capture.
+//     cudaGetSymbolAddress (once per device, with that device current).
 #include <cuda_runtime.h>
 
 #include <exception>

@@ -85,14 +85,24 @@ int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_
 int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals);
 
 /* ALResidual_t without device allocation -- no counterpart in the reference.  For callers that
- * cannot call cudaMalloc where they need a residual (inside a captured CUDA-graph region, or
- * under a framework that owns the device memory pool).  x and R are caller-owned DEVICE
- * vectors in the public free-dof order.  The element-force scratch is a fixed file-scope device
- * array of 2^20 doubles (8 MiB per GPU, held until exit); problems with more than 2^20
- * element-force entries (elements x 3(p+1)^2) are rejected with KLSA_INVALID_ARGUMENT.  Calls
- * share that array: calls that overlap on the GPU race.  The first call on a device resolves
- * the array's address once; make it before any stream capture.  Synchronises the problem's
- * stream before returning. */
+ * must not allocate device memory at the point where they need a residual: a host framework
+ * that owns the whole device memory pool and forbids allocations outside it, or a
+ * memory-budgeted service whose device footprint is fixed when it starts.  The regular
+ * klsa_al_residual grows its element-force and staging buffers with cudaMalloc on first use;
+ * this one does not.  x and R are caller-owned DEVICE vectors in the public free-dof order.
+ *   - Scratch: a fixed file-scope device array of 2^20 doubles (8 MiB on every GPU that loads
+ *     the library, held until exit).  Problems needing more than 2^20 element-force entries
+ *     (elements x 3(p+1)^2) are rejected with KLSA_INVALID_ARGUMENT.
+ *   - Every call shares that array and it keeps the last call's contents; calls that overlap on
+ *     the GPU (two host threads, or two problems) race on it: serialise them.
+ *   - The call also overwrites the problem's own displacement state (the full-layout vector
+ *     that klsa_residual / klsa_al_residual and the solvers of this problem write), so it must
+ *     not overlap any other call on the same problem.
+ *   - The kernels run on the problem's own stream, which does not wait for other streams: all
+ *     pending writes to x must be complete before the call (synchronise the stream that wrote
+ *     it).  The call synchronises the problem's stream before it returns, so R is ready then.
+ *   - The first call on a device resolves the array's device address once
+ *     (cudaGetSymbolAddress, with that device current). */
 int klsa_al_residual_noalloc(klsa_problem* prob, const double* d_x, double lambda, double* d_R);
 
 /* ---- options (gsOptionList keys and defaults of the mirrored classes) ------------------ */

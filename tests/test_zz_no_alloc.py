@@ -1,12 +1,13 @@
 """The allocation-free ALResidual entry point (klsa_al_residual_noalloc).
 
-It exists for callers that cannot call cudaMalloc where they need a residual -- inside a
-captured CUDA-graph region, or under a framework that owns the device memory pool -- and keeps
-its element-force scratch in a fixed file-scope device array instead of growing a buffer.  The
-test compares it, through the C-ABI, with the allocating klsa_al_residual on two calls in a row
-(the second call reuses the shared scratch left by the first), and checks that a problem larger
-than the scratch is rejected.  This file is collected last so that a stop-at-first-failure run
-has already run every other test.
+It exists for callers that must not allocate device memory where they need a residual -- a host
+framework that owns the whole device memory pool, or a service whose device footprint is fixed
+at start-up -- and keeps its element-force scratch in a fixed file-scope device array instead of
+growing a buffer.  The test compares it, through the C-ABI, with the allocating
+klsa_al_residual on two calls in a row (the second call reuses the shared scratch left by the
+first), and checks that a problem larger than the scratch is rejected.  As the entry point
+requires, every write to the input vector is complete (torch.cuda.synchronize) before the call.
+This file is collected last so that a stop-at-first-failure run has already run every other test.
 """
 import numpy as np
 import pytest
