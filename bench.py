@@ -34,7 +34,8 @@ from gsstructuralanalysis_gb300 import problems as P  # noqa: E402
 
 WORKLOAD = dict(m=128, p=2, load=1.0)
 ALM_OPTS = dict(Length=0.005, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
-TEST_SEED = 1000          # imperfection seed of the measured path (training seeds are 0..n_train-1)
+TEST_SEED = 1000          # first held-out imperfection seed (training seeds are 0..n_train-1)
+TRAIN_POINTS = 200        # arc-length steps per path, training and test
 COARSE_M = 16             # imperfection modes: buckling modes of the 16x16 roof, transferred exactly
 METRIC = "arc-length path points/s at 50k dofs, learned vs plain predictor, ||R||/||F||<=1e-8"
 MAX_RETRIES = 6
@@ -154,6 +155,37 @@ def step_with_retry(alm, G):
 # ---------------------------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------------------------
+def train_predictor(G, learned, base, modes, args):
+    """Training set of the learned predictor: ``args.train_paths`` seeded imperfect roofs (seeds
+    0..n-1), each a Crisfield path of TRAIN_POINTS points generated by the library's GPU
+    arc-length solver, several paths at a time on separate host threads.  The POD basis comes
+    from the first ``args.pod_paths`` paths (full vectors); the other paths are kept as their
+    modal projections only.  The last path is held out for early stopping."""
+    n_train = max(2, args.train_paths)
+    n_pod = max(2, min(args.pod_paths, n_train))
+    t0 = time.perf_counter()
+    pod = learned.generate_paths(G, base, modes, range(n_pod), ALM_OPTS, TRAIN_POINTS, workers=args.train_workers)
+    Phi = learned.pod_modes(pod, 32)
+    rest = learned.generate_paths(G, base, modes, range(n_pod, n_train), ALM_OPTS, TRAIN_POINTS,
+                                  workers=args.train_workers, Phi=Phi) if n_train > n_pod else []
+    paths = [(U @ Phi.T, L) for U, L in pod] + rest
+    del pod
+    t1 = time.perf_counter()
+    samples = sum(max(len(L) - 4, 0) for _, L in paths)
+    batch = 128 if samples < 20000 else 256
+    epochs = int(np.clip(np.ceil(args.train_updates / max(samples / batch, 1.0)), 10, 400))
+    chunk = max(1, epochs // 40)
+    tp = learned.train(G, paths, nm=32, hidden=256, epochs=epochs, batch=batch, lr=1e-3, chunk=chunk, Phi=Phi)
+    info = {"paths": n_train, "points_per_path": TRAIN_POINTS, "pod_paths": n_pod,
+            "points_generated": int(sum(len(L) - 1 for _, L in paths)), "samples": tp.nsamples,
+            "epochs": epochs, "batch": batch, "path_generation_s": t1 - t0,
+            "path_generation_points_per_s": sum(len(L) - 1 for _, L in paths) / (t1 - t0),
+            "generation_workers": args.train_workers, "training_s": tp.seconds["train"], "alpha": tp.alpha,
+            "best_epoch": tp.best_epoch, "val_rel_error_vs_extrapolation": tp.val_rel_error,
+            "seeds": f"0..{n_train - 1} (held out for early stopping: {n_train - 1})"}
+    return tp, info
+
+
 def run_ours(args):
     import gsstructuralanalysis_gb300 as G
     from gsstructuralanalysis_gb300 import build as B, learned
@@ -166,28 +198,28 @@ def run_ours(args):
     base = workload_problem()
     t_setup = time.perf_counter()
     modes, bvals, _ = learned.buckling_modes(G, base, nmodes=5, shift=-0.5, coarse=workload_problem(m=COARSE_M))
-    prob = learned.imperfect_problem(base, modes, TEST_SEED + rank)
     tp, train_info = None, None
-    nsteps_path = args.steps + args.warmup
     if args.predictor == "learned":
-        t0 = time.perf_counter()
-        paths = [learned.generate_path(G, learned.imperfect_problem(base, modes, s), ALM_OPTS, nsteps_path)
-                 for s in range(args.train_paths)]
-        t1 = time.perf_counter()
-        tp = learned.train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=1e-3, chunk=5)
-        train_info = {"paths": args.train_paths, "points_per_path": nsteps_path, "samples": tp.nsamples,
-                      "path_generation_s": t1 - t0, "training_s": tp.seconds["train"], "alpha": tp.alpha,
-                      "best_epoch": tp.best_epoch, "val_rel_error_vs_extrapolation": tp.val_rel_error}
+        tp, train_info = train_predictor(G, learned, base, modes, args)
+    # the test shells: held-out seeds, one device problem each, primed (graphs captured) before timing
+    n_prob = max(1, min(args.steps, args.test_problems))
+    seeds = [TEST_SEED + (rank * n_prob + i) % 64 for i in range(n_prob)]
+    gps = [G.Problem(learned.imperfect_problem(base, modes, sd)) for sd in seeds]
+    for g in gps:
+        alm = G.ALMCrisfield(g, ALM_OPTS)
+        alm.initialize(stability=False)
+        alm.step()
+        del alm
     t_setup = time.perf_counter() - t_setup
-    gp = G.Problem(prob)
-    stats = gp.stats()
+    gp0 = gps[0]
+    stats = gp0.stats()
 
-    def make_arm(mode, frozen):
-        """A fresh Crisfield path and its step function.  The guess modes place the predicted point
-        and, with frozen > 0, start the corrector on the factorisation the solver already holds
-        (FrozenIterations); the plain mode is the reference's tangent predictor."""
+    def make_arm(gp, mode, frozen):
+        """A fresh Crisfield path on ``gp`` and its step function.  The guess modes place the
+        predicted point and, with frozen > 0, start the corrector on the factorisation the solver
+        already holds (FrozenIterations); the plain mode is the reference's tangent predictor."""
         alm = G.ALMCrisfield(gp, alm_options(mode, frozen))
-        alm.initialize()
+        alm.initialize(stability=False)
         pred = None if mode == "plain" else learned.make_predictor(G, gp, tp, use_net=(mode == "learned"))
         gmi = frozen + 4 if (frozen and pred is not None) else 6
 
@@ -198,110 +230,124 @@ def run_ours(args):
             return st == G.SUCCESS or step_with_retry(alm, G)
         return alm, pred, one
 
-    def run_path(mode, frozen=args.frozen_it):
-        alm, pred, one = make_arm(mode, frozen)
-
-        for _ in range(args.warmup):
-            one()
-        gp.sync()
-        barrier(world)
+    def run_path(gp, mode, frozen):
+        """One whole TRAIN_POINTS-point path; device time between events on the problem's stream
+        (every step synchronises with the host, so the span covers the path's GPU timeline)."""
+        alm, pred, one = make_arm(gp, mode, frozen)
         j0 = alm.info()["n_jac"]
+        gp.record(2)
+        pts = sum(1 for _ in range(TRAIN_POINTS) if one())
+        gp.record(3)
+        ms = gp.elapsed_ms(2, 3)
+        return dict(pts=pts, ms=ms, jac=alm.info()["n_jac"] - j0, L=alm.solutionL())
+
+    def run_arm(mode, frozen, npaths, warm=0):
+        for i in range(warm):
+            run_path(gps[i % n_prob], mode, frozen)
+        for g in gps:
+            g.sync()
+        barrier(world)
         l0 = G.launch_count()
         profiler_range(True)
-        gp.record(0)
+        gp0.record(0)
         t_wall = time.perf_counter()
-        pts = 0
-        for _ in range(args.steps):
-            pts += 1 if one() else 0
-        gp.record(1)
+        per = [run_path(gps[i % n_prob], mode, frozen) for i in range(npaths)]
+        gp0.record(1)
         profiler_range(False)
-        ms = gp.elapsed_ms(0, 1)
-        t_wall = time.perf_counter() - t_wall
-        return dict(alm=alm, pred=pred, pts=pts, ms=ms, wall=t_wall, launches=G.launch_count() - l0,
-                    jac_per_point=(alm.info()["n_jac"] - j0) / max(pts, 1))
+        ms = gp0.elapsed_ms(0, 1)
+        return dict(per=per, pts=sum(r["pts"] for r in per), ms=ms, wall=time.perf_counter() - t_wall,
+                    launches=G.launch_count() - l0,
+                    jac_per_point=sum(r["jac"] for r in per) / max(sum(r["pts"] for r in per), 1))
 
     mode = args.predictor
     clk = ClockSampler()
     clk.start()
-    main = run_path(mode)
+    main = run_arm(mode, args.frozen_it, args.steps, args.warmup)
     clocks = clk.stop()
     ms = reduce_max(main["ms"], world)
     barrier(world)
     value = world * main["pts"] / (ms / 1e3)
-    alm = main["alm"]
-    U_end, L_end = alm.solutionU(), alm.solutionL()
     launches = main["launches"]
     pts = main["pts"]
     if args.lean:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "points/s", "steps": args.steps,
-                              "ms_per_step": ms / max(pts, 1), "gpu_launches": int(launches), "lean": True}))
+                              "ms_per_step": ms / max(args.steps, 1), "gpu_launches": int(launches), "lean": True}))
         return
-    compare = {}
+    # comparison arms on the same test paths (the first n_cmp of the timed ones)
+    compare, top = {}, {}
     if mode == "learned":
+        n_cmp = max(1, min(args.compare_paths, args.steps))
+        same = main["per"][:n_cmp]
+        learned_same = sum(r["pts"] for r in same) / (sum(r["ms"] for r in same) / 1e3)
         arms = [("plain", "plain", 0), ("extrapolation", "extrapolation", args.frozen_it)]
         if args.frozen_it:
             arms.append(("learned_full_newton", "learned", 0))
         for name, m, fz in arms:
-            r = run_path(m, fz)
+            r = run_arm(m, fz, n_cmp)
             compare[name] = {"points_per_s": world * r["pts"] / (reduce_max(r["ms"], world) / 1e3),
-                             "jacobians_per_point": r["jac_per_point"], "frozen_iterations": fz}
-        compare["learned"] = {"points_per_s": value, "jacobians_per_point": main["jac_per_point"],
-                              "frozen_iterations": args.frozen_it}
-        compare["learned_over_plain"] = value / compare["plain"]["points_per_s"]
-        compare["final_load_factor_plain_vs_learned"] = None
+                             "jacobians_per_point": r["jac_per_point"], "frozen_iterations": fz,
+                             "final_load_factors": [x["L"] for x in r["per"]]}
+        compare["learned"] = {"points_per_s": learned_same, "jacobians_per_point":
+                              sum(r["jac"] for r in same) / max(sum(r["pts"] for r in same), 1),
+                              "frozen_iterations": args.frozen_it, "final_load_factors": [x["L"] for x in same]}
+        compare["paths"] = n_cmp
+        top = {"plain_points_per_s": compare["plain"]["points_per_s"],
+               "learned_over_plain": learned_same / compare["plain"]["points_per_s"],
+               "network_over_extrapolation": learned_same / compare["extrapolation"]["points_per_s"]}
 
-    # e2e: the same steps again through the C-ABI with host vectors in and out every step
-    alm2, pred2, one2 = make_arm(mode, args.frozen_it)
-    U = np.zeros(gp.ndof)
-    L = 0.0
-    pin_bytes = 8 * gp.ndof
-
-    for _ in range(args.warmup):
-        alm2.setSolution(U, L)
-        one2()
-        U, L = alm2.solutionU(), alm2.solutionL()
-    gp.sync()
+    # e2e: the same paths again through the C-ABI with host vectors in and out every step
+    pin_bytes = 8 * gp0.ndof
+    record = []
+    gp0.sync()
     barrier(world)
     t0 = time.perf_counter()
     pts2 = 0
-    for _ in range(args.steps):
-        alm2.setSolution(U, L)                 # H2D: the step's input state
-        pts2 += 1 if one2() else 0
-        U, L = alm2.solutionU(), alm2.solutionL()   # D2H: the step's result
-    gp.sync()
+    for i in range(args.steps):
+        g = gps[i % n_prob]
+        alm2, pred2, one2 = make_arm(g, mode, args.frozen_it)
+        U, L = np.zeros(g.ndof), 0.0
+        for _ in range(TRAIN_POINTS):
+            alm2.setSolution(U, L)                 # H2D: the step's input state
+            pts2 += 1 if one2() else 0
+            U, L = alm2.solutionU(), alm2.solutionL()   # D2H: the step's result
+            if i == 0:
+                record.append((U, L))
+        del alm2, pred2
+    for g in gps:
+        g.sync()
     e2e_s = reduce_max(time.perf_counter() - t0, world)
-    e2e = {"value": world * pts2 / e2e_s, "unit": "points/s", "h2d_bytes_per_step": pin_bytes,
-           "d2h_bytes_per_step": pin_bytes + 8}
-    if compare:
-        compare["final_load_factor_plain_vs_learned"] = [float(L), float(L_end)]
+    e2e = {"value": world * pts2 / e2e_s, "unit": "points/s", "h2d_bytes_per_step": pin_bytes * TRAIN_POINTS,
+           "d2h_bytes_per_step": (pin_bytes + 8) * TRAIN_POINTS}
 
-    prof = profile_phases(G, gp, args, lambda: make_arm(mode, args.frozen_it)[::2])
+    prof = profile_phases(G, gps[0], args, lambda: make_arm(gps[0], mode, args.frozen_it)[::2])
     roof = roofline(prof, stats, args)
-    info = alm.info()
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.skip_cpu:
-        cpu = cpu_baseline(prob)
+        cpu, parity = cpu_baseline_and_parity(record, gps[0].prob, args.parity_points)
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / max(pts, 1), "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        **top,
         "config": {"workload": "Crisfield arc-length, shallow cylindrical roof R=2.5 L=2.5 span=0.2 t=0.01, "
-                               "degree 2, 128x128 elements (50,700 dofs), imperfection of 5 buckling modes "
-                               f"(seed {TEST_SEED})",
-                   "ndof_free": int(gp.ndof), "nnz": int(gp.nnz), "predictor": mode,
+                               "degree 2, 128x128 elements (50,700 dofs), imperfection of 5 buckling modes; "
+                               f"one step = one {TRAIN_POINTS}-point path of a held-out imperfect roof "
+                               f"(test seeds {seeds[0]}..{seeds[-1]}, cycled)",
+                   "ndof_free": int(gp0.ndof), "nnz": int(gp0.nnz), "predictor": mode,
+                   "points_per_step": TRAIN_POINTS, "points_timed": int(pts),
                    "arc_length": ALM_OPTS["Length"], "TolF": 1e-8, "TolU": 1e-6,
                    "solver": "SimplicialLDLT -> nested-dissection multifrontal LDL^T (FP32 fronts)",
-                   "l2": "inputs larger than L2 (multifrontal fronts %.0f MB)" % (stats["front_bytes"] / 1e6),
+                   "l2": "inputs larger than L2 (multifrontal fronts %.0f MB per roof)" % (stats["front_bytes"] / 1e6),
                    "corrector": ("Crisfield; after a placed guess the first %d iteration(s) reuse the held "
                                  "factorisation (FrozenIterations), then a fresh Jacobian per iteration"
                                  % args.frozen_it) if (mode != "plain" and args.frozen_it) else "Crisfield, full Newton",
-                   "final_load_factor": L_end, "jacobians_per_point": main["jac_per_point"],
+                   "final_load_factors": [r["L"] for r in main["per"][:n_prob]],
+                   "jacobians_per_point": main["jac_per_point"],
                    "setup_s": t_setup, "training": train_info, "compare": compare,
                    "parallelism": f"replicas x{world}"},
-        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-        "phases_ms_per_step": prof["per_step"], "wall_s_timed": main["wall"],
-        "last_point": {"iterations": info["iterations"], "residueF": info["residueF"]},
+        "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "parity": parity,
+        "clocks": clocks, "phases_ms_per_point": prof["per_step"], "wall_s_timed": main["wall"],
     }
     if rank == 0:
         print(json.dumps(line))
@@ -310,11 +356,11 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def profile_phases(G, gp, args, make_arm, nsteps=None):
-    """Per-phase device times of the measured arm (serialised launches with CUDA events)."""
-    nsteps = nsteps or min(args.steps, 20)
+def profile_phases(G, gp, args, make_arm, nsteps=40, warm=8):
+    """Per-phase device times of the measured arm (serialised launches with CUDA events), per
+    point, over ``nsteps`` points after ``warm`` points of a fresh path."""
     alm, one = make_arm()
-    for _ in range(args.warmup):
+    for _ in range(warm):
         one()
     gp.sync()
     G.profile_reset()
@@ -364,32 +410,12 @@ def roofline(prof, stats, args):
         if not n:
             continue
         t = ms / n / 1e3
-        detail[k] = {"ms_total_per_step": ms / prof["nsteps"], "avg_launch_us": 1e6 * t,
+        detail[k] = {"ms_per_point": ms / prof["nsteps"], "avg_launch_us": 1e6 * t,
                      "gbs": byts / t / 1e9, "tflops": fl / t / 1e12, "bytes_per_launch": byts}
-    dom = max(detail, key=lambda k: detail[k]["ms_total_per_step"])
+    dom = max(detail, key=lambda k: detail[k]["ms_per_point"])
     ach = detail[dom]["gbs"]
-    # DRAM traffic per launch from ncu captures (profiles/arclength_50k_launches_diag_update.md).
-    # The first three timed mf_update_kernel launches (bottom levels, 957-1710 tiles) read 27-47 MB
-    # of DRAM against at most 64 KB algorithmic per tile; mid-level launches of 21, 7 and 15 tiles
-    # read 533, 257 and 404 KB and wrote 0 B: the written tiles stay in L2, and the panel blocks are read from
-    # L2 by the tiles that share them.  Top-level single-front mf_diag_kernel tiles read 45 KB and
-    # wrote 0 B against 48 KB algorithmic.  The live averages above span every level's launch shape,
-    # so the captured launches are reported beside them rather than as their traffic.
-    capture = [
-        {"kernel": "mf_update_kernel", "launches": "first three timed launches (1710, 1056, 957 tiles, bottom levels)",
-         "dram_bytes_per_launch": [46553344 + 123392, 38491136 + 2048, 26986240],
-         "algorithmic_bytes_upper_bound": [1710 * 65536, 1056 * 65536, 957 * 65536],
-         "source": "profiles/arclength_50k_launches_diag_update.md"},
-        {"kernel": "mf_update_kernel", "launches": "timed launches 60-62 (21, 7, 15 tiles)",
-         "dram_bytes_per_launch": [532736, 256512, 404480],
-         "algorithmic_bytes_per_launch": [21 * 65536, 7 * 65536, 15 * 65536],
-         "source": "profiles/arclength_50k_launches_diag_update.md"},
-        {"kernel": "mf_diag_kernel", "launches": "top-level single-front tiles (timed launches 35-37)",
-         "dram_bytes_per_launch": [45056, 45056, 44544], "algorithmic_bytes_per_launch": [49152] * 3,
-         "source": "profiles/arclength_50k_launches_diag_update.md"},
-    ]
     return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-            "traffic": None, "traffic_capture": capture, "peak_source": src,
+            "traffic": None, "peak_source": src,
             "note": "multifrontal kernels are bound by the latency of the pivot-tile chain, not by HBM or FLOP rate; "
                     "per-kernel bandwidth and FLOP rates in detail",
             "factorization_ms": raw["factorization"][0] / fac_n,
@@ -440,11 +466,39 @@ def _cpu_step(alm):
     return False
 
 
-def cpu_baseline(prob):
-    n, dt = cpu_points(prob, 1)
-    return {"value": n / dt, "unit": "points/s", "cores": host_cores(), "kind": "port",
-            "sample": "first arc-length point of the same workload (1 point: FP64 C++ OpenMP assembly on all "
-                      "host cores, scipy SuperLU LDL^T stand-in, restated Crisfield logic)"}
+def cpu_baseline_and_parity(record, gpu_prob, k):
+    """CPU baseline and parity of the headline path, after the timed region.
+
+    * residueF at every GPU point of the first recorded path, with the FP64 oracle's residual
+      on the identical shell: ||Fint(U) - lambda F|| / ||lambda F|| (gsALMBase.hpp:156-168
+      measures the converged point against (lambda + dlambda) F, which is lambda F here);
+    * the oracle's own first ``k`` points (plain tangent predictor, restated gsALMCrisfield,
+      SuperLU as the SimplicialLDLT stand-in), timed: the CPU baseline;
+    * the relative difference of the GPU's first ``k`` points from the oracle's."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build_oracle()
+    A = O.OracleAssembler(gpu_prob, nthreads=host_cores())
+    F = A.force()
+    resF = [float(np.linalg.norm(A.al_residual(U, L)) / np.linalg.norm(L * F)) for U, L in record]
+    alm = O.ALMCrisfield(A.jacobian, A.al_residual, F, dict(ALM_OPTS))
+    pts = []
+    t0 = time.perf_counter()
+    for _ in range(k):
+        if not _cpu_step(alm):
+            break
+        pts.append((alm.U.copy(), float(alm.L)))
+    dt = time.perf_counter() - t0
+    dU = [float(np.linalg.norm(record[i][0] - u) / np.linalg.norm(u)) for i, (u, _) in enumerate(pts)]
+    dL = [float(abs(record[i][1] - l) / abs(l)) for i, (_, l) in enumerate(pts)]
+    cpu = {"value": len(pts) / dt, "unit": "points/s", "cores": host_cores(), "kind": "port",
+           "sample": f"first {len(pts)} arc-length points of the first test path (FP64 C++ OpenMP assembly on "
+                     "all host cores, scipy SuperLU LDL^T stand-in, restated gsALMCrisfield, plain predictor)"}
+    parity = {"oracle_residueF_max": max(resF), "oracle_residueF_points": len(resF),
+              "oracle_residueF_bound": 1e-8, "dU_rel_max": max(dU) if dU else None,
+              "dL_rel_max": max(dL) if dL else None, "points_compared": len(pts), "point_bound": 1e-6,
+              "ok": bool(max(resF) <= 1e-8 and (not dU or (max(dU) <= 1e-6 and max(dL) <= 1e-6)))}
+    return cpu, parity
 
 
 def run_reference(args):
@@ -836,11 +890,18 @@ def eigen_cpu_baseline():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=197)
+    ap.add_argument("--steps", type=int, default=6,
+                    help="timed steps; arc-length: one step = one whole 200-point path of a held-out roof")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
-    ap.add_argument("--train-paths", type=int, default=32)
+    ap.add_argument("--train-paths", type=int, default=96, help="training paths (seeds 0..n-1), 200 points each")
+    ap.add_argument("--pod-paths", type=int, default=32, help="training paths whose full vectors give the POD basis")
+    ap.add_argument("--train-workers", type=int, default=8, help="paths generated concurrently (host threads)")
+    ap.add_argument("--train-updates", type=int, default=40000, help="Adam updates of the training (sets the epochs)")
+    ap.add_argument("--test-problems", type=int, default=8, help="distinct held-out roofs the timed paths cycle over")
+    ap.add_argument("--compare-paths", type=int, default=2, help="test paths the plain / extrapolation arms run")
+    ap.add_argument("--parity-points", type=int, default=3, help="oracle points compared with the GPU path")
     ap.add_argument("--frozen-it", type=int, default=1,
                     help="corrector iterations on the held factorisation after a placed guess (0: full Newton)")
     ap.add_argument("--seed", type=int, default=0)

@@ -401,7 +401,7 @@ int BatchedNewton::solve() {
     }
     dU_.zero(s);
     if (!graph_) {
-        unsigned long long before = g_launch_count;
+        CaptureCount cc;
         KL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         try {
             iteration_launches();
@@ -415,8 +415,7 @@ int BatchedNewton::solve() {
         KL_CUDA(cudaStreamEndCapture(s, &g));
         KL_CUDA(cudaGraphInstantiate(&graph_, g, 0));
         cudaGraphDestroy(g);
-        graph_kernels_ = g_launch_count - before;
-        g_launch_count = before;
+        graph_kernels_ = cc.n;
     }
     for (int it = 0; it < maxIt_; ++it) {
         KL_CUDA(cudaGraphLaunch(graph_, s));

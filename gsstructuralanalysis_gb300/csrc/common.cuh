@@ -1,6 +1,7 @@
 // common.cuh -- shared helpers for the sm_103a Kirchhoff-Love shell library.
 #pragma once
 
+#include <atomic>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -79,9 +80,25 @@ struct DevBuf {
     size_t size() const { return n; }
 };
 
-// Launch counter for the kernels of this library (reported by the benchmark).
-extern unsigned long long g_launch_count;
-inline void count_launch(unsigned long long k = 1) { g_launch_count += k; }
+// Launch counter for the kernels of this library (reported by the benchmark).  Several host
+// threads may drive separate problems at once, so the counter is atomic; while a thread captures
+// a graph, its launches go to that capture's own counter (CaptureCount) instead.
+extern std::atomic<unsigned long long> g_launch_count;
+extern thread_local unsigned long long* t_capture_count;
+inline void count_launch(unsigned long long k = 1) {
+    if (t_capture_count)
+        *t_capture_count += k;
+    else
+        g_launch_count.fetch_add(k, std::memory_order_relaxed);
+}
+struct CaptureCount {
+    unsigned long long n = 0;
+    unsigned long long* prev;
+    CaptureCount() : prev(t_capture_count) { t_capture_count = &n; }
+    ~CaptureCount() { t_capture_count = prev; }
+    CaptureCount(const CaptureCount&) = delete;
+    CaptureCount& operator=(const CaptureCount&) = delete;
+};
 
 }  // namespace klsa
 

@@ -993,7 +993,7 @@ void MultifrontalT<T>::replay(GraphSlot& slot, const void* key0, const void* key
     if (!slot.exec || slot.key0 != key0 || slot.key1 != key1) {
         if (slot.exec) cudaGraphExecDestroy(slot.exec);
         slot.exec = nullptr;
-        unsigned long long before = g_launch_count;
+        CaptureCount cc;
         KL_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         try {
             launches();
@@ -1007,8 +1007,7 @@ void MultifrontalT<T>::replay(GraphSlot& slot, const void* key0, const void* key
         KL_CUDA(cudaStreamEndCapture(stream_, &g));
         KL_CUDA(cudaGraphInstantiate(&slot.exec, g, 0));
         cudaGraphDestroy(g);
-        slot.kernels = g_launch_count - before;
-        g_launch_count = before;
+        slot.kernels = cc.n;
         slot.key0 = key0;
         slot.key1 = key1;
     }

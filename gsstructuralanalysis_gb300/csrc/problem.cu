@@ -12,7 +12,8 @@
 
 namespace klsa {
 
-unsigned long long g_launch_count = 0;
+std::atomic<unsigned long long> g_launch_count{0};
+thread_local unsigned long long* t_capture_count = nullptr;
 PhaseTimer g_timer;
 
 namespace {

@@ -87,8 +87,53 @@ def generate_path(G, prob, alm_opts, nsteps):
             break
         Us.append(alm.solutionU())
         Ls.append(alm.solutionL())
+    del alm                      # the solver's device state goes before the problem's
     gp.close()
     return np.array(Us), np.array(Ls)
+
+
+def generate_paths(G, base, modes, seeds, alm_opts, nsteps, workers=8, frozen=1, Phi=None, on_done=None):
+    """Converged Crisfield paths of the imperfect shells ``seeds``, generated concurrently: each
+    host thread drives its own problem (own stream, own fronts) through ``nsteps`` points.
+
+    The corrector starts from the cubic extrapolation of the last four points (the placement
+    mode with ``frozen`` iterations on the held factorisation, plain tangent steps for the first
+    points and whenever a placed start fails).  Every point meets the same arc-length constraint
+    and the same TolF/TolU test as the plain predictor, so the paths are the same equilibrium
+    points.  With ``Phi`` each point is stored as its modal projection q = Phi U (nm numbers);
+    without, as the full vector.  Returns [(U or q, lambda)] in the order of ``seeds``."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
+    opts = dict(alm_opts, FrozenIterations=int(frozen)) if frozen else dict(alm_opts)
+    gmi = frozen + 4 if frozen else 6
+    lock = threading.Lock()
+
+    def one(seed):
+        gp = G.Problem(imperfect_problem(base, modes, seed))
+        alm = G.ALMCrisfield(gp, opts)
+        alm.initialize(stability=False)
+        pred = G.Predictor(gp, None, np.zeros((0, gp.ndof)))
+        U0 = np.zeros(gp.ndof)
+        Us = [U0 if Phi is None else Phi @ U0]
+        Ls = [0.0]
+        for _ in range(nsteps):
+            st, _ = pred.step(alm, guess_max_iter=gmi)
+            if st != G.SUCCESS and not step_with_retry(alm, G):
+                break
+            U = alm.solutionU()
+            Us.append(U if Phi is None else Phi @ U)
+            Ls.append(alm.solutionL())
+        del pred, alm
+        gp.close()
+        out = (np.array(Us), np.array(Ls))
+        if on_done is not None:
+            with lock:
+                on_done(seed, out)
+        return out
+
+    with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+        return list(ex.map(one, seeds))
 
 
 def pod_modes(paths, nm):
@@ -103,10 +148,12 @@ def pod_modes(paths, nm):
 
 
 def features_targets(paths, Phi):
+    """Features and targets of every point that has four predecessors and a successor.  A path
+    is (U, lambda) with full vectors, or (q, lambda) with modal projections (q.shape[1] = nm)."""
     nm = Phi.shape[0]
     X, T = [], []
     for U, L in paths:
-        q = U @ Phi.T                     # (N, nm)
+        q = U if U.shape[1] == nm else U @ Phi.T          # (N, nm)
         for k in range(3, len(U) - 1):
             f = []
             for b in range(4):
@@ -134,12 +181,14 @@ class TrainedPredictor:
     seconds: dict
 
 
-def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0, chunk=25, val_paths=1):
+def train(G, paths, nm=32, hidden=256, epochs=400, batch=128, lr=2e-3, seed=0, chunk=25, val_paths=1, Phi=None):
     """Train on all but the last ``val_paths`` paths, early-stop on the held-out paths, and scale
     the network's correction by the validation-optimal trust factor alpha in [0, 1]
-    (alpha = 0 reduces the predictor to the cubic extrapolation)."""
+    (alpha = 0 reduces the predictor to the cubic extrapolation).  ``Phi`` (nm x ndof) is the
+    modal basis when the paths are already projected; without it the POD of the paths is used."""
     t0 = time.perf_counter()
-    Phi = pod_modes(paths, nm)
+    if Phi is None:
+        Phi = pod_modes(paths, nm)
     tr, va = (paths[:-val_paths], paths[-val_paths:]) if len(paths) > val_paths else (paths, paths)
     X, T = features_targets(tr, Phi)
     Xv, Tv = features_targets(va, Phi)

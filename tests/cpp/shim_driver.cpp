@@ -1,6 +1,7 @@
-// C++ driver of the header-only layer (include/klshell_gb300.hpp): builds a 2x2-element clamped
-// plate, and either solves it statically (a device is present) or reports the library's CUDA
-// error through klsa::Error (no device).  Checks ABI error handling on every path.
+// C++ driver of the header-only layer (include/klshell_gb300.hpp): builds a 2x2-element simply
+// supported plate (degree 2, boundary control points fixed), and either solves it with
+// gsStaticNewton's mirror and prints the free-dof solution (a device is present) or reports the
+// library's CUDA error through klsa::Error (no device).  Checks ABI error handling on every path.
 #include <cstdio>
 #include <vector>
 
@@ -43,6 +44,9 @@ int main() {
         double wmax = 0.0;
         for (double v : U) wmax = v > wmax ? v : wmax;
         std::printf("ok status=%d ndof=%lld wmax=%.6e\n", st, (long long)P.numDofs(), wmax);
+        std::printf("U");
+        for (double v : U) std::printf(" %.17e", v);
+        std::printf("\n");
         return st == 0 ? 0 : 1;
     } catch (const klsa::Error& e) {
         std::printf("no-device code=%d\n", e.code);

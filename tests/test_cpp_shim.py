@@ -1,6 +1,7 @@
 """The header-only C++ layer (include/klshell_gb300.hpp) compiles against the C-ABI, links the
-built library, and reports ABI errors as klsa::Error; without a device, creating a problem fails
-with the library's CUDA error code instead of crashing."""
+built library, and reports ABI errors as klsa::Error.  Without a device, creating a problem fails
+with the library's CUDA error code instead of crashing; with one (the gpu-marked test), the C++
+StaticNewton solves the plate and its solution matches the FP64 oracle's gsStaticNewton."""
 import os
 import shutil
 import subprocess
@@ -10,7 +11,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_cpp_driver_builds_and_handles_errors(lib, tmp_path):
+def _build_and_run(tmp_path):
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("g++ not available")
@@ -27,4 +28,25 @@ def test_cpp_driver_builds_and_handles_errors(lib, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=120)
     out = r.stdout.strip()
     assert r.returncode == 0, (out, r.stderr)
+    return out
+
+
+def test_cpp_driver_builds_and_handles_errors(lib, tmp_path):
+    out = _build_and_run(tmp_path)
     assert out.startswith("no-device code=-2") or out.startswith("ok status=0"), out
+
+
+@pytest.mark.gpu
+def test_cpp_driver_solves_on_the_gpu(lib, oracle_mod, tmp_path):
+    import numpy as np
+    from gsstructuralanalysis_gb300 import problems as P
+    out = _build_and_run(tmp_path)
+    lines = out.splitlines()
+    assert lines[0].startswith("ok status=0"), out
+    U = np.array([float(v) for v in lines[1].split()[1:]])
+    prob = P.flat_plate(m=2, p=2, bc="simply", pressure=1.0)
+    oa = oracle_mod.OracleAssembler(prob)
+    ref = oracle_mod.StaticNewton(oa.linear(), oa.force(), oa.jacobian, oa.residual, dict(tol=1e-10, maxIt=20))
+    assert ref.solve() == 0
+    assert U.shape == ref.U.shape
+    assert np.linalg.norm(U - ref.U) <= 1e-6 * np.linalg.norm(ref.U)

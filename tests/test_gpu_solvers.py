@@ -206,3 +206,40 @@ def test_singular_point_and_branch_switch(lib, oracle_mod, tolB):
                 assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-6 * np.linalg.norm(ref.U)
             break
     assert found
+
+
+@pytest.mark.parametrize("method", ["Crisfield", "Riks"])
+def test_reference_predictor_guess(lib, oracle_mod, method):
+    """setInitialGuess in the reference's own mode, step by step against the oracle.  Crisfield
+    uses the guess only as the old increment that orients the tangent predictor
+    (gsALMCrisfield.hpp:167-191); Riks rescales the guessed chord by Length / previous Length
+    (gsALMRiks.hpp:137-170).  The guess is selected only when it differs from the current point
+    in U and in lambda (gsALMBase.hpp:365-368).  Both sides get the identical host guess: the
+    linear extrapolation of the oracle's last two points, perturbed."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=8, p=2, load=1e5 if method == "Riks" else 1.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    length = {"Crisfield": 0.004, "Riks": 0.003}[method]
+    opts = dict(Length=length, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=30)
+    cls = {"Crisfield": G.ALMCrisfield, "Riks": G.ALMRiks}[method]
+    rcls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks}[method]
+    alm = cls(gp, opts)
+    alm.initialize()
+    ref = rcls(oa.jacobian, oa.al_residual, oa.force(), opts)
+    rng = np.random.default_rng(3)
+    prev = (np.zeros(gp.ndof), 0.0)
+    guessed = 0
+    for k in range(5):
+        if k >= 2:
+            Ug = 2 * ref.U - prev[0] + 1e-3 * np.linalg.norm(ref.U - prev[0]) * rng.standard_normal(gp.ndof) / np.sqrt(gp.ndof)
+            Lg = 2 * ref.L - prev[1]
+            alm.setInitialGuess(Ug, Lg)
+            ref.set_initial_guess(Ug, Lg)
+            guessed += 1
+        prev = (ref.U.copy(), ref.L)
+        assert alm.step() == 0, k
+        assert ref.step() == 0, k
+        U, L = alm.solutionU(), alm.solutionL()
+        assert np.linalg.norm(U - ref.U) / np.linalg.norm(ref.U) < 1e-6, k
+        assert abs(L - ref.L) / abs(ref.L) < 1e-6, k
+    assert guessed == 3
