@@ -316,7 +316,6 @@ BatchedNewton::~BatchedNewton() {
 void BatchedNewton::reset() {
     U_.zero(B_.stream);
     DU_.zero(B_.stream);
-    has_DU_ = false;
 }
 
 void BatchedNewton::residual(const double* d_x, double* d_R) {
@@ -370,20 +369,8 @@ void BatchedNewton::iteration_launches() {
 int BatchedNewton::solve() {
     const int n = B_.nfree;
     cudaStream_t s = B_.stream;
-    if (!has_DU_) {
-        // linear head start on the first call (gsStaticNewton.hpp:148-153): DU = K_L^-1 (L F)
-        x_.zero(s);
-        B_.set_displacement(x_.get());
-        B_.tangent_f32();
-        B_.mf->enqueue_factorize(B_.d_vals32.get());
-        vec::lincomb(L_, B_.d_F.get(), 0.0, B_.d_F.get(), R_.get(), n, s);
-        vec::to_f32(R_.get(), b32_.get(), n, s);
-        B_.mf->enqueue_solve(b32_.get(), x32_.get());
-        vec::to_f64(x32_.get(), DU_.get(), n, s);
-        U_.zero(s);
-        has_DU_ = true;
-        headstart_ = true;
-    }
+    // No linear head start: after gsStaticBase::initialize() (what the reference's drivers call)
+    // m_DeltaU has the dofs' rows, so gsStaticNewton.hpp:148-153 never takes it.
     // _start (gsStaticNewton.hpp:274-316): R0 = R(U); with the head start the iteration begins at
     // U + DU, otherwise DU = 0
     if (!headstart_) DU_.zero(s);

@@ -102,7 +102,7 @@ private:
     DevBuf<float> b32_, x32_;
     DevBuf<int> active_, fin_, st_, its_, it_, count_;
     int* h_count_ = nullptr;
-    bool has_DU_ = false, headstart_ = false;
+    bool headstart_ = false;
     cudaGraphExec_t graph_ = nullptr;
     unsigned long long graph_kernels_ = 0;
     std::vector<int> status_, iters_;

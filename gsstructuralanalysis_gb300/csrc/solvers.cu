@@ -62,7 +62,6 @@ void StaticNewtonGPU::set_displacement(const double* d_U) {
 void StaticNewtonGPU::set_update(const double* d_DU) {
     KL_CUDA(cudaMemcpyAsync(DU_.get(), d_DU, sizeof(double) * P_.nfree, cudaMemcpyDeviceToDevice, P_.stream));
     headstart_ = true;
-    has_DU_ = true;
 }
 
 int StaticNewtonGPU::solve_nonlinear_impl() {
@@ -73,17 +72,10 @@ int StaticNewtonGPU::solve_nonlinear_impl() {
     double tolU = opt_.real("tolU", -1) != -1 ? opt_.real("tolU", -1) : tol;
     int maxIt = (int)opt_.integer("maxIt", 25);
     double relax = opt_.real("Relaxation", 1.0);
-    if (!has_DU_) {
-        // first call: linear solve as head start (gsStaticNewton.hpp:148-153)
-        DevBuf<double> Usave(n);
-        KL_CUDA(cudaMemcpyAsync(Usave.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        if (solve_linear() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
-        KL_CUDA(cudaMemcpyAsync(DU_.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        KL_CUDA(cudaMemcpyAsync(dU_.get(), U_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        KL_CUDA(cudaMemsetAsync(U_.get(), 0, sizeof(double) * n, s));
-        headstart_ = true;
-        has_DU_ = true;
-    }
+    // gsStaticNewton.hpp:148-153 takes a linear head start only while m_DeltaU has no rows.  The
+    // reference's drivers construct the solver and call initialize() (gsStaticBase.h:53-57), whose
+    // reset() sizes m_DeltaU to the dofs (gsStaticBase.h:136-144), so that branch never runs: the
+    // iteration starts from U with a zero increment.  This solver is created in that state.
     // _start (hpp:274-316)
     if (!headstart_) {
         KL_CUDA(cudaMemsetAsync(DU_.get(), 0, sizeof(double) * n, s));

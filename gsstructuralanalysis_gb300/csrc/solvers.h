@@ -61,7 +61,7 @@ private:
     std::unique_ptr<LinearSolver> S_;
     DevBuf<double> U_, DU_, dU_, R_, x_, fint_;
     double L_ = 1.0;
-    bool headstart_ = false, has_DU_ = false;
+    bool headstart_ = false;
     int num_it_ = 0;
     double residual_ = 0, residualIni_ = 1, residualOld_ = 0;
 };

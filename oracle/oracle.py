@@ -219,8 +219,12 @@ class StaticNewton:
         if options:
             self.opts.update(options)
         n = len(self.F)
+        # the state after the constructor: gsStaticNewton::_init calls its reset(), which sets
+        # the dofs from the force vector and sizes DeltaU to them (gsStaticNewton.hpp:243-250,
+        # gsStaticBase.h:136-144), so the linear head start of gsStaticNewton.hpp:148-153 (taken
+        # only while DeltaU has no rows) never runs
         self.U = np.zeros(n)
-        self.DeltaU = np.zeros(0)
+        self.DeltaU = np.zeros(n)
         self.deltaU = np.zeros(n)
         self.headstart = False
         self.num_iterations = 0

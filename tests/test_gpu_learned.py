@@ -121,36 +121,38 @@ def test_frozen_tangent_corrector_same_points(lib, oracle_mod):
 
 
 def test_network_gains_over_extrapolation(lib):
-    """What the trained network adds to the method without it.  The same placement corrector
-    runs the held-out path twice: with the cubic extrapolation alone, and with the network's
-    correction of it.  The network's guesses are closer (held-out error well below the
-    extrapolation's, measured on a path not trained on), and the corrector needs fewer
-    iterations and no more Jacobians for the same points."""
+    """What the trained network adds to the method without it.  The held-out path runs twice with
+    the same placement corrector (FrozenIterations = 1: the first iteration after a placed guess
+    reuses the held factorisation, as in the measured configuration): with the cubic
+    extrapolation alone, and with the network's correction of it.  The network's guesses are
+    closer -- its held-out error is well below the extrapolation's on a path it was not trained
+    on -- so more steps finish on the held factorisation: fewer Jacobians for the same points.
+    (With the full-Newton corrector both need two iterations per point, because the second one
+    is what passes TolU; the gain shows in the Jacobians, not in the iteration count.)"""
     import gsstructuralanalysis_gb300 as G
     opts = dict(Length=0.0025, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=25, BifurcationMethod=-1)
     base = P.cylindrical_panel(m=12, p=2, load=1.0)
     modes, _, st = learned.buckling_modes(G, base, nmodes=5, shift=-0.5)
     assert st == 0
-    paths = learned.generate_paths(G, base, modes, range(12), opts, 60, workers=6)
+    paths = learned.generate_paths(G, base, modes, range(24), opts, 80, workers=8)
     tp = learned.train(G, paths, nm=16, hidden=64, epochs=300, batch=64, lr=2e-3)
-    assert tp.val_rel_error < 0.7, tp.val_rel_error
+    assert tp.val_rel_error < 0.5, tp.val_rel_error
     test_prob = learned.imperfect_problem(base, modes, 1000)
     runs = {}
     for use_net in (False, True):
         gp = G.Problem(test_prob)
-        alm = G.ALMCrisfield(gp, opts)
+        alm = G.ALMCrisfield(gp, dict(opts, FrozenIterations=1))
         alm.initialize(stability=False)
         pred = learned.make_predictor(G, gp, tp, use_net=use_net)
-        pts, its = [], 0
-        for _ in range(50):
-            st, _ = pred.step(alm, guess_max_iter=6)
+        pts = []
+        for _ in range(60):
+            st, _ = pred.step(alm, guess_max_iter=5)
             assert st == 0
-            its += alm.info()["iterations"]
             pts.append((alm.solutionU(), alm.solutionL()))
-        runs[use_net] = (pts, its, alm.info()["n_jac"])
+        runs[use_net] = (pts, alm.info()["n_jac"])
     for (U, L), (Ue, Le) in zip(runs[True][0], runs[False][0]):
         assert abs(L - Le) <= 1e-6 * abs(Le)
         assert np.linalg.norm(U - Ue) <= 1e-5 * np.linalg.norm(Ue)
-    print({"extrapolation": runs[False][1:], "network": runs[True][1:], "val_rel_error": tp.val_rel_error})
-    assert runs[True][1] < runs[False][1]          # fewer corrector iterations
-    assert runs[True][2] <= runs[False][2]         # no more Jacobians
+    print({"extrapolation_jacobians": runs[False][1], "network_jacobians": runs[True][1],
+           "val_rel_error": tp.val_rel_error})
+    assert runs[True][1] < runs[False][1]

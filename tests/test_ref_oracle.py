@@ -1,0 +1,207 @@
+"""The oracle's restatement (oracle/oracle.py) pinned against the reference's OWN solver code.
+
+oracle/_ref/libref_solvers.so is gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl,
+gsALMConsistentCrisfield, gsModalSolver and gsBucklingSolver compiled unchanged from the
+reference tree against the test-only linear-algebra stand-in (oracle/refshim/).  Both sides get
+the same FP64 KL-shell operators (oracle.OracleAssembler), so every difference would be a
+difference of solver logic.  The reference tree exists only where the library can be built;
+elsewhere these tests skip (the golden fixtures written from it, tests/golden/ref_solvers.npz,
+carry the pin to the GPU tests).
+"""
+import numpy as np
+import pytest
+
+from gsstructuralanalysis_gb300 import problems as P
+
+RS = pytest.importorskip("refsolvers")
+pytestmark = pytest.mark.skipif(not RS.available(), reason="reference tree not present: reference solvers not built")
+
+ALM_BASE = dict(TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=30, BifurcationMethod=-1)
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("solver", ["SimplicialLDLT", "CGDiagonal"])
+def test_static_newton_matches_reference(oracle_mod, solver):
+    """gsStaticNewton::solve from zero (after initialize(), as the reference's drivers call it):
+    same iterations, same point."""
+    prob = P.cylindrical_panel(m=6, p=3, load=800.0)
+    A = oracle_mod.OracleAssembler(prob)
+    ops = RS.Operators.from_assembler(A)
+    ref = RS.StaticNewton(ops, dict(tol=1e-8, maxIt=30, Solver=solver))
+    assert ref.solve() == 0
+    ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(tol=1e-8, maxIt=30))
+    assert ora.solve() == 0
+    assert _rel(ora.U, ref.solution()) < 1e-12
+    assert ora.num_iterations == ref.iterations()
+
+
+def test_static_newton_statuses_match_reference(oracle_mod):
+    """throw 1 (maxIt) -> NotConverged; a zero pivot (E = 0) -> SolverError (gsStaticNewton.hpp:75-98)."""
+    prob = P.cylindrical_panel(m=6, p=3, load=800.0)
+    A = oracle_mod.OracleAssembler(prob)
+    ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(tol=1e-8, maxIt=1))
+    ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(tol=1e-8, maxIt=1))
+    assert ref.solve() == ora.solve() == 1
+    # the factorising solver (gsStaticNewton's default, CGDiagonal, has no pivot to fail)
+    prob = P.flat_plate(m=4, p=2, E=0.0)
+    A = oracle_mod.OracleAssembler(prob)
+    ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(tol=1e-8, maxIt=5, Solver="SimplicialLDLT"))
+    ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(tol=1e-8, maxIt=5))
+    assert ref.solve() == ora.solve() == 3
+
+
+def test_static_newton_nan_start_is_not_converged(oracle_mod):
+    """A NaN in the start displacement stays in the iteration (no head start replaces it) and the
+    reference's convergence test never passes: NotConverged, with either solver (Eigen's LDL^T
+    flags only an exact zero pivot).  The oracle's SuperLU and the GPU's pivot check reject the
+    non-finite matrix instead (SolverError): a different failure status, never Success."""
+    prob = P.cylindrical_panel(m=6, p=2, load=500.0)
+    A = oracle_mod.OracleAssembler(prob)
+    U = np.zeros(len(A.force()))
+    U[len(U) // 3] = np.nan
+    for solver in ("CGDiagonal", "SimplicialLDLT"):
+        ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(tol=1e-8, maxIt=5, Solver=solver))
+        ref.set_displacement(U)
+        assert ref.solve() == 1
+    ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, dict(tol=1e-8, maxIt=5))
+    ora.set_displacement(U)
+    assert ora.solve() in (1, 3)
+
+
+def test_static_newton_load_ramp_matches_reference(oracle_mod):
+    """Load steps continued from the previous solution (setLoad through the Residual_t closure,
+    as the reference's ramp drivers rebuild it), through the limit point of the roof."""
+    Pmax = 30000.0
+    prob = P.cylindrical_panel(m=8, p=3, load=Pmax)
+    A = oracle_mod.OracleAssembler(prob)
+    F = A.force()
+    load = {"L": 0.0}
+    ops = RS.Operators(len(F), F, A.jacobian, lambda x, lam: A.fint(x) - lam * F,
+                       lambda x: load["L"] * F - A.fint(x))
+    ref = RS.StaticNewton(ops, dict(tol=1e-8, maxIt=50))
+    ora = None
+    for k in range(1, 6):
+        L = k / 5.0
+        load["L"] = L
+        if ora is None:
+            ora = oracle_mod.StaticNewton(A.linear(), L * F, A.jacobian, lambda U, L=L: L * F - A.fint(U),
+                                          dict(tol=1e-8, maxIt=50))
+        else:
+            ora.F = L * F
+            ora.res = (lambda U, L=L: L * F - A.fint(U))
+        assert ref.solve() == 0, k
+        assert ora.solve() == 0, k
+        assert _rel(ora.U, ref.solution()) < 1e-10, k
+        assert ora.num_iterations == ref.iterations(), k
+
+
+@pytest.mark.parametrize("method", ["Crisfield", "Riks", "LoadControl", "ConsistentCrisfield"])
+def test_arc_length_path_matches_reference(oracle_mod, method):
+    """Five steps of each arc-length method: same points, same iteration counts."""
+    prob = P.cylindrical_panel(m=6, p=2, load=1e5 if method == "Riks" else 1.0)
+    A = oracle_mod.OracleAssembler(prob)
+    length = {"Crisfield": 0.004, "Riks": 0.003, "LoadControl": 100.0, "ConsistentCrisfield": 0.004}[method]
+    opts = dict(ALM_BASE, Length=length)
+    cls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks,
+           "LoadControl": oracle_mod.ALMLoadControl, "ConsistentCrisfield": oracle_mod.ALMConsistentCrisfield}[method]
+    ref = RS.ALM(RS.Operators.from_assembler(A), method, opts)
+    ref.initialize()
+    ora = cls(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(5):
+        assert ref.step() == 0, k
+        assert ora.step() == 0, k
+        U, L = ref.solution()
+        assert _rel(ora.U, U) < 1e-10, k
+        assert abs(ora.L - L) <= 1e-10 * abs(L), k
+        assert ora.num_iterations == ref.info()["iterations"], k
+
+
+@pytest.mark.parametrize("variant", ["Quasi", "AdaptiveLength", "AngleMethod"])
+def test_crisfield_variants_match_reference(oracle_mod, variant):
+    """Quasi-Newton (QuasiIterations), AdaptiveLength and the angle-method root choice."""
+    prob = P.cylindrical_panel(m=6, p=2, load=1.0)
+    A = oracle_mod.OracleAssembler(prob)
+    extra = {"Quasi": dict(Quasi=True, QuasiIterations=2), "AdaptiveLength": dict(AdaptiveLength=True,
+             AdaptiveIterations=3), "AngleMethod": dict(AngleMethod=1)}[variant]
+    opts = dict(ALM_BASE, Length=0.004, **extra)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(5):
+        assert ref.step() == ora.step() == 0, k
+        U, L = ref.solution()
+        assert _rel(ora.U, U) < 1e-9, k
+        assert abs(ora.L - L) <= 1e-9 * abs(L), k
+        assert abs(ora.arcLength - ref.info()["length"]) <= 1e-12 * abs(ora.arcLength), k
+
+
+@pytest.mark.parametrize("method", ["Crisfield", "Riks"])
+def test_predictor_guess_matches_reference(oracle_mod, method):
+    """setInitialGuess -> predictorGuess (gsALMCrisfield.hpp:167-191, gsALMRiks.hpp:137-170)."""
+    prob = P.cylindrical_panel(m=6, p=2, load=1e5 if method == "Riks" else 1.0)
+    A = oracle_mod.OracleAssembler(prob)
+    opts = dict(ALM_BASE, Length=0.004 if method == "Crisfield" else 0.003)
+    cls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks}[method]
+    ref = RS.ALM(RS.Operators.from_assembler(A), method, opts)
+    ref.initialize()
+    ora = cls(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    rng = np.random.default_rng(3)
+    prev = (np.zeros(len(A.force())), 0.0)
+    for k in range(5):
+        if k >= 2:
+            Ug = 2 * ora.U - prev[0] + 1e-3 * np.linalg.norm(ora.U - prev[0]) * rng.standard_normal(len(ora.U)) / np.sqrt(len(ora.U))
+            Lg = 2 * ora.L - prev[1]
+            ref.set_initial_guess(Ug, Lg)
+            ora.set_initial_guess(Ug, Lg)
+        prev = (ora.U.copy(), ora.L)
+        assert ref.step() == ora.step() == 0, k
+        U, L = ref.solution()
+        assert _rel(ora.U, U) < 1e-10, k
+        assert abs(ora.L - L) <= 1e-10 * abs(L), k
+
+
+def test_stability_determinant_matches_reference(oracle_mod):
+    """BifurcationMethod 0 (Determinant: the LDL^T D, gsALMBase.hpp:547-570) along a Crisfield path
+    through the limit point: the same stability flag and stability change at every step."""
+    prob = P.cylindrical_panel(m=6, p=2, load=1.0)
+    A = oracle_mod.OracleAssembler(prob)
+    opts = dict(ALM_BASE, Length=0.006, BifurcationMethod=0)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    changes = 0
+    for k in range(14):
+        assert ref.step() == ora.step() == 0, k
+        info = ref.info()
+        assert int(info["stability"]) == ora.stability, k
+        assert bool(info["stability_change"]) == ora.stability_change(), k
+        changes += int(info["stability_change"])
+    assert changes >= 1
+
+
+def test_dense_eigen_compute_and_power_match_reference(oracle_mod):
+    """gsEigenProblemBase::compute (dense generalized solver, all pairs, with and without a shift)
+    and ::computePower (power iteration on A^-1 B: the pair of smallest |lambda|) of
+    gsModalSolver, against scipy's dense generalized eigensolver."""
+    import scipy.linalg as sla
+    prob = P.flat_plate(m=4, p=2, bc="simply")
+    A = oracle_mod.OracleAssembler(prob)
+    K, M = A.linear().toarray(), A.mass().toarray()
+    w = sla.eigh(K, M, eigvals_only=True)
+    for shift in (0.0, 0.5 * w[0]):
+        st, vals, vecs = RS.eigen_dense("modal", K, M, dict(shift=shift))
+        assert st == 0
+        assert np.abs(vals - w).max() <= 1e-9 * np.abs(w).max()
+        for j in range(len(w)):
+            v = vecs[:, j]
+            assert np.linalg.norm(K @ v - vals[j] * (M @ v)) <= 1e-8 * np.linalg.norm(K @ v)
+    st, val, vec = RS.eigen_dense("modal", K, M, dict(tolerance=1e-12), power=True)
+    assert st == 0
+    assert abs(val[0] - w[0]) <= 1e-8 * w[0]
