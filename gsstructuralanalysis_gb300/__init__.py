@@ -46,6 +46,7 @@ SIGNATURES = {
     "klsa_al_residual": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
     "klsa_al_residual_noalloc": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
     "klsa_jacobian_csr": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "klsa_djacobian_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
     "klsa_mass_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_options_create": (_c_vp, []),
     "klsa_options_destroy": (None, [_c_vp]),
@@ -316,6 +317,12 @@ class Problem:
         """Jacobian_t: K(x); precision 0 = FP32 element integration, 1 = FP64."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         return self._csr(_lib.klsa_jacobian_csr, _ptr(x), int(precision))
+
+    def djacobian(self, x, dx, precision: int = 1):
+        """dJacobian_t: the Jacobian called with the solution update (gsALMBase.hpp:214-223)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        return self._csr(_lib.klsa_djacobian_csr, _ptr(x), _ptr(dx), int(precision))
 
     def mass(self):
         return self._csr(_lib.klsa_mass_csr)

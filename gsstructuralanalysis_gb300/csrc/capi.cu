@@ -177,6 +177,16 @@ int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_
     });
 }
 
+int klsa_djacobian_csr(klsa_problem* prob, const double* x, const double* dx, int precision, int64_t* rowptr,
+                       int32_t* cols, double* vals) {
+    // The tangent at x.  The increment dx is part of the signature the solvers call
+    // (gsALMBase.hpp:214-223, gsStaticNewton.hpp:205-212) and is not used by this material: the
+    // reference itself builds its dJacobian from a Jacobian this way (gsALMBase.h:57-60,
+    // gsStaticNewton.h:79-82).
+    if (!dx) return KLSA_INVALID_ARGUMENT;
+    return klsa_jacobian_csr(prob, x, precision, rowptr, cols, vals);
+}
+
 int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals) {
     if (!prob || !rowptr || !cols || !vals) return KLSA_INVALID_ARGUMENT;
     return guarded([&] {

@@ -10,6 +10,8 @@
 // No pivoting (as Eigen's SimplicialLDLT); a zero or non-finite pivot sets the status word.
 #include "multifrontal.h"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -711,6 +713,265 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_bwd_own_kernel(
             x[o + j + (int64_t)n * q] = (part[0][q][jl] + part[1][q][jl]) + (part[2][q][jl] + part[3][q][jl]);
 }
 
+// ---- triangular solves in one persistent cooperative launch --------------------------------------
+// The products of the five-launch solve above, cut into 64 x 64 tiles of X = L11^-1 and L21 so
+// that every phase offers hundreds to thousands of independent tiles: one tile is one round of
+// 16 independent loads per thread, and its partial mat-vec is added atomically into the target
+// vector.  One grid walks all levels with a grid-wide barrier between phases:
+//   forward (leaves first), per level
+//     A  z(rows rb) += X(rb, cb) y(cb),  y = b_own + children's update vectors (inverse maps);
+//        the (0, 0) tile of a node also writes u = children's contributions to its halo
+//     B  u(rows ab) -= L21(ab, cb) z(cb)
+//   backward (root first), per level
+//     C  w(cols cb) -= L21(ab, cb)^T x(halo rows ab)
+//     D  x(cols jb) += X(ib, jb)^T (z / D + w)(ib)
+// z, w and x start at zero (prologue).  Atomic accumulation makes the summation order, and so
+// the last bits of the result, vary from run to run.
+template <class T>
+struct SolveArgs {
+    int n;
+    const int4* items;
+    const int *f, *k, *own, *child0, *child1, *halo, *inv;
+    const int64_t *front_off, *upd_off, *xinv_off, *halo_off, *inv_off;
+    const T *pool, *xinv, *D, *b;
+    T *x, *z, *w, *upd;
+};
+
+// sum of the children's update-vector entries that land on front position pos of node nd
+template <class T>
+__device__ __forceinline__ T mf_child_sum(const SolveArgs<T>& a, int nd, int pos, int q) {
+    const int2 iv = reinterpret_cast<const int2*>(a.inv)[a.inv_off[nd] + pos];
+    T s = T(0);
+    if (iv.x >= 0) {
+        const int c = a.child0[nd];
+        s += a.upd[a.upd_off[c] + iv.x + (int64_t)(a.f[c] - a.k[c]) * q];
+    }
+    if (iv.y >= 0) {
+        const int c = a.child1[nd];
+        s += a.upd[a.upd_off[c] + iv.y + (int64_t)(a.f[c] - a.k[c]) * q];
+    }
+    return s;
+}
+
+template <class T>
+__device__ __forceinline__ T mf_warp_sum(T v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Phase A tile (nd, rb, cb): rows i = rb*64 + warp + 8s, columns m = cb*64 + lane (+32).
+template <class T, int NR>
+__device__ __forceinline__ void mf_pt_own(const SolveArgs<T>& a, int4 it, T (*vs)[NB]) {
+    const int nd = it.x, rb = it.y, cb = it.z;
+    const int kN = a.k[nd], o = a.own[nd], n = a.n;
+    const int r0 = rb * NB, c0 = cb * NB;
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, m = e % NB, col = c0 + m;
+        vs[q][m] = col < kN ? a.b[o + col + (int64_t)n * q] + mf_child_sum(a, nd, col, q) : T(0);
+    }
+    if (rb == 0 && cb == 0) {           // the node's halo starts as the children's contributions
+        const int hN = a.f[nd] - kN;
+        T* u = a.upd + a.upd_off[nd];
+        for (int e = threadIdx.x; e < NR * hN; e += blockDim.x) {
+            const int q = e / hN, r = e % hN;
+            u[r + (int64_t)hN * q] = mf_child_sum(a, nd, kN + r, q);
+        }
+    }
+    __syncthreads();
+    const T* X = a.xinv + a.xinv_off[nd];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T xv[8][2];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int i = r0 + warp + 8 * s;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int m = c0 + lane + 32 * h;
+            xv[s][h] = (i < kN && m < kN && m <= i) ? X[(int64_t)i * kN + m] : T(0);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int i = r0 + warp + 8 * s;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            const T v = mf_warp_sum(xv[s][0] * vs[q][lane] + xv[s][1] * vs[q][lane + 32]);
+            if (lane == 0 && i < kN) atomicAdd(a.z + o + i + (int64_t)n * q, v);
+        }
+    }
+}
+
+// Phase B tile (nd, ab, cb): halo rows r = ab*64 + lane (+32), columns j = cb*64 + warp + 8s.
+template <class T, int NR>
+__device__ __forceinline__ void mf_pt_halo(const SolveArgs<T>& a, int4 it, T (*vs)[NB], T (*part)[NR][NB]) {
+    const int nd = it.x, ab = it.y, cb = it.z;
+    const int fN = a.f[nd], kN = a.k[nd], hN = fN - kN, o = a.own[nd], n = a.n;
+    const int r0 = ab * NB, c0 = cb * NB;
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, m = e % NB, col = c0 + m;
+        vs[q][m] = col < kN ? a.z[o + col + (int64_t)n * q] : T(0);
+    }
+    __syncthreads();
+    const T* F = a.pool + a.front_off[nd] + kN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T lv[8][2];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int j = c0 + warp + 8 * s;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = r0 + lane + 32 * h;
+            lv[s][h] = (j < kN && r < hN) ? F[(int64_t)j * fN + r] : T(0);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            T acc = T(0);
+#pragma unroll
+            for (int s = 0; s < 8; ++s) acc += lv[s][h] * vs[q][warp + 8 * s];
+            part[warp][q][lane + 32 * h] = acc;
+        }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, rl = e % NB, r = r0 + rl;
+        if (r < hN) {
+            T acc = T(0);
+#pragma unroll
+            for (int w = 0; w < 8; ++w) acc += part[w][q][rl];
+            atomicAdd(a.upd + a.upd_off[nd] + r + (int64_t)hN * q, -acc);
+        }
+    }
+}
+
+// Phase C tile (nd, ab, cb): w(j) -= sum_r L21(r, j) x(halo r); lanes over rows, warps over columns.
+template <class T, int NR>
+__device__ __forceinline__ void mf_pt_bwd_z(const SolveArgs<T>& a, int4 it, T (*vs)[NB]) {
+    const int nd = it.x, ab = it.y, cb = it.z;
+    const int fN = a.f[nd], kN = a.k[nd], hN = fN - kN, o = a.own[nd], n = a.n;
+    const int r0 = ab * NB, c0 = cb * NB;
+    const int* hl = a.halo + a.halo_off[nd];
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, rl = e % NB, r = r0 + rl;
+        vs[q][rl] = r < hN ? a.x[hl[r] + (int64_t)n * q] : T(0);
+    }
+    __syncthreads();
+    const T* F = a.pool + a.front_off[nd] + kN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T lv[8][2];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int j = c0 + warp + 8 * s;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = r0 + lane + 32 * h;
+            lv[s][h] = (j < kN && r < hN) ? F[(int64_t)j * fN + r] : T(0);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int j = c0 + warp + 8 * s;
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            const T v = mf_warp_sum(lv[s][0] * vs[q][lane] + lv[s][1] * vs[q][lane + 32]);
+            if (lane == 0 && j < kN) atomicAdd(a.w + o + j + (int64_t)n * q, -v);
+        }
+    }
+}
+
+// Phase D tile (nd, ib, jb): x(j) += sum_i X(i, j) (z(i) / D(i) + w(i)); lanes over columns.
+template <class T, int NR>
+__device__ __forceinline__ void mf_pt_bwd_own(const SolveArgs<T>& a, int4 it, T (*vs)[NB], T (*part)[NR][NB]) {
+    const int nd = it.x, ib = it.y, jb = it.z;
+    const int kN = a.k[nd], o = a.own[nd], n = a.n;
+    const int r0 = ib * NB, c0 = jb * NB;
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, rl = e % NB, i = r0 + rl;
+        vs[q][rl] = i < kN ? a.z[o + i + (int64_t)n * q] / a.D[o + i] + a.w[o + i + (int64_t)n * q] : T(0);
+    }
+    __syncthreads();
+    const T* X = a.xinv + a.xinv_off[nd];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T xv[8][2];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int i = r0 + warp + 8 * s;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = c0 + lane + 32 * h;
+            xv[s][h] = (i < kN && j < kN && i >= j) ? X[(int64_t)i * kN + j] : T(0);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            T acc = T(0);
+#pragma unroll
+            for (int s = 0; s < 8; ++s) acc += xv[s][h] * vs[q][warp + 8 * s];
+            part[warp][q][lane + 32 * h] = acc;
+        }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
+        const int q = e / NB, jl = e % NB, j = c0 + jl;
+        if (j < kN) {
+            T acc = T(0);
+#pragma unroll
+            for (int w = 0; w < 8; ++w) acc += part[w][q][jl];
+            atomicAdd(a.x + o + j + (int64_t)n * q, acc);
+        }
+    }
+}
+
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_solve_persistent_kernel(SolveArgs<T> a, SolveLevels lv) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ T vs[NR][NB];
+    __shared__ T part[8][NR][NB];
+    const int64_t nn = (int64_t)a.n * NR;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+        a.z[e] = T(0);
+        a.w[e] = T(0);
+        a.x[e] = T(0);
+    }
+    grid.sync();
+    for (int L = 0; L < lv.nlev; ++L) {
+        const int4* own = a.items + lv.own_off[L];
+        for (int i = blockIdx.x; i < lv.own_cnt[L]; i += gridDim.x) {
+            mf_pt_own<T, NR>(a, own[i], vs);
+            __syncthreads();
+        }
+        grid.sync();
+        if (lv.halo_cnt[L]) {
+            const int4* hal = a.items + lv.halo_off[L];
+            for (int i = blockIdx.x; i < lv.halo_cnt[L]; i += gridDim.x) {
+                mf_pt_halo<T, NR>(a, hal[i], vs, part);
+                __syncthreads();
+            }
+            grid.sync();
+        }
+    }
+    for (int L = lv.nlev - 1; L >= 0; --L) {
+        if (lv.halo_cnt[L]) {
+            const int4* hal = a.items + lv.halo_off[L];
+            for (int i = blockIdx.x; i < lv.halo_cnt[L]; i += gridDim.x) {
+                mf_pt_bwd_z<T, NR>(a, hal[i], vs);
+                __syncthreads();
+            }
+            grid.sync();
+        }
+        const int4* own = a.items + lv.own_off[L];
+        for (int i = blockIdx.x; i < lv.own_cnt[L]; i += gridDim.x) {
+            mf_pt_bwd_own<T, NR>(a, own[i], vs, part);
+            __syncthreads();
+        }
+        if (L > 0) grid.sync();
+    }
+}
+
 template <class T>
 __global__ void mf_stability_kernel(int n, const T* __restrict__ D, double* out_min, unsigned long long* out_neg) {
     __shared__ double smin[256];
@@ -861,6 +1122,17 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
         for (int nd : ln)
             for (int ab = 0; ab * NB < f[nd] - k[nd]; ++ab) items.push_back(make_int4(nd, ab, 0, 0));
         marks.push_back({L, 7, 0, 0, b, items.size()});
+        // persistent-solve tiles: lower-triangular 64x64 blocks of X (rb >= cb), all blocks of L21
+        b = items.size();
+        for (int nd : ln)
+            for (int rb = 0; rb * NB < k[nd]; ++rb)
+                for (int cb = 0; cb <= rb; ++cb) items.push_back(make_int4(nd, rb, cb, 0));
+        marks.push_back({L, 10, 0, 0, b, items.size()});
+        b = items.size();
+        for (int nd : ln)
+            for (int ab = 0; ab * NB < f[nd] - k[nd]; ++ab)
+                for (int cb = 0; cb * NB < k[nd]; ++cb) items.push_back(make_int4(nd, ab, cb, 0));
+        marks.push_back({L, 11, 0, 0, b, items.size()});
         int maxb = 0;
         for (int nd : ln) maxb = std::max(maxb, (k[nd] + NB - 1) / NB);
         levels_[L].xdiag.resize(maxb);
@@ -912,6 +1184,8 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
             case 7: lv.halo_blocks = w; break;
             case 8: lv.xdiag[m.step] = w; break;
             case 9: lv.xoff[m.step] = w; break;
+            case 10:
+            case 11: break;                      // persistent-solve tiles (solve_levels_)
             default: lv.nodes = w; break;
         }
     }
@@ -921,6 +1195,35 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
             kernel_launches[1] += st.panel.count > 0;
             kernel_launches[2] += (st.upd_next.count > 0) + (st.upd_rest.count > 0);
         }
+    }
+    // persistent solve: inverse child maps (front position -> child halo index, per child slot)
+    // and the per-level own / halo block lists
+    {
+        std::vector<int64_t> inv_off(nnodes_);
+        int64_t io = 0;
+        for (int i = 0; i < nnodes_; ++i) { inv_off[i] = io; io += f[i]; }
+        std::vector<int> inv((size_t)2 * std::max<int64_t>(io, 1), -1);
+        for (int i = 0; i < nnodes_; ++i) {
+            const int cs[2] = {c0[i], c1[i]};
+            for (int sl = 0; sl < 2; ++sl) {
+                const int c = cs[sl];
+                if (c < 0) continue;
+                const std::vector<int>& mp = Tr.parent_map[c];
+                for (int a = 0; a < (int)mp.size(); ++a) inv[2 * (inv_off[i] + mp[a]) + sl] = a;
+            }
+        }
+        d_inv_off_.upload(inv_off, stream_);
+        d_inv_.upload(inv, stream_);
+        if (nlevels_ > MF_MAX_LEVELS) throw std::invalid_argument("multifrontal: elimination tree too deep");
+        solve_levels_ = new SolveLevels();
+        solve_levels_->nlev = nlevels_;
+        for (const Pending& m : marks) {
+            if (m.kind == 10) { solve_levels_->own_off[m.level] = (int)m.begin; solve_levels_->own_cnt[m.level] = (int)(m.end - m.begin); }
+            if (m.kind == 11) { solve_levels_->halo_off[m.level] = (int)m.begin; solve_levels_->halo_cnt[m.level] = (int)(m.end - m.begin); }
+        }
+        // every node with a halo needs an own tile (0, 0) to start its update vector
+        for (int i = 0; i < nnodes_; ++i)
+            if (k[i] == 0 && f[i] > 0) persistent_ok_ = false;
     }
     d_f_.upload(f, stream_); d_k_.upload(k, stream_); d_own_.upload(own, stream_); d_parent_.upload(parent, stream_);
     d_child0_.upload(c0, stream_); d_child1_.upload(c1, stream_);
@@ -964,6 +1267,27 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
     KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
     KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
     KL_CUDA(cudaFuncSetAttribute(mf_bwd_own_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, ak));
+    {
+        // persistent solve: one CTA set resident on every SM (cooperative launch), shared memory
+        // for the largest own or halo part
+        int dev = 0, sms = 0;
+        KL_CUDA(cudaGetDevice(&dev));
+        KL_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int coop = 0;
+        KL_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        int cap = 4;
+        if (const char* e = std::getenv("KLSA_SOLVE_CTAS_PER_SM")) cap = std::max(1, std::atoi(e));
+        const void* fns[3] = {(const void*)mf_solve_persistent_kernel<T, 1>, (const void*)mf_solve_persistent_kernel<T, 2>,
+                              (const void*)mf_solve_persistent_kernel<T, 4>};
+        const int nrs[3] = {1, 2, 4};
+        for (int v = 0; v < 3; ++v) {
+            (void)nrs;
+            ps_smem_[v] = 0;
+            int bps = 0;
+            KL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fns[v], SOLVE_THREADS, ps_smem_[v]));
+            ps_grid_[v] = coop ? sms * std::min(bps, cap) : 0;
+        }
+    }
     const int gsm = (int)gemm_smem(sizeof(T));
     KL_CUDA(cudaFuncSetAttribute(mf_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
     KL_CUDA(cudaFuncSetAttribute(mf_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
@@ -1017,6 +1341,7 @@ void MultifrontalT<T>::replay(GraphSlot& slot, const void* key0, const void* key
 
 template <class T>
 MultifrontalT<T>::~MultifrontalT() {
+    delete solve_levels_;
     for (GraphSlot* s : {&fact_graph_, &solve_graph_[0], &solve_graph_[1], &solve_graph_[2]})
         if (s->exec) cudaGraphExecDestroy(s->exec);
     if (ev_panel_) cudaEventDestroy(ev_panel_);
@@ -1175,6 +1500,34 @@ void MultifrontalT<T>::solve_impl(const T* d_b, T* d_x) {
 }
 
 template <class T>
+template <int NR>
+void MultifrontalT<T>::solve_persistent(const T* d_b, T* d_x) {
+    const int v = NR == 1 ? 0 : NR == 2 ? 1 : 2;
+    SolveArgs<T> a;
+    a.n = n_;
+    a.items = items_.get();
+    a.f = d_f_.get(); a.k = d_k_.get(); a.own = d_own_.get(); a.child0 = d_child0_.get(); a.child1 = d_child1_.get();
+    a.halo = d_halo_.get(); a.inv = d_inv_.get();
+    a.front_off = d_front_off_.get(); a.upd_off = d_upd_off_.get(); a.xinv_off = d_xinv_off_.get();
+    a.halo_off = d_halo_off_.get(); a.inv_off = d_inv_off_.get();
+    a.pool = pool_.get(); a.xinv = xinv_.get(); a.D = D_.get(); a.b = d_b;
+    a.x = d_x; a.z = z_.get(); a.w = y_.get(); a.upd = upd_.get();
+    void* args[2] = {&a, solve_levels_};
+    KL_CUDA(cudaLaunchCooperativeKernel((const void*)mf_solve_persistent_kernel<T, NR>, dim3(ps_grid_[v]),
+                                        dim3(SOLVE_THREADS), args, ps_smem_[v], stream_));
+    count_launch();
+}
+
+template <class T>
+bool MultifrontalT<T>::persistent_solve_enabled() const {
+    static const bool levels = [] {
+        const char* e = std::getenv("KLSA_SOLVE_KERNEL");
+        return e && std::string(e) == "levels";
+    }();
+    return !levels && persistent_ok_ && ps_grid_[0] > 0;
+}
+
+template <class T>
 void MultifrontalT<T>::enqueue_factorize(const T* d_vals) {
     ++generation_;
     factorize_launches(d_vals);
@@ -1185,6 +1538,16 @@ void MultifrontalT<T>::enqueue_solve(const T* d_b, T* d_x) { solve_impl<1>(d_b, 
 
 template <class T>
 void MultifrontalT<T>::solve(const T* d_b, T* d_x, int nrhs) {
+    // the persistent solve zeroes x before it reads b: an in-place call takes the level path
+    if (persistent_solve_enabled() && d_b != d_x) {
+        switch (nrhs) {
+            case 1: solve_persistent<1>(d_b, d_x); return;
+            case 2: solve_persistent<2>(d_b, d_x); return;
+            case 3: solve_persistent<2>(d_b, d_x); solve_persistent<1>(d_b + 2 * (size_t)n_, d_x + 2 * (size_t)n_); return;
+            case 4: solve_persistent<4>(d_b, d_x); return;
+            default: throw std::invalid_argument("multifrontal solve: nrhs out of range");
+        }
+    }
     switch (nrhs) {
         case 1: replay(solve_graph_[0], d_b, d_x, [&] { solve_impl<1>(d_b, d_x); }); break;
         case 2: replay(solve_graph_[1], d_b, d_x, [&] { solve_impl<2>(d_b, d_x); }); break;

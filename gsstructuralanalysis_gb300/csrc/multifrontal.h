@@ -21,6 +21,14 @@
 
 namespace klsa {
 
+// Per-level tile lists of the persistent triangular solve (offsets into the work-item pool):
+// own = lower-triangular 64x64 tiles of X = L11^-1, halo = 64x64 tiles of L21.
+constexpr int MF_MAX_LEVELS = 48;
+struct SolveLevels {
+    int nlev;
+    int own_off[MF_MAX_LEVELS], own_cnt[MF_MAX_LEVELS], halo_off[MF_MAX_LEVELS], halo_cnt[MF_MAX_LEVELS];
+};
+
 constexpr int MF_NB = 64;          // tile size
 constexpr int MF_MAX_RHS = 4;
 
@@ -75,6 +83,16 @@ private:
     template <class Fn> void replay(GraphSlot& slot, const void* key0, const void* key1, Fn&& launches);
     void factorize_launches(const T* d_vals);
     template <int NR> void solve_impl(const T* d_b, T* d_x);
+    // one cooperative launch per solve (all levels, both sweeps); the five-launch-per-level
+    // solve_impl stays for graph-captured callers and as the "levels" variant
+    template <int NR> void solve_persistent(const T* d_b, T* d_x);
+    bool persistent_solve_enabled() const;
+    SolveLevels* solve_levels_ = nullptr;
+    DevBuf<int64_t> d_inv_off_;
+    DevBuf<int> d_inv_;
+    int ps_grid_[3] = {0, 0, 0};
+    bool persistent_ok_ = true;
+    size_t ps_smem_[3] = {0, 0, 0};
     GraphSlot fact_graph_, solve_graph_[3];
     cudaStream_t stream_;
     cudaStream_t side_ = nullptr;          // look-ahead stream of the off-critical-path updates

@@ -81,6 +81,13 @@ int klsa_al_residual(klsa_problem* prob, const double* x, double lambda, double*
  * precision 0: FP32 element integration, 1: FP64.  rowptr has ndof+1 entries. */
 int klsa_jacobian_csr(klsa_problem* prob, const double* x, int precision, int64_t* rowptr, int32_t* cols,
                       double* vals);
+/* dJacobian_t (Types.h:91-92): the Jacobian with the solution update as an extra argument, as
+ * gsALMBase::_computeJacobian (gsALMBase.hpp:214-223) and gsStaticNewton::_computeJacobian
+ * (gsStaticNewton.hpp:205-212) call it.  Same output as klsa_jacobian_csr at x: for the SVK
+ * material the tangent does not depend on dx, exactly as the reference wraps a Jacobian_t into
+ * its dJacobian_t (gsALMBase.h:57-60, gsStaticNewton.h:79-82).  dx: ndof values (must be given). */
+int klsa_djacobian_csr(klsa_problem* prob, const double* x, const double* dx, int precision, int64_t* rowptr,
+                       int32_t* cols, double* vals);
 /* Mass_t (Types.h:71): consistent mass matrix int rho t N_A N_B dA, same CSR pattern. */
 int klsa_mass_csr(klsa_problem* prob, int64_t* rowptr, int32_t* cols, double* vals);
 

@@ -82,3 +82,18 @@ def test_multifrontal_solve(lib, oracle_mod, name, make):
     assert s2.compute_jacobian(x) == 0
     y2 = s2.solve(b)
     assert np.linalg.norm(y2 - ref) / np.linalg.norm(ref) < 1e-9
+
+
+def test_djacobian_matches(lib, oracle_mod):
+    """dJacobian_t (gsStructuralAnalysisTypes.h:91-92), called with a solution update as
+    gsALMBase::_computeJacobian does (gsALMBase.hpp:214-223): the oracle's tangent at x, for
+    any update (the reference wraps a Jacobian_t the same way, gsALMBase.h:57-60)."""
+    prob, gp, oa = _pair(lib, oracle_mod, CASES[1][1])
+    rng = np.random.default_rng(5)
+    x = 1e-2 * rng.standard_normal(gp.ndof)
+    Kr = oa.jacobian(x)
+    rowmax = np.abs(Kr.toarray()).max(axis=1, keepdims=True)
+    for dx in (np.zeros(gp.ndof), 1e-3 * rng.standard_normal(gp.ndof)):
+        K = gp.djacobian(x, dx)
+        assert K.nnz == Kr.nnz
+        assert np.max(np.abs((K - Kr).toarray()) / rowmax) < 1e-10
