@@ -20,6 +20,7 @@
 #include <utility>
 
 #include "batch.h"
+#include "df64.cuh"
 #include "problem.h"
 
 namespace klsa {
@@ -382,6 +383,164 @@ __device__ __forceinline__ void fint_group(int grp, int nel, int m1, int n1, int
     }
 }
 
+// The same element group with the two long accumulations -- the displacement derivatives at a
+// Gauss point (sum over control points of N u) and the control-point forces (sum over Gauss
+// points of N times the point's stress terms) -- in double-float arithmetic (df64.cuh) on the
+// FP32 pipes, from basis tables pre-split into FP32 hi/lo pairs (tab1s, tab2s).  The Gauss-point
+// state (deformed geometry, strains, stress resultants) stays FP64.  The sums carry about 48
+// significant bits: the residual's relative error stays near 1e-14, six orders of magnitude
+// under the 1e-8 force tolerance it decides.
+template <int P>
+__device__ __forceinline__ void fint_group_df(int grp, int nel, int m1, int n1, int ncp, int nq,
+                                              const float2* __restrict__ tab1s, const float2* __restrict__ tab2s,
+                                              const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                              double tm, double tb, double* __restrict__ elemR, df2 (*usw)[3],
+                                              df2 (*qsw)[15], int lane) {
+    constexpr int NB1 = P + 1, NB = NB1 * NB1, D = 3 * NB;
+    const int nqp = nq * nq;
+    const int lpe = NB > nqp ? NB : nqp;
+    const int es = 32 / lpe;
+    const int slot = lane / lpe, idx = lane % lpe;
+    const int e = grp * es + slot;
+    const bool live = slot < es && e < nel;
+    const int e1 = live ? e % m1 : 0, e2 = live ? e / m1 : 0;
+    if (live && idx < NB) {
+        const int A = (e2 + idx / NB1) * n1 + (e1 + idx % NB1);
+        usw[slot * NB + idx][0] = df_split(ufull[A]);
+        usw[slot * NB + idx][1] = df_split(ufull[ncp + A]);
+        usw[slot * NB + idx][2] = df_split(ufull[2 * ncp + A]);
+    }
+    __syncwarp();
+    if (live && idx < nqp) {
+        const int q1 = idx % nq, q2 = idx / nq;
+        df2 t1[3 * NB1], t2[3 * NB1];
+        const float2* r1 = tab1s + (((size_t)e1 * nq + q1) * 3) * NB1;
+        const float2* r2 = tab2s + (((size_t)e2 * nq + q2) * 3) * NB1;
+#pragma unroll
+        for (int k = 0; k < 3 * NB1; ++k) {
+            const float2 a = r1[k], b = r2[k];
+            t1[k] = {a.x, a.y};
+            t2[k] = {b.x, b.y};
+        }
+        df2 du[15];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) du[k] = {0.f, 0.f};
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            const int a = c % NB1, b = c / NB1;
+            const df2 Ns[5] = {df_mul(t1[NB1 + a], t2[b]), df_mul(t1[a], t2[NB1 + b]), df_mul(t1[2 * NB1 + a], t2[b]),
+                               df_mul(t1[a], t2[2 * NB1 + b]), df_mul(t1[NB1 + a], t2[NB1 + b])};
+            const df2* u = usw[slot * NB + c];
+#pragma unroll
+            for (int g = 0; g < 5; ++g) {
+                df_fma(du[3 * g], Ns[g], u[0]);
+                df_fma(du[3 * g + 1], Ns[g], u[1]);
+                df_fma(du[3 * g + 2], Ns[g], u[2]);
+            }
+        }
+        double dud[15];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) dud[k] = df_to_double(du[k]);
+        const double* geo = qpgeo + ((size_t)e * nqp + idx) * 22;
+        QPState<double> st;
+        qp_state<P, double>(geo, dud, tm, tb, st);
+        const double dV = st.dV;
+        V3T<double> u1 = cross3(st.a2, st.w), u2 = cross3(st.w, st.a1);
+        df2* o = qsw[slot * nqp + idx];
+        o[0] = df_split(dV * (st.n[0] * st.a1.x + st.n[2] * st.a2.x - u1.x * st.il));
+        o[1] = df_split(dV * (st.n[0] * st.a1.y + st.n[2] * st.a2.y - u1.y * st.il));
+        o[2] = df_split(dV * (st.n[0] * st.a1.z + st.n[2] * st.a2.z - u1.z * st.il));
+        o[3] = df_split(dV * (st.n[1] * st.a2.x + st.n[2] * st.a1.x - u2.x * st.il));
+        o[4] = df_split(dV * (st.n[1] * st.a2.y + st.n[2] * st.a1.y - u2.y * st.il));
+        o[5] = df_split(dV * (st.n[1] * st.a2.z + st.n[2] * st.a1.z - u2.z * st.il));
+        const double s11 = dV * st.m[0], s22 = dV * st.m[1], s12 = 2.0 * dV * st.m[2];
+        o[6] = df_split(s11 * st.a3.x); o[7] = df_split(s11 * st.a3.y); o[8] = df_split(s11 * st.a3.z);
+        o[9] = df_split(s22 * st.a3.x); o[10] = df_split(s22 * st.a3.y); o[11] = df_split(s22 * st.a3.z);
+        o[12] = df_split(s12 * st.a3.x); o[13] = df_split(s12 * st.a3.y); o[14] = df_split(s12 * st.a3.z);
+    }
+    __syncwarp();
+    if (live && idx < NB) {
+        const int a = idx % NB1, b = idx / NB1;
+        df2 f[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (int qq = 0; qq < nqp; ++qq) {
+            const int q1 = qq % nq, q2 = qq / nq;
+            const float2* r1 = tab1s + (((size_t)e1 * nq + q1) * 3) * NB1;
+            const float2* r2 = tab2s + (((size_t)e2 * nq + q2) * 3) * NB1;
+            const float2 v0 = r1[a], v1 = r1[NB1 + a], v2 = r1[2 * NB1 + a];
+            const float2 w0 = r2[b], w1 = r2[NB1 + b], w2 = r2[2 * NB1 + b];
+            const df2 t10 = {v0.x, v0.y}, t11 = {v1.x, v1.y}, t12 = {v2.x, v2.y};
+            const df2 t20 = {w0.x, w0.y}, t21 = {w1.x, w1.y}, t22 = {w2.x, w2.y};
+            const df2 N1 = df_mul(t11, t20), N2 = df_mul(t10, t21), N11 = df_mul(t12, t20), N22 = df_mul(t10, t22),
+                      N12 = df_mul(t11, t21);
+            const df2* o = qsw[slot * nqp + qq];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                df_fma(f[i], N1, o[i]);
+                df_fma(f[i], N2, o[3 + i]);
+                df_fms(f[i], N11, o[6 + i]);
+                df_fms(f[i], N22, o[9 + i]);
+                df_fms(f[i], N12, o[12 + i]);
+            }
+        }
+        for (int i = 0; i < 3; ++i) elemR[(size_t)e * D + 3 * idx + i] = df_to_double(f[i]);
+    }
+}
+
+// FP32 pairs underflow below ~1e-38 (and lose their low word below ~1e-31): a warp whose
+// elements' displacements are all nonzero and tiny (largest |u| under 1e-20, e.g. an iteration
+// converging to the undeformed state) evaluates its elements in plain FP64 instead.
+template <int P>
+__device__ __forceinline__ bool fint_group_tiny(int grp, int nel, int m1, int n1, int ncp, int nq,
+                                                const double* __restrict__ ufull, int lane) {
+    constexpr int NB1 = P + 1, NB = NB1 * NB1;
+    const int lpe = NB > nq * nq ? NB : nq * nq;
+    const int slot = lane / lpe, idx = lane % lpe;
+    const int e = grp * (32 / lpe) + slot;
+    double m = 0.0;
+    if (slot < 32 / lpe && e < nel && idx < NB) {
+        const int e1 = e % m1, e2 = e / m1;
+        const int A = (e2 + idx / NB1) * n1 + (e1 + idx % NB1);
+        m = fmax(fabs(ufull[A]), fmax(fabs(ufull[ncp + A]), fabs(ufull[2 * ncp + A])));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    return m > 0.0 && m < 1e-20;
+}
+
+// shared memory of one warp, for either variant of the element group
+union FintShared {
+    struct { double us[32][3]; double qs[32][QSTATE]; } d;
+    struct { df2 us[32][3]; df2 qs[32][15]; } f;
+};
+
+template <int P>
+__device__ __forceinline__ void fint_group_auto(int grp, int nel, int m1, int n1, int ncp, int nq,
+                                                const double* __restrict__ tab1, const double* __restrict__ tab2,
+                                                const float2* __restrict__ tab1s, const float2* __restrict__ tab2s,
+                                                const double* __restrict__ qpgeo, const double* __restrict__ ufull,
+                                                double tm, double tb, double* __restrict__ elemR, FintShared& sh,
+                                                int lane) {
+    if (fint_group_tiny<P>(grp, nel, m1, n1, ncp, nq, ufull, lane))
+        fint_group<P>(grp, nel, m1, n1, ncp, nq, tab1, tab2, qpgeo, ufull, tm, tb, elemR, sh.d.us, sh.d.qs, lane);
+    else
+        fint_group_df<P>(grp, nel, m1, n1, ncp, nq, tab1s, tab2s, qpgeo, ufull, tm, tb, elemR, sh.f.us, sh.f.qs, lane);
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) kl_fint_df_kernel(int nel, int m1, int n1, int ncp, int nq,
+                                                         const double* __restrict__ tab1,
+                                                         const double* __restrict__ tab2,
+                                                         const float2* __restrict__ tab1s,
+                                                         const float2* __restrict__ tab2s,
+                                                         const double* __restrict__ qpgeo,
+                                                         const double* __restrict__ ufull, double tm, double tb,
+                                                         double* __restrict__ elemR) {
+    __shared__ FintShared sh[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    fint_group_auto<P>(blockIdx.x * 4 + warp, nel, m1, n1, ncp, nq, tab1, tab2, tab1s, tab2s, qpgeo, ufull, tm, tb,
+                       elemR, sh[warp], lane);
+}
+
 template <int P>
 __global__ void __launch_bounds__(128) kl_fint_kernel(int nel, int m1, int n1, int ncp, int nq,
                                                       const double* __restrict__ tab1, const double* __restrict__ tab2,
@@ -400,15 +559,14 @@ template <int P>
 __global__ void __launch_bounds__(128) kl_fint_batch_kernel(int ninst, const int* __restrict__ insts,
                                                             const int* __restrict__ grp_off,
                                                             const BatchInst* __restrict__ desc) {
-    __shared__ double us[4][32][3];
-    __shared__ double qs[4][32][QSTATE];
+    __shared__ FintShared sh[4];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int total = grp_off[ninst];
     for (int g = blockIdx.x * 4 + warp; g < total; g += gridDim.x * 4) {
         const int k = find_segment(grp_off, ninst, g);
         const BatchInst& d = desc[insts[k]];
-        fint_group<P>(g - grp_off[k], d.nel, d.m1, d.n1, d.ncp, d.nq, d.tab1, d.tab2, d.qpgeo, d.ufull, d.tm, d.tb,
-                      d.elemR, us[warp], qs[warp], lane);
+        fint_group_auto<P>(g - grp_off[k], d.nel, d.m1, d.n1, d.ncp, d.nq, d.tab1, d.tab2, d.tab1s, d.tab2s, d.qpgeo,
+                           d.ufull, d.tm, d.tb, d.elemR, sh[warp], lane);
         __syncwarp();
     }
 }
@@ -670,8 +828,14 @@ void Problem::internal_force(double* d_out) {
     int grid = ceil_div(nel, 4 * es);
     double tm = t, tb = t * t * t / 12.0;
     switch (p) {
-        case 2: kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get()); break;
-        case 3: kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get()); break;
+        case 2:
+            if (fint_fp64) kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get());
+            else kl_fint_df_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_tab1s.get(), d_tab2s.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get());
+            break;
+        case 3:
+            if (fint_fp64) kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get());
+            else kl_fint_df_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_tab1s.get(), d_tab2s.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, d_elemR.get());
+            break;
         default: throw std::invalid_argument("unsupported degree");
     }
     count_launch();
@@ -686,8 +850,14 @@ void Problem::internal_force_elements(double* elemR) {
     int grid = ceil_div(nel, 4 * (32 / lpe));
     double tm = t, tb = t * t * t / 12.0;
     switch (p) {
-        case 2: kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR); break;
-        case 3: kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR); break;
+        case 2:
+            if (fint_fp64) kl_fint_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR);
+            else kl_fint_df_kernel<2><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_tab1s.get(), d_tab2s.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR);
+            break;
+        case 3:
+            if (fint_fp64) kl_fint_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR);
+            else kl_fint_df_kernel<3><<<grid, 128, 0, stream>>>(nel, m1, n1, ncp, nq, d_tab1.get(), d_tab2.get(), d_tab1s.get(), d_tab2s.get(), d_qpgeo.get(), d_ufull.get(), tm, tb, elemR);
+            break;
         default: throw std::invalid_argument("unsupported degree");
     }
     count_launch();

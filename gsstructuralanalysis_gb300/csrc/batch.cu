@@ -206,7 +206,7 @@ BatchedProblem::BatchedProblem(const std::vector<const klsa_patch_desc*>& descs)
         P.d_elemKf.alloc((size_t)P.nel * D * D);
         P.d_elemR.alloc((size_t)P.nel * D);
         BatchInst& b = desc[i];
-        b.tab1 = P.d_tab1.get(); b.tab2 = P.d_tab2.get(); b.qpgeo = P.d_qpgeo.get(); b.ufull = P.d_ufull.get();
+        b.tab1 = P.d_tab1.get(); b.tab2 = P.d_tab2.get(); b.tab1s = P.d_tab1s.get(); b.tab2s = P.d_tab2s.get(); b.qpgeo = P.d_qpgeo.get(); b.ufull = P.d_ufull.get();
         b.elemK = P.d_elemKf.get(); b.elemR = P.d_elemR.get(); b.int2full = P.d_int2full.get();
         b.p = P.p; b.nq = P.nq; b.m1 = P.m1; b.m2 = P.m2; b.n1 = P.n1; b.ncp = P.ncp; b.nel = P.nel;
         b.nfree = P.nfree; b.dof_off = dof_off[i];

@@ -28,6 +28,8 @@ namespace klsa {
 struct BatchInst {
     const double* tab1;
     const double* tab2;
+    const float2* tab1s;     // the same tables as FP32 hi/lo pairs (double-float internal force)
+    const float2* tab2s;
     const double* qpgeo;
     double* ufull;
     float* elemK;

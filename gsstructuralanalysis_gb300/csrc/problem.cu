@@ -1,5 +1,6 @@
 // problem.cu -- host set-up of a patch problem: B-spline tables, Gauss-point geometry,
 // dof maps, nested-dissection numbering, CSR pattern, external loads.
+#include <cstdlib>
 #include "problem.h"
 
 #include <algorithm>
@@ -321,6 +322,19 @@ Problem::Problem(const klsa_patch_desc& d) {
     std::vector<float> t1f(tab1.begin(), tab1.end()), t2f(tab2.begin(), tab2.end());
     d_tab1f.upload(t1f, stream);
     d_tab2f.upload(t2f, stream);
+    {
+        auto split = [](const std::vector<double>& t) {
+            std::vector<float2> o(t.size());
+            for (size_t i = 0; i < t.size(); ++i) {
+                const float h = (float)t[i];
+                o[i] = make_float2(h, (float)(t[i] - (double)h));
+            }
+            return o;
+        };
+        d_tab1s.upload(split(tab1), stream);
+        d_tab2s.upload(split(tab2), stream);
+    }
+    if (const char* e = std::getenv("KLSA_RESIDUAL_FP64")) fint_fp64 = e[0] == '1';
     d_qpgeo.upload(qpgeo, stream);
     d_int2full.upload(tree.int2full, stream);
     d_full2int.upload(tree.full2int, stream);

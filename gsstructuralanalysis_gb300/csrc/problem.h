@@ -42,6 +42,8 @@ struct Problem {
     cudaStream_t stream = nullptr;
     DevBuf<double> d_tab1, d_tab2, d_qpgeo;
     DevBuf<float> d_tab1f, d_tab2f;
+    DevBuf<float2> d_tab1s, d_tab2s;       // basis tables as FP32 hi/lo pairs (double-float residual)
+    bool fint_fp64 = false;                // internal force: plain FP64 kernel instead of double-float sums
     DevBuf<int> d_int2full, d_full2int, d_pub2int, d_int2pub;
     DevBuf<int> d_rowptr, d_cols;
     DevBuf<double> d_F;                // external load, internal order

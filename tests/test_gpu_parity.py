@@ -97,3 +97,26 @@ def test_djacobian_matches(lib, oracle_mod):
         K = gp.djacobian(x, dx)
         assert K.nnz == Kr.nnz
         assert np.max(np.abs((K - Kr).toarray()) / rowmax) < 1e-10
+
+
+@pytest.mark.parametrize("m,p", [(128, 2), (48, 3)])
+def test_residual_double_float_matches_fp64_kernel(lib, m, p, monkeypatch):
+    """The internal force sums in double-float arithmetic on the FP32 pipes (the default) against
+    the plain FP64 kernel (KLSA_RESIDUAL_FP64=1, read when a problem is created), at the
+    headline's 50k dofs and at degree 3: displacements of the size met on the path, near zero
+    (where the membrane strains are smallest), and vanishingly small (an iteration converging to
+    the undeformed state: the kernel keeps those elements on FP64 sums, since FP32 pairs
+    underflow)."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=m, p=p, load=1.0)
+    gp_df = G.Problem(prob)
+    monkeypatch.setenv("KLSA_RESIDUAL_FP64", "1")
+    gp_64 = G.Problem(prob)
+    monkeypatch.delenv("KLSA_RESIDUAL_FP64")
+    rng = np.random.default_rng(9)
+    for scale in (1e-2, 1e-7, 1e-30, 1e-150):
+        x = scale * rng.standard_normal(gp_df.ndof)
+        r_df, r_64 = gp_df.al_residual(x, 0.7), gp_64.al_residual(x, 0.7)
+        assert np.linalg.norm(r_df - r_64) <= 1e-12 * np.linalg.norm(r_64), scale
+        f_df, f_64 = gp_df.al_residual(x, 0.0), gp_64.al_residual(x, 0.0)   # Fint alone
+        assert np.linalg.norm(f_df - f_64) <= 1e-12 * np.linalg.norm(f_64), scale
