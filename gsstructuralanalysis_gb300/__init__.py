@@ -47,6 +47,8 @@ SIGNATURES = {
     "klsa_al_residual_noalloc": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_vp]),
     "klsa_jacobian_csr": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
     "klsa_djacobian_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "klsa_eigen_dense": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
+    "klsa_eigen_power": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
     "klsa_mass_csr": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_options_create": (_c_vp, []),
     "klsa_options_destroy": (None, [_c_vp]),
@@ -557,6 +559,28 @@ def modal(problem: Problem, nev: int, shift: float = 0.0, options: dict | None =
     vecs = np.zeros((nev, problem.ndof)) if vectors else None
     st = _check(_lib.klsa_modal(problem.h, o.h, int(nev), float(shift), _ptr(vals), _ptr(vecs)))
     return st, vals, vecs
+
+
+def eigen_dense(problem: Problem, kind: str = "modal", scaling: float = 1.0, options: dict | None = None,
+                vectors: bool = True):
+    """gsEigenProblemBase::compute: all eigenpairs of the modal or buckling pencil (dense sizes)."""
+    o = Options(options)
+    n = problem.ndof
+    vals = np.zeros(n)
+    vecs = np.zeros((n, n)) if vectors else None
+    st = _check(_lib.klsa_eigen_dense(problem.h, o.h, 0 if kind == "modal" else 1, float(scaling), _ptr(vals),
+                                      _ptr(vecs)))
+    return st, vals, vecs
+
+
+def eigen_power(problem: Problem, kind: str = "modal", scaling: float = 1.0, options: dict | None = None):
+    """gsEigenProblemBase::computePower: the pair of smallest |lambda| by power iteration."""
+    o = Options(options)
+    val = np.zeros(1)
+    vec = np.zeros(problem.ndof)
+    st = _check(_lib.klsa_eigen_power(problem.h, o.h, 0 if kind == "modal" else 1, float(scaling), _ptr(val),
+                                      _ptr(vec)))
+    return st, float(val[0]), vec
 
 
 class APALM:

@@ -746,6 +746,23 @@ int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shif
     return guarded([&] { return modal_gpu(*prob->P, opt ? opt->o : Options(), nev, shift, values, vectors); });
 }
 
+int klsa_eigen_dense(klsa_problem* prob, const klsa_options* opt, int kind, double scaling, double* values,
+                     double* vectors) {
+    if (!prob || !values || (kind != 0 && kind != 1)) return KLSA_INVALID_ARGUMENT;
+    if (prob->P->nfree > 4096) {
+        klsa_set_error("klsa_eigen_dense: the dense eigensolver holds n x n matrices; at most 4096 dofs (use "
+                       "klsa_modal / klsa_buckling for sparse sizes)");
+        return KLSA_INVALID_ARGUMENT;
+    }
+    return guarded([&] { return dense_gpu(*prob->P, opt ? opt->o : Options(), kind, scaling, values, vectors); });
+}
+
+int klsa_eigen_power(klsa_problem* prob, const klsa_options* opt, int kind, double scaling, double* value,
+                     double* vector) {
+    if (!prob || !value || (kind != 0 && kind != 1)) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] { return power_gpu(*prob->P, opt ? opt->o : Options(), kind, scaling, value, vector); });
+}
+
 // ---- adaptive parallel arc-length method -----------------------------------------------------
 int klsa_apalm_create(klsa_alm* alm, const klsa_options* opt, klsa_apalm** out) {
     if (!alm || !out) return KLSA_INVALID_ARGUMENT;

@@ -20,6 +20,14 @@ int modal_gpu(Problem& P, const Options& opt, int nev, double shift, double* val
 // factorisation workspace (the caller's factorisation is overwritten).
 int standard_eigs_gpu(Problem& P, const double* valsA, int nev, int ncv_fac, double shift, double tol, double* values);
 
+// gsEigenProblemBase::computePower of the modal (kind 0) or buckling (kind 1) pencil: the
+// eigenpair of smallest |lambda| by power iteration on A^-1 B (gsEigenProblemBase.hpp:218-258).
+int power_gpu(Problem& P, const Options& opt, int kind, double scaling, double* value, double* vector);
+
+// gsEigenProblemBase::compute of the modal (kind 0) or buckling (kind 1) pencil: every eigenpair
+// of the dense pencil (gsEigenProblemBase.hpp:21-50).  values: ndof, vectors: ndof x ndof.
+int dense_gpu(Problem& P, const Options& opt, int kind, double scaling, double* values, double* vectors);
+
 // y = A x with an explicit FP64 value array over the problem's CSR pattern
 void spmv_vals(const Problem& P, const double* vals, const double* x, double* y);
 

@@ -225,6 +225,18 @@ int klsa_buckling(klsa_problem* prob, const klsa_options* opt, int nev, double s
 /* Modal (gsModalSolver.h:46-51): eigenpairs of K v = omega^2 M v about ``shift``. */
 int klsa_modal(klsa_problem* prob, const klsa_options* opt, int nev, double shift, double* values,
                double* vectors);
+/* gsEigenProblemBase::compute (gsEigenProblemBase.hpp:21-50): every eigenpair of the dense pencil
+ * -- kind 0 gsModalSolver (K, M), kind 1 gsBucklingSolver (K_L, K(u_L) - K_L, u_L = K_L^-1 scaling F)
+ * -- with the "shift" option applied as A - shift B and added back; eigenvalues ascending,
+ * vectors B-normalised.  values: ndof, vectors: ndof x ndof (or NULL).  For dense sizes
+ * (at most 4096 dofs); B must be positive definite (else KLSA_SOLVER_ERROR). */
+int klsa_eigen_dense(klsa_problem* prob, const klsa_options* opt, int kind, double scaling, double* values,
+                     double* vectors);
+/* gsEigenProblemBase::computePower (gsEigenProblemBase.hpp:218-258): the eigenpair of smallest
+ * |lambda| by power iteration on A^-1 B from the all-ones vector ("tolerance" option, at most 100
+ * steps, KLSA_NOT_CONVERGED after the last).  value: 1, vector: ndof (Euclidean-normalised) or NULL. */
+int klsa_eigen_power(klsa_problem* prob, const klsa_options* opt, int kind, double scaling, double* value,
+                     double* vector);
 
 /* ---- adaptive parallel arc-length method (gsALMSolvers/gsAPALM.hpp, gsAPALMData.hpp) -----
  * Over an arc-length object of method Crisfield or Riks (the methods with a distance).  The jobs

@@ -18,6 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import ref_cases as C  # noqa: E402
 
+from gsstructuralanalysis_gb300 import problems as P  # noqa: E402
+
 pytestmark = pytest.mark.gpu
 FIX = np.load(os.path.join(HERE, "golden", "ref_solvers.npz"))
 EXACT = {"FrontPrecision": 64}
@@ -67,3 +69,65 @@ def test_static_newton_case_matches_reference(lib, name):
         assert st.solve() == int(FIX[f"{name}/status"][k]) == 0, k
         assert _rel(st.solution(), FIX[f"{name}/U"][k]) < 1e-8, k
         assert st.iterations() == int(FIX[f"{name}/iterations"][k]), k
+
+
+def test_dense_compute_matches_reference(lib, oracle_mod):
+    """gsEigenProblemBase::compute of gsModalSolver: every eigenvalue as the reference's own
+    compute() gives it (Eigen's GeneralizedSelfAdjointEigenSolver behind the test shim's dense
+    solver), with and without the shift option; the vectors are B-normalised eigenvectors of
+    the oracle's pencil (sign and the basis inside a repeated eigenvalue are free)."""
+    import gsstructuralanalysis_gb300 as G
+    case = C.CASES["modal_dense"]
+    prob = C.build(case)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    ref = FIX["modal_dense/values"]
+    for shift in (0.0, 0.5 * ref[0]):
+        st, vals, vecs = G.eigen_dense(gp, "modal", options=dict(case["options"], shift=shift))
+        assert st == 0
+        np.testing.assert_allclose(vals, ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
+    K, M = oa.linear(), oa.mass()
+    for lam, v in zip(vals, vecs):
+        assert np.linalg.norm(K @ v - lam * (M @ v)) <= 1e-8 * np.linalg.norm(K @ v)
+        assert abs(v @ (M @ v) - 1.0) <= 1e-10
+
+
+def test_power_method_matches_reference(lib):
+    """gsEigenProblemBase::computePower: the same iterates as the reference's (all-ones start,
+    Euclidean normalisation), so the same value and vector."""
+    import gsstructuralanalysis_gb300 as G
+    case = C.CASES["modal_dense"]
+    gp = G.Problem(C.build(case))
+    st, val, vec = G.eigen_power(gp, "modal", options=case["options"])
+    assert st == int(FIX["modal_dense/power_status"][0])
+    assert abs(val - float(FIX["modal_dense/power_value"][0])) <= 1e-10 * abs(val)
+    assert np.linalg.norm(vec - FIX["modal_dense/power_vector"]) <= 1e-8
+
+
+def test_power_method_buckling_pencil(lib):
+    """computePower of gsBucklingSolver's pencil on the simply supported square plate: the
+    critical load factor (the smallest |lambda|, well separated from the next one), which the
+    shift-invert Lanczos (Buckling mode) finds too.  The reference load is a tension, so lambda
+    (and the dominant eigenvalue of A^-1 B) is positive; under a compressive reference load it is
+    negative, the power iterates flip sign every step and, as in the reference, the method stops
+    NotConverged after 100 steps."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.flat_plate(m=8, p=3, E=1.0, nu=0.3, t=0.01, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True
+    fixed[0, ii == 0] = True
+    fixed[1, 0] = True
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, 1.0, 0.0, 0.0]])
+    gp = G.Problem(prob)
+    s = 1e-8
+    st, val, _ = G.eigen_power(gp, "buckling", scaling=s, options={"tolerance": 1e-12})
+    assert st == 0
+    st, vals, _ = G.buckling(gp, 3, shift=1.05 * val, scaling=s, vectors=False)
+    assert st == 0
+    lam = vals[np.argmin(np.abs(vals))]
+    assert abs(val - lam) <= 1e-8 * abs(lam)
+    D = 0.01 ** 3 / (12 * (1 - 0.3 ** 2))
+    assert abs(val * s / (4 * np.pi ** 2 * D) - 1) < 1e-4         # q_cr = 4 pi^2 D / b^2
