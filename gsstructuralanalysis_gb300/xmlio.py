@@ -179,7 +179,8 @@ def _geometry(root, ids):
     if typ == "TensorNurbs2":
         w = _numbers(basis.find("weights").text)
         if not np.allclose(w, 1.0):
-            raise NotImplementedError("rational (NURBS) geometry with non-unit weights")
+            raise NotImplementedError("rational (NURBS) geometry with non-unit weights: the device kernels "
+                                      "evaluate a polynomial B-spline basis")
         basis = basis.find("Basis")
     elif typ != "TensorBSpline2":
         raise NotImplementedError(f"geometry type {typ}")
@@ -257,10 +258,40 @@ def _corner(corner, n1, n2):
     return {1: 0, 2: n1 - 1, 3: (n2 - 1) * n1, 4: n2 * n1 - 1}[corner]
 
 
+def _parse(path: str):
+    """Root element of a gsFileData file.  gismo's reader accepts an XML declaration after a
+    leading comment (filedata/surface/scordelis_lo_roof_shallow.xml starts with one); a strict
+    XML parser does not, so the declaration is dropped wherever it stands."""
+    import re
+    with open(path, "r", encoding="utf-8") as f:
+        text = f.read()
+    return ET.fromstring(re.sub(r"<\?xml[^>]*\?>", "", text))
+
+
+def read_geometry(path: str, elevate: int = 0, refine: int = 0):
+    """The geometry of a file that holds only a surface (gsReadFile<>(file, mp) on a file with a
+    ``Geometry`` or single-patch ``MultiPatch`` id 0, as benchmarks/benchmark_Roof.cpp:146-157
+    reads filedata/surface/scordelis_lo_roof_shallow.xml), degree-elevated ``elevate`` times and
+    uniformly refined ``refine`` times.  Returns (p, knots1, knots2, ctrl (n1*n2, 3))."""
+    root = _parse(path)
+    U1, U2, p1, p2, ctrl = _geometry(root, _by_id(root))
+    for _ in range(elevate):
+        V1, V2 = elevate_knots(U1), elevate_knots(U2)
+        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1 + 1, p2 + 1)
+        U1, U2, p1, p2 = V1, V2, p1 + 1, p2 + 1
+    for _ in range(refine):
+        V1, V2 = refine_knots(U1), refine_knots(U2)
+        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1, p2)
+        U1, U2 = V1, V2
+    if p1 != p2:
+        raise NotImplementedError(f"degrees {p1} and {p2}: the device path takes equal degrees")
+    return p1, U1, U2, ctrl
+
+
 def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProblem:
     """Read a problem file; ``elevate`` / ``refine`` as the -e / -r arguments of the reference's
     XML solvers (static_shell_XML.cpp:95-104)."""
-    root = ET.parse(path).getroot()
+    root = _parse(path)
     ids = _by_id(root)
     U1, U2, p1, p2, ctrl = _geometry(root, ids)
     for _ in range(elevate):

@@ -105,3 +105,36 @@ def test_unsupported_content_is_rejected(tmp_path, old, new, what):
     f = _edit(tmp_path, "roof_point_load.xml", old, new)
     with pytest.raises(NotImplementedError, match=what):
         X.read(f)
+
+
+def test_reference_roof_geometry_file(oracle_mod):
+    """The reference's own geometry file (filedata/surface/scordelis_lo_roof_shallow.xml, read by
+    benchmarks/benchmark_Roof.cpp:146-157): a degree-2 3x3 net, read despite the comment in
+    front of its XML declaration; elevated and refined it gives exactly the geometry of the
+    golden fixture tests/golden/roof_xml.npz, on which the oracle's Crisfield restatement meets
+    the reference's compiled gsALMCrisfield."""
+    import os
+    import sys
+    from gsstructuralanalysis_gb300 import xmlio
+    ref = os.environ.get("KLSA_REFERENCE_TREE", "/root/reference")
+    path = os.path.join(ref, "filedata/surface/scordelis_lo_roof_shallow.xml")
+    if not os.path.exists(path):
+        pytest.skip("reference tree not present")
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import ref_roof_xml as R
+    p, U1, U2, ctrl = xmlio.read_geometry(path)
+    assert p == 2 and ctrl.shape == (9, 3)
+    fix = np.load(os.path.join(here, "golden", "roof_xml.npz"))
+    p, U1, U2, ctrl = xmlio.read_geometry(path, R.ELEVATE, R.REFINE)
+    assert p == int(fix["p"])
+    np.testing.assert_array_equal(U1, fix["knots1"])
+    np.testing.assert_array_equal(U2, fix["knots2"])
+    np.testing.assert_allclose(ctrl, fix["ctrl"], rtol=0, atol=1e-12)
+    A = oracle_mod.OracleAssembler(R.problem(p, U1, U2, ctrl))
+    alm = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), dict(R.ALM))
+    alm.initialize()
+    for k in range(2):
+        assert alm.step() == 0
+        assert np.linalg.norm(alm.U - fix["U"][k]) <= 1e-10 * np.linalg.norm(fix["U"][k])
+        assert abs(alm.L - fix["L"][k]) <= 1e-10 * abs(fix["L"][k])
