@@ -91,6 +91,7 @@ SIGNATURES = {
     "klsa_apalm_initialize": (_c_int, [_c_vp]),
     "klsa_apalm_add_start": (_c_int, [_c_vp, _c_vp, _c_dbl, _c_dbl]),
     "klsa_apalm_serial_solve": (_c_int, [_c_vp, _c_int]),
+    "klsa_apalm_add_worker": (_c_int, [_c_vp, _c_vp]),
     "klsa_apalm_parallel_solve": (_c_int, [_c_vp]),
     "klsa_apalm_solve": (_c_int, [_c_vp, _c_int]),
     "klsa_apalm_branches": (_c_int, [_c_vp]),
@@ -608,6 +609,12 @@ class APALM:
 
     def serialSolve(self, nsteps=10):
         _check(_lib.klsa_apalm_serial_solve(self.h, int(nsteps)))
+
+    def addWorker(self, alm: "_ALM"):
+        """Another solver (same method and options, its own Problem of the same description) for
+        parallelSolve: the reference's MPI workers as concurrent solvers on one GPU."""
+        self._workers = getattr(self, "_workers", []) + [alm]
+        _check(_lib.klsa_apalm_add_worker(self.h, alm.h))
 
     def parallelSolve(self):
         _check(_lib.klsa_apalm_parallel_solve(self.h))

@@ -1,6 +1,8 @@
 // apalm.cpp -- gsAPALM / gsAPALMData over the device arc-length solver (see apalm.h).
 #include "apalm.h"
 
+#include <future>
+
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -191,22 +193,29 @@ APALM::APALM(ALMGPU& alm, const Options& opt) : alm_(alm), P_(alm.problem()) {
     if (subIntervals_ < 1) throw std::invalid_argument("APALM: SubIntervals must be >= 1");
     if (alm_.method() != ALMGPU::Crisfield && alm_.method() != ALMGPU::Riks)
         throw std::invalid_argument("APALM needs an arc-length method with a distance (Crisfield or Riks)");
-    tmp_.alloc(P_.nfree);
+    workers_.push_back(APWorker{&alm_, &P_, std::make_shared<DevBuf<double>>(P_.nfree)});
 }
 
-APSolution APALM::copy_of(const double* d_U, double L) {
+APSolution APALM::copy_of(APWorker& w, const double* d_U, double L) {
     APSolution s;
-    s.U = std::make_shared<DevBuf<double>>(P_.nfree);
-    KL_CUDA(cudaMemcpyAsync(s.U->get(), d_U, sizeof(double) * P_.nfree, cudaMemcpyDeviceToDevice, P_.stream));
+    s.U = std::make_shared<DevBuf<double>>(w.P->nfree);
+    KL_CUDA(cudaMemcpyAsync(s.U->get(), d_U, sizeof(double) * w.P->nfree, cudaMemcpyDeviceToDevice, w.P->stream));
     s.L = L;
     return s;
 }
 
-APSolution APALM::copy_current() { return copy_of(alm_.U(), alm_.L()); }
+APSolution APALM::copy_current(APWorker& w) { return copy_of(w, w.alm->U(), w.alm->L()); }
 
-double APALM::distance_between(const APSolution& a, const APSolution& b) {
-    vec::lincomb(1.0, a.U->get(), -1.0, b.U->get(), tmp_.get(), P_.nfree, P_.stream);
-    return alm_.distance(tmp_.get(), a.L - b.L);
+double APALM::distance_between(APWorker& w, const APSolution& a, const APSolution& b) {
+    vec::lincomb(1.0, a.U->get(), -1.0, b.U->get(), w.tmp->get(), w.P->nfree, w.P->stream);
+    return w.alm->distance(w.tmp->get(), a.L - b.L);
+}
+
+void APALM::add_worker(ALMGPU& alm, Problem& P) {
+    if (P.nfree != P_.nfree) throw std::invalid_argument("APALM worker: its problem has a different number of dofs");
+    if (alm.method() != alm_.method()) throw std::invalid_argument("APALM worker: a different arc-length method");
+    if (&P == &P_) throw std::invalid_argument("APALM worker: it needs its own problem (its own stream and state)");
+    workers_.push_back(APWorker{&alm, &P, std::make_shared<DevBuf<double>>(P.nfree)});
 }
 
 void APALM::initialize() {
@@ -274,9 +283,10 @@ void APALM::initiation(const APALMData::Job& job, double startTime, double& dist
 }
 
 // gsAPALM.hpp:1013-1170
-void APALM::correction(const APALMData::Job& job, std::pair<double, double> interval, const APSolution& reference,
-                       std::vector<double>& distances, std::vector<APSolution>& stepSolutions, double& upper,
-                       double& lower) {
+void APALM::correction(APWorker& w, const APALMData::Job& job, std::pair<double, double> interval,
+                       const APSolution& reference, std::vector<double>& distances,
+                       std::vector<APSolution>& stepSolutions, double& upper, double& lower) {
+    ALMGPU& alm = *w.alm;
     int N = subIntervals_;
     stepSolutions.assign(N, APSolution());
     distances.assign(N + 1, 0.0);
@@ -290,24 +300,24 @@ void APALM::correction(const APALMData::Job& job, std::pair<double, double> inte
     dL0 /= N;
     double dL = dL0, dL_rem = 0.0;
     bool bisected = false;
-    alm_.set_length(dL);
-    alm_.set_solution(start.U->get(), start.L);
-    alm_.set_previous(prev.U->get(), prev.L);
+    alm.set_length(dL);
+    alm.set_solution(start.U->get(), start.L);
+    alm.set_previous(prev.U->get(), prev.L);
     int tries = 0;
     for (int k = 0; k != N; ++k) {
-        const int status = alm_.step();
+        const int status = alm.step();
         if (status == ST_NOT_CONVERGED || status == ST_ASSEMBLY_ERROR) {
             if (++tries > step_retry_limit()) throw std::runtime_error("APALM: the arc-length step keeps failing");
             dL /= 2.0;
             dL_rem += dL;   // the remainder of the interval
-            alm_.set_length(dL);
-            alm_.set_solution(old.U->get(), old.L);
+            alm.set_length(dL);
+            alm.set_solution(old.U->get(), old.L);
             bisected = true;
             k -= 1;
             continue;
         }
-        stepSolutions[k] = copy_current();
-        distances[k] = distance_between(stepSolutions[k], old);
+        stepSolutions[k] = copy_current(w);
+        distances[k] = distance_between(w, stepSolutions[k], old);
         old = stepSolutions[k];
         if (!bisected) {
             dL = dL0;
@@ -318,14 +328,15 @@ void APALM::correction(const APALMData::Job& job, std::pair<double, double> inte
             stepSolutions.resize(N);
             distances.resize(N + 1);
         }
-        alm_.set_length(dL);
+        alm.set_length(dL);
         dL_rem = 0.0;
         bisected = false;
     }
-    APSolution cur = copy_current();
-    distances.back() = distance_between(reference, cur);
-    upper = distance_between(reference, ori);
-    lower = distance_between(stepSolutions.back(), ori);
+    APSolution cur = copy_current(w);
+    distances.back() = distance_between(w, reference, cur);
+    upper = distance_between(w, reference, ori);
+    lower = distance_between(w, stepSolutions.back(), ori);
+    KL_CUDA(cudaStreamSynchronize(w.P->stream));
 }
 
 // gsAPALM.hpp:122-220
@@ -379,6 +390,7 @@ void APALM::serial_solve(int nsteps) {
 
 // gsAPALM.hpp:430-472
 void APALM::parallel_solve() {
+    if (workers_.size() > 1) return parallel_solve_workers();
     int it = 0;
     while (!data_empty() && it < maxIt_) {
         const int b = first_nonempty_branch();
@@ -389,10 +401,60 @@ void APALM::parallel_solve() {
         std::vector<double> distances;
         std::vector<APSolution> stepSolutions;
         double upper = 0.0, lower = 0.0;
-        correction(job, data_[b].jobTimes(ID), reference, distances, stepSolutions, upper, lower);
+        correction(workers_[0], job, data_[b].jobTimes(ID), reference, distances, stepSolutions, upper, lower);
         data_[b].submit(ID, distances, stepSolutions, upper, lower);
         data_[b].finishJob(ID);
         ++it;
+    }
+    finalize();
+}
+
+// gsAPALM.hpp:276-378 with W workers: hand a job to every idle worker (queue order, workers in
+// FIFO order), then take the oldest job handed out, submit it, return its worker to the pool and
+// hand out jobs again.  The jobs of the busy workers run concurrently, one host thread each.
+void APALM::parallel_solve_workers() {
+    struct Flight {
+        int b, ID, w;
+        std::vector<double> distances;
+        std::vector<APSolution> sols;
+        double upper = 0.0, lower = 0.0;
+        std::future<void> done;
+    };
+    std::deque<int> idle;
+    for (int w = 0; w < (int)workers_.size(); ++w) idle.push_back(w);
+    std::deque<std::unique_ptr<Flight>> flights;
+    int it = 0;
+    auto dispatch = [&] {
+        while (!data_empty() && it < maxIt_ && !idle.empty()) {
+            const int b = first_nonempty_branch();
+            APALMData::Job job = data_[b].pop();
+            auto f = std::make_unique<Flight>();
+            f->b = b;
+            f->ID = std::get<0>(job);
+            f->w = idle.front();
+            idle.pop_front();
+            APSolution reference;
+            if (!data_[b].referenceByID(f->ID, reference)) throw std::logic_error("APALM: reference not found");
+            const std::pair<double, double> interval = data_[b].jobTimes(f->ID);
+            // the job's start / previous / reference buffers are complete before another stream reads them
+            for (auto& wk : workers_) KL_CUDA(cudaStreamSynchronize(wk.P->stream));
+            Flight* fp = f.get();
+            fp->done = std::async(std::launch::async, [this, fp, job, interval, reference] {
+                correction(workers_[fp->w], job, interval, reference, fp->distances, fp->sols, fp->upper, fp->lower);
+            });
+            flights.push_back(std::move(f));
+            ++it;
+        }
+    };
+    dispatch();
+    while (!flights.empty()) {
+        std::unique_ptr<Flight> f = std::move(flights.front());
+        flights.pop_front();
+        f->done.get();   // rethrows a worker's failure
+        data_[f->b].submit(f->ID, f->distances, f->sols, f->upper, f->lower);
+        data_[f->b].finishJob(f->ID);
+        idle.push_back(f->w);
+        dispatch();
     }
     finalize();
 }
@@ -448,7 +510,7 @@ void APALM::solve(int nsteps) {
             std::vector<double> distances;
             std::vector<APSolution> stepSolutions;
             double upper = 0.0, lower = 0.0;
-            correction(job, data_[b].jobTimes(ID), reference, distances, stepSolutions, upper, lower);
+            correction(workers_[0], job, data_[b].jobTimes(ID), reference, distances, stepSolutions, upper, lower);
             data_[b].submit(ID, distances, stepSolutions, upper, lower);
             data_[b].finishJob(ID);
             ++it;

@@ -7,9 +7,14 @@
 // (gsAPALMData.hpp) keeps per branch the two knot vectors of the path (curve time t and its
 // parameter xi), the solutions and their levels, and the job queue.
 //
-// Here the jobs run on the device arc-length solver and every solution stays in HBM.  The
-// schedule is the reference's single-process one (gsAPALM.hpp:430-472, 822-932): jobs run in
-// queue order, so the points and their order are those of a one-process reference run.
+// Here the jobs run on the device arc-length solver and every solution stays in HBM.  With one
+// solver the schedule is the reference's single-process one (gsAPALM.hpp:430-472, 822-932): jobs
+// run in queue order, so the points and their order are those of a one-process reference run.
+// With W worker solvers (add_worker: each its own arc-length object on its own problem and
+// stream) parallel_solve runs the reference's MPI schedule (gsAPALM.hpp:276-378): a job goes to
+// every idle worker, each finished job is submitted and its worker refilled at once, with the
+// jobs finishing in the order they were handed out; the workers run concurrently on the GPU,
+// each driven by its own host thread.
 #pragma once
 
 #include <deque>
@@ -67,14 +72,25 @@ private:
     double dt_ = 1.0;
 };
 
-// gsAPALM (gsALMSolvers/gsAPALM.hpp), single process
+// one arc-length solver that runs jobs: its object, its problem (stream, device state) and scratch
+struct APWorker {
+    ALMGPU* alm;
+    Problem* P;
+    std::shared_ptr<DevBuf<double>> tmp;
+};
+
+// gsAPALM (gsALMSolvers/gsAPALM.hpp)
 class APALM {
 public:
     APALM(ALMGPU& alm, const Options& opt);
+    // another solver for the interval corrections of parallel_solve (same method, options and
+    // problem description as the first; MPI rank w + 1 of the reference's schedule)
+    void add_worker(ALMGPU& alm, Problem& P);
+    int workers() const { return (int)workers_.size(); }
     void initialize();                                          // gsAPALM.hpp:86-100
     void add_start(const double* d_U, double L, double dL);     // _initStart (:102-120)
     void serial_solve(int nsteps);                              // :122-220
-    void parallel_solve();                                      // :430-472
+    void parallel_solve();                                      // :430-472 (one worker), :276-378 (several)
     void solve(int nsteps);                                     // :822-932
     int branches() const { return (int)times_.size(); }
     int solutions(int b) const { return (int)times_.at(b).size(); }
@@ -83,15 +99,19 @@ public:
     int level(int b, int k) const { return levels_.at(b).at(k); }
 
 private:
-    APSolution copy_current();                                   // (solutionU, solutionL) of the ALM
-    APSolution copy_of(const double* d_U, double L);
-    double distance_between(const APSolution& a, const APSolution& b);   // distance(a - b)
+    APSolution copy_current() { return copy_current(workers_[0]); }
+    APSolution copy_current(APWorker& w);                        // (solutionU, solutionL) of a worker's ALM
+    APSolution copy_of(const double* d_U, double L) { return copy_of(workers_[0], d_U, L); }
+    APSolution copy_of(APWorker& w, const double* d_U, double L);
+    double distance_between(const APSolution& a, const APSolution& b) { return distance_between(workers_[0], a, b); }
+    double distance_between(APWorker& w, const APSolution& a, const APSolution& b);   // distance(a - b)
     int step_retry_limit() const { return 60; }
     void initiation(const APALMData::Job& job, double startTime, double& distance, std::vector<APSolution>& sols,
                     bool& bifurcation);
-    void correction(const APALMData::Job& job, std::pair<double, double> interval, const APSolution& reference,
-                    std::vector<double>& distances, std::vector<APSolution>& stepSolutions, double& upper,
-                    double& lower);
+    void correction(APWorker& w, const APALMData::Job& job, std::pair<double, double> interval,
+                    const APSolution& reference, std::vector<double>& distances,
+                    std::vector<APSolution>& stepSolutions, double& upper, double& lower);
+    void parallel_solve_workers();
     void finalize();
     int first_nonempty_branch() const;
     bool data_empty() const;
@@ -106,7 +126,7 @@ private:
     std::vector<std::vector<APSolution>> sols_;
     std::vector<std::vector<double>> times_;
     std::vector<std::vector<int>> levels_;
-    DevBuf<double> tmp_;
+    std::vector<APWorker> workers_;
 };
 
 }  // namespace klsa

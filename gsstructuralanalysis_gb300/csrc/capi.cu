@@ -781,6 +781,13 @@ int klsa_apalm_destroy(klsa_apalm* ap) {
         return KLSA_SUCCESS;
     });
 }
+int klsa_apalm_add_worker(klsa_apalm* ap, klsa_alm* worker) {
+    if (!ap || !worker) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        ap->A->add_worker(*worker->A, *worker->prob->P);
+        return KLSA_SUCCESS;
+    });
+}
 int klsa_apalm_initialize(klsa_apalm* ap) {
     if (!ap) return KLSA_INVALID_ARGUMENT;
     return guarded([&] {

@@ -249,6 +249,13 @@ int klsa_apalm_destroy(klsa_apalm* ap);
 int klsa_apalm_initialize(klsa_apalm* ap);                           /* initialize(): start at (0, 0) */
 int klsa_apalm_add_start(klsa_apalm* ap, const double* U, double L, double dL);   /* _initStart */
 int klsa_apalm_serial_solve(klsa_apalm* ap, int nsteps);             /* serialSolve(Nsteps) */
+/* Another solver for parallelSolve's interval corrections -- the reference's MPI workers
+ * (gsAPALM.hpp:276-378) as concurrent solvers on one GPU.  worker: an arc-length object of the
+ * same method and options on its own problem made from the same description.  With W solvers
+ * parallelSolve hands a job to every idle one, submits the oldest job handed out when it is
+ * done and refills its solver at once (the MPI schedule, jobs finishing in the order they were
+ * handed out); each solver runs on its own stream from its own host thread. */
+int klsa_apalm_add_worker(klsa_apalm* ap, klsa_alm* worker);
 int klsa_apalm_parallel_solve(klsa_apalm* ap);                       /* parallelSolve() */
 int klsa_apalm_solve(klsa_apalm* ap, int nsteps);                    /* solve(Nsteps) */
 int klsa_apalm_branches(klsa_apalm* ap);

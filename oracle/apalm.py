@@ -161,6 +161,7 @@ class APALM:
                  BifLengthMultiplier=0.1, MaxLevel=5, Tolerance=1e-1)
         o.update(options or {})
         self.alm, self.o = alm, o
+        self.workers = [alm]
         self.starts = deque()
         self.data = []
         self.solutions, self.times, self.levels = [], [], []
@@ -209,8 +210,8 @@ class APALM:
             sols.append((a.U.copy(), a.L))
         return dist, sols, bif
 
-    def _correction(self, job, reference):
-        a = self.alm
+    def _correction(self, job, reference, alm=None):
+        a = self.alm if alm is None else alm
         N = int(self.o["SubIntervals"])
         _, dL0, start, prev = job
         dL0 = dL0 / N
@@ -294,11 +295,46 @@ class APALM:
         self.data[b].submit(ID, dists, steps, upper, lower)
         self.data[b].finish_job(ID)
 
+    def add_worker(self, alm):
+        """Another solver for parallel_solve (an MPI worker of the reference)."""
+        self.workers.append(alm)
+
     def parallel_solve(self):
+        if len(self.workers) > 1:
+            return self._parallel_solve_workers()
         it = 0
         while self._any_jobs() and it < self.o["MaxIt"]:
             self._correct(self._first_nonempty())
             it += 1
+        self._finalize()
+
+    def _parallel_solve_workers(self):
+        """gsAPALM.hpp:276-378: hand a job to every idle worker (queue order, workers FIFO), then
+        take the oldest job handed out, submit it, return its worker and hand out jobs again.
+        A job's correction depends only on the job and its worker, so it is computed when it is
+        handed out and submitted in turn."""
+        idle = deque(range(len(self.workers)))
+        flights = deque()
+        it = 0
+
+        def dispatch():
+            nonlocal it
+            while self._any_jobs() and it < self.o["MaxIt"] and idle:
+                b = self._first_nonempty()
+                job = self.data[b].pop()
+                ID = job[0]
+                w = idle.popleft()
+                res = self._correction(job, self.data[b].reference(ID), self.workers[w])
+                flights.append((b, ID, w, res))
+                it += 1
+
+        dispatch()
+        while flights:
+            b, ID, w, res = flights.popleft()
+            self.data[b].submit(ID, *res)
+            self.data[b].finish_job(ID)
+            idle.append(w)
+            dispatch()
         self._finalize()
 
     def solve(self, nsteps=10):

@@ -5,6 +5,7 @@ as serialSolve() followed by parallelSolve() (initiation jobs are queued at the 
 import numpy as np
 
 import apalm as AP
+from gsstructuralanalysis_gb300 import problems as P
 
 
 def _alm(oracle_mod, oa):
@@ -60,3 +61,31 @@ def test_apalm_over_riks(oracle_mod):
     a.solve(4)
     t, lv = np.array(a.times[0]), np.array(a.levels[0])
     assert len(t) >= 7 and np.all(np.diff(t) > 0) and lv.max() == 1
+
+
+def test_worker_schedule_one_level_equals_serial(oracle_mod):
+    """The MPI schedule of parallelSolve (gsAPALM.hpp:276-378) in the restatement, with three
+    workers: with one refinement level every job corrects a coarse interval that no other job's
+    submission changes, and the workers' corrections are identical (Scaling fixed), so the flat
+    path is the one-process schedule's point for point."""
+    import apalm as AP
+    prob = P.cylindrical_panel(m=4, p=2, load=1.0)
+    oa = oracle_mod.OracleAssembler(prob)
+    opts = dict(Length=0.02, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=30, BifurcationMethod=-1)
+    ap_opts = dict(SubIntervals=2, MaxLevel=1, Tolerance=1e-3, MaxIt=40)
+    mk = lambda: oracle_mod.ALMCrisfield(oa.jacobian, oa.al_residual, oa.force(), opts)
+    serial = AP.APALM(mk(), ap_opts)
+    serial.initialize()
+    serial.serial_solve(4)
+    serial.parallel_solve()
+    par = AP.APALM(mk(), ap_opts)
+    par.add_worker(mk())
+    par.add_worker(mk())
+    par.initialize()
+    par.serial_solve(4)
+    par.parallel_solve()
+    # with one refinement level the corrections of the coarse intervals are independent jobs
+    assert list(par.levels[0]) == list(serial.levels[0])
+    np.testing.assert_allclose(par.times[0], serial.times[0], rtol=1e-12, atol=1e-14)
+    for (U, L), (Us, Ls) in zip(par.solutions[0], serial.solutions[0]):
+        assert abs(L - Ls) <= 1e-12 * max(abs(Ls), 1.0)
