@@ -887,6 +887,64 @@ def eigen_cpu_baseline():
                       "C++ OpenMP assembly, scipy SuperLU + ARPACK"}
 
 
+# ---------------------------------------------------------------------------------------------
+# preconditioned CG against the multifrontal LDL^T on the shell tangents
+# ---------------------------------------------------------------------------------------------
+PCG_METRIC = "linear solves/s on shell tangents: preconditioned CG (Jacobi, nodal block-Jacobi) vs multifrontal LDL^T"
+
+
+def run_pcg(args):
+    """The solves the benchmark spec names for the Newton and Lanczos inner systems, measured on the
+    tangents of the ramp roof (degree 3, 64x64, K at zero and at the 10%-load solution) and of the
+    headline roof (degree 2, 128x128, K at zero): CG to a relative residual of 1e-8 with the
+    Jacobi (CGDiagonal) and nodal 3x3 block-Jacobi (GPUPCG) preconditioners, against the
+    multifrontal LDL^T (factorisation + solve, FP64 fronts).  One step = every case once."""
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    B.build()
+    G.load_library()
+    cases = []
+    for m, p, load, state in ((64, 3, RAMP_LOAD, "zero"), (64, 3, RAMP_LOAD, "load10"), (128, 2, 1.0, "zero")):
+        prob = P.cylindrical_panel(m=m, p=p, load=load)
+        gp = G.Problem(prob)
+        x = np.zeros(gp.ndof)
+        if state == "load10":
+            sn = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "tol": 1e-8, "maxIt": 50})
+            sn.setLoad(0.1)
+            sn.solve()
+            x = sn.solution()
+        cases.append((f"degree {p}, {m}x{m}, K({state})", gp, x))
+    rows = []
+    t_all = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        rows = []
+        for name, gp, x in cases:
+            F = gp.force()
+            row = {"case": name, "ndof": int(gp.ndof)}
+            for sname, opts in (("SimplicialLDLT", {"FrontPrecision": 64}),
+                                ("CGDiagonal", {"CGTolerance": 1e-8, "CGMaxIterations": args.cg_max_it}),
+                                ("GPUPCG", {"CGTolerance": 1e-8, "CGMaxIterations": args.cg_max_it})):
+                S = G.SparseSolver(gp, sname, opts)
+                gp.sync()
+                t0 = time.perf_counter()
+                S.compute_jacobian(x)
+                u = S.solve(F)
+                gp.sync()
+                dt = time.perf_counter() - t0
+                K = gp.jacobian(x, 1)
+                rel = float(np.linalg.norm(K @ u - F) / np.linalg.norm(F))
+                row[sname] = {"s": dt, "iterations": int(S.iterations()), "rel_residual": rel}
+            rows.append(row)
+    total = time.perf_counter() - t_all
+    nsolves = 3 * len(cases) * max(1, args.steps)
+    line = {"metric": PCG_METRIC, "value": nsolves / total, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 0, "ms_per_step": 1e3 * total / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "F = K x solves on shell tangents, per solver and case", "cases": rows,
+                       "cg_tolerance": 1e-8, "cg_max_iterations": args.cg_max_it}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -907,13 +965,16 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
-    ap.add_argument("--workload", default="arc-length", choices=["arc-length", "batched", "ramp", "eigen"],
+    ap.add_argument("--workload", default="arc-length", choices=["arc-length", "batched", "ramp", "eigen", "pcg"],
                     help="arc-length: the headline path-following workload; batched: 256 uneven Newton solves; "
                          "ramp: degree-3 static Newton load ramp; eigen: buckling + modal at 201k dofs")
     ap.add_argument("--batch", type=int, default=BATCH_N, help="instances per GPU of the batched workload")
     ap.add_argument("--eig-m", type=int, default=EIG_M, help="elements per direction of the eigen workload")
     ap.add_argument("--eig-shift", type=float, default=-1.0, help="buckling shift of the eigen workload")
+    ap.add_argument("--cg-max-it", type=int, default=20000, help="CG iteration limit of the pcg workload")
     args = ap.parse_args()
+    if args.workload == "pcg":
+        return run_pcg(args)
     if args.workload == "ramp":
         return run_ramp(args)
     if args.workload == "eigen":

@@ -60,6 +60,7 @@ SIGNATURES = {
     "klsa_solver_compute_jacobian": (_c_int, [_c_vp, _c_vp]),
     "klsa_solver_compute_linear": (_c_int, [_c_vp]),
     "klsa_solver_solve": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int]),
+    "klsa_solver_iterations": (_c_int, [_c_vp]),
     "klsa_solver_stability": (_c_int, [_c_vp, _c_vp, _c_vp]),
     "klsa_static_create": (_c_int, [_c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
     "klsa_static_destroy": (_c_int, [_c_vp]),
@@ -360,6 +361,10 @@ class SparseSolver:
         x = np.zeros_like(b)
         _check(_lib.klsa_solver_solve(self.h, _ptr(b), _ptr(x), nrhs))
         return x
+
+    def iterations(self):
+        """CG iterations (PCG solvers) or refinement sweeps (LDL^T) of the last solve."""
+        return _check(_lib.klsa_solver_iterations(self.h))
 
     def stability(self):
         mn = np.zeros(1)

@@ -278,6 +278,8 @@ int klsa_solver_solve(klsa_solver* s, const double* b, double* x, int nrhs) {
     });
 }
 
+int klsa_solver_iterations(klsa_solver* s) { return s ? s->S->last_iterations() : KLSA_INVALID_ARGUMENT; }
+
 int klsa_solver_stability(klsa_solver* s, double* min_d, int64_t* negatives) {
     if (!s || !min_d || !negatives) return KLSA_INVALID_ARGUMENT;
     return guarded([&] {

@@ -1,6 +1,8 @@
 // linalg.cu -- FP64 vector kernels, multi-dot reductions and the named linear solvers.
 #include "linalg.h"
 
+#include <vector>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -70,6 +72,53 @@ __global__ void diag_extract_kernel(int n, const int* __restrict__ rowptr, const
     for (int k = rowptr[r]; k < rowptr[r + 1]; ++k)
         if (cols[k] == r) d = vals[k];
     dinv[r] = d != 0.0 ? 1.0 / d : 1.0;
+}
+// Nodal block-Jacobi: the (up to 3 x 3) diagonal block of every control point's free dofs, which
+// are consecutive in the internal order, inverted in FP64 (row-major, padded to 3 x 3).
+__global__ void block_extract_kernel(int nblk, const int* __restrict__ start, const int* __restrict__ rowptr,
+                                     const int* __restrict__ cols, const float* __restrict__ vals,
+                                     double* __restrict__ binv) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    const int s0 = start[b], sz = start[b + 1] - s0;
+    double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, X[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < sz; ++i)
+        for (int k = rowptr[s0 + i]; k < rowptr[s0 + i + 1]; ++k) {
+            const int c = cols[k] - s0;
+            if (c >= 0 && c < sz) A[i][c] = vals[k];
+        }
+    bool ok = true;
+    for (int j = 0; j < sz; ++j) {            // Gauss-Jordan with partial pivoting
+        int piv = j;
+        for (int i = j + 1; i < sz; ++i)
+            if (fabs(A[i][j]) > fabs(A[piv][j])) piv = i;
+        if (A[piv][j] == 0.0) { ok = false; break; }
+        for (int c = 0; c < 3; ++c) {
+            double t = A[j][c]; A[j][c] = A[piv][c]; A[piv][c] = t;
+            t = X[j][c]; X[j][c] = X[piv][c]; X[piv][c] = t;
+        }
+        const double inv = 1.0 / A[j][j];
+        for (int c = 0; c < 3; ++c) { A[j][c] *= inv; X[j][c] *= inv; }
+        for (int i = 0; i < sz; ++i) {
+            if (i == j) continue;
+            const double f = A[i][j];
+            for (int c = 0; c < 3; ++c) { A[i][c] -= f * A[j][c]; X[i][c] -= f * X[j][c]; }
+        }
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) binv[9 * (size_t)b + 3 * i + c] = ok ? X[i][c] : (i == c ? 1.0 : 0.0);
+}
+__global__ void block_apply_kernel(int nblk, const int* __restrict__ start, const double* __restrict__ binv,
+                                   const double* __restrict__ r, double* __restrict__ z) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    const int s0 = start[b], sz = start[b + 1] - s0;
+    const double* M = binv + 9 * (size_t)b;
+    for (int i = 0; i < sz; ++i) {
+        double v = 0.0;
+        for (int c = 0; c < sz; ++c) v += M[3 * i + c] * r[s0 + c];
+        z[s0 + i] = v;
+    }
 }
 __global__ void mul_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c, int64_t n) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -234,16 +283,44 @@ void MFSolver::stability(double* min_d, int64_t* neg) {
 // ------------------------------------------------------------------------------------------
 // Jacobi-preconditioned CG ("CGDiagonal": Eigen ConjugateGradient + DiagonalPreconditioner)
 // ------------------------------------------------------------------------------------------
-PCGSolver::PCGSolver(Problem& P, int max_it, double tol) : P_(P), max_it_(max_it), tol_(tol) {
+PCGSolver::PCGSolver(Problem& P, int max_it, double tol, bool block)
+    : P_(P), max_it_(max_it), tol_(tol), block_(block) {
     int n = P_.nfree;
     dinv_.alloc(n); r_.alloc(n); z_.alloc(n); p_.alloc(n); q_.alloc(n);
     if (max_it_ <= 0) max_it_ = 2 * n;
+    if (block_) {
+        // blocks: runs of consecutive internal dofs of one control point
+        std::vector<int> i2f(n);
+        P_.d_int2full.download(i2f.data(), n, P_.stream);
+        KL_CUDA(cudaStreamSynchronize(P_.stream));
+        std::vector<int> start;
+        for (int i = 0; i < n; ++i)
+            if (i == 0 || i2f[i] % P_.ncp != i2f[i - 1] % P_.ncp || i - start.back() == 3) start.push_back(i);
+        start.push_back(n);
+        nblk_ = (int)start.size() - 1;
+        blk_start_.upload(start, P_.stream);
+        binv_.alloc((size_t)9 * nblk_);
+    }
+}
+
+void PCGSolver::precondition(const double* r, double* z) {
+    if (block_) {
+        block_apply_kernel<<<ceil_div(nblk_, 256), 256, 0, P_.stream>>>(nblk_, blk_start_.get(), binv_.get(), r, z);
+    } else {
+        mul_kernel<<<ceil_div(P_.nfree, 256), 256, 0, P_.stream>>>(dinv_.get(), r, z, P_.nfree);
+    }
+    count_launch();
 }
 
 int PCGSolver::compute_tangent() {
     P_.tangent_f32();
-    diag_extract_kernel<<<ceil_div(P_.nfree, 256), 256, 0, P_.stream>>>(P_.nfree, P_.d_rowptr.get(), P_.d_cols.get(),
-                                                                         P_.d_vals32.get(), dinv_.get());
+    if (block_) {
+        block_extract_kernel<<<ceil_div(nblk_, 256), 256, 0, P_.stream>>>(nblk_, blk_start_.get(), P_.d_rowptr.get(),
+                                                                         P_.d_cols.get(), P_.d_vals32.get(), binv_.get());
+    } else {
+        diag_extract_kernel<<<ceil_div(P_.nfree, 256), 256, 0, P_.stream>>>(P_.nfree, P_.d_rowptr.get(), P_.d_cols.get(),
+                                                                             P_.d_vals32.get(), dinv_.get());
+    }
     count_launch();
     return ST_SUCCESS;
 }
@@ -256,8 +333,7 @@ int PCGSolver::solve(const double* d_b, double* d_x, int nrhs) {
         double* x = d_x + (size_t)q * n;
         KL_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
         KL_CUDA(cudaMemcpyAsync(r_.get(), b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        mul_kernel<<<ceil_div(n, 256), 256, 0, s>>>(dinv_.get(), r_.get(), z_.get(), n);
-        count_launch();
+        precondition(r_.get(), z_.get());
         KL_CUDA(cudaMemcpyAsync(p_.get(), z_.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         double d[2];
         const double* xs[2] = {r_.get(), b};
@@ -275,8 +351,7 @@ int PCGSolver::solve(const double* d_b, double* d_x, int nrhs) {
             double alpha = rz / pq;
             vec::axpby(alpha, p_.get(), 1.0, x, n, s);
             vec::axpby(-alpha, q_.get(), 1.0, r_.get(), n, s);
-            mul_kernel<<<ceil_div(n, 256), 256, 0, s>>>(dinv_.get(), r_.get(), z_.get(), n);
-            count_launch();
+            precondition(r_.get(), z_.get());
             double dd[2];
             const double* u1[2] = {r_.get(), r_.get()};
             const double* u2[2] = {z_.get(), r_.get()};
@@ -296,8 +371,10 @@ std::unique_ptr<LinearSolver> make_linear_solver(Problem& P, const std::string& 
     if (front_precision != 32 && front_precision != 64) throw std::invalid_argument("FrontPrecision must be 32 or 64");
     if (name == "SimplicialLDLT" || name == "GPUMultifrontalLDLT" || name == "SimplicialLLT" || name == "LDLT")
         return std::unique_ptr<LinearSolver>(new MFSolver(P, refine, refine_tol, front_precision == 64));
-    if (name == "CGDiagonal" || name == "GPUPCG" || name == "ConjugateGradient")
-        return std::unique_ptr<LinearSolver>(new PCGSolver(P, cg_max_it, cg_tol));
+    if (name == "CGDiagonal" || name == "ConjugateGradient")
+        return std::unique_ptr<LinearSolver>(new PCGSolver(P, cg_max_it, cg_tol, false));
+    if (name == "GPUPCG" || name == "BlockJacobiCG")
+        return std::unique_ptr<LinearSolver>(new PCGSolver(P, cg_max_it, cg_tol, true));
     return nullptr;
 }
 

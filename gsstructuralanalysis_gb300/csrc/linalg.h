@@ -52,17 +52,21 @@ private:
 
 class PCGSolver : public LinearSolver {
 public:
-    PCGSolver(Problem& P, int max_it, double tol);
+    // block = false: Jacobi (Eigen's DiagonalPreconditioner); true: nodal 3 x 3 block-Jacobi
+    PCGSolver(Problem& P, int max_it, double tol, bool block = false);
     int compute_tangent() override;
     int solve(const double* d_b, double* d_x, int nrhs) override;
     int last_iterations() const override { return iterations_; }
 
 private:
+    void precondition(const double* r, double* z);
     Problem& P_;
     int max_it_;
     double tol_;
-    int iterations_ = 0;
-    DevBuf<double> dinv_, r_, z_, p_, q_;
+    bool block_;
+    int iterations_ = 0, nblk_ = 0;
+    DevBuf<double> dinv_, r_, z_, p_, q_, binv_;
+    DevBuf<int> blk_start_;
 };
 
 std::unique_ptr<LinearSolver> make_linear_solver(Problem& P, const std::string& name, int refine, double refine_tol,

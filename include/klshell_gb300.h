@@ -122,7 +122,9 @@ int klsa_options_set_string(klsa_options* opt, const char* key, const char* valu
 /* ---- named sparse solver (gsSparseSolver<T>::get(name), gsStaticBase.h:85) --------------
  * "SimplicialLDLT" / "GPUMultifrontalLDLT": nested-dissection multifrontal LDL^T, FP32
  * fronts, optional FP64 iterative refinement ("Refinement" steps, tolerance "RefineTol").
- * "CGDiagonal" / "GPUPCG": Jacobi (3x3 nodal block) preconditioned CG on the CSR matrix. */
+ * "CGDiagonal": Jacobi-preconditioned CG on the CSR matrix (Eigen's ConjugateGradient with the
+ * DiagonalPreconditioner); "GPUPCG" / "BlockJacobiCG": CG with the nodal 3x3 block-Jacobi
+ * preconditioner.  Options "CGMaxIterations" (default 2 ndof) and "CGTolerance". */
 int klsa_solver_create(klsa_problem* prob, const char* name, const klsa_options* opt, klsa_solver** out);
 int klsa_solver_destroy(klsa_solver* s);
 /* compute(K(x)) of the named solver: assemble the tangent at x on the device and factorise. */
@@ -131,6 +133,8 @@ int klsa_solver_compute_jacobian(klsa_solver* s, const double* x);
 int klsa_solver_compute_linear(klsa_solver* s);
 /* solve(b) for nrhs right-hand sides stored one after the other (ndof each). */
 int klsa_solver_solve(klsa_solver* s, const double* b, double* x, int nrhs);
+/* Iterations of the last solve: CG iterations (the PCG solvers) or refinement sweeps (LDL^T). */
+int klsa_solver_iterations(klsa_solver* s);
 /* LDL^T pivots: minimum of D and number of negative entries (determinant stability
  * indicator, gsStaticBase.h:162-179). */
 int klsa_solver_stability(klsa_solver* s, double* min_d, int64_t* negatives);

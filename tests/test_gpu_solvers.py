@@ -21,7 +21,7 @@ def test_linear_plate_config1(lib, oracle_mod):
     assert gp.ndof == 164
 
 
-@pytest.mark.parametrize("solver", ["SimplicialLDLT", "CGDiagonal"])
+@pytest.mark.parametrize("solver", ["SimplicialLDLT", "CGDiagonal", "GPUPCG"])
 def test_static_newton_panel(lib, oracle_mod, solver):
     import gsstructuralanalysis_gb300 as G
     prob = P.cylindrical_panel(m=6, p=3, load=800.0)
