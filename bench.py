@@ -158,28 +158,45 @@ def step_with_retry(alm, G):
 def train_predictor(G, learned, base, modes, args):
     """Training set of the learned predictor: ``args.train_paths`` seeded imperfect roofs (seeds
     0..n-1), each a Crisfield path of TRAIN_POINTS points generated by the library's GPU
-    arc-length solver, several paths at a time on separate host threads.  The POD basis comes
-    from the first ``args.pod_paths`` paths (full vectors); the other paths are kept as their
-    modal projections only.  The last path is held out for early stopping."""
+    arc-length solver, several paths at a time on separate host threads.  The first
+    ``args.pod_paths`` paths (placed extrapolation guesses) give the POD basis and a bootstrap
+    network; the other paths are generated with that network's guesses (every point still meets
+    the same arc-length constraint and TolF/TolU test, so they are the same equilibrium points)
+    and kept as modal projections only.  The final network trains on all paths; the last path is
+    held out for early stopping."""
     n_train = max(2, args.train_paths)
     n_pod = max(2, min(args.pod_paths, n_train))
+
+    def fit(paths, Phi):
+        samples = sum(max(len(L) - 4, 0) for _, L in paths)
+        batch = 128 if samples < 20000 else 256
+        epochs = int(np.clip(np.ceil(args.train_updates / max(samples / batch, 1.0)), 10, 400))
+        tp = learned.train(G, paths, nm=32, hidden=256, epochs=epochs, batch=batch, lr=1e-3,
+                           chunk=max(1, epochs // 40), Phi=Phi)
+        return tp, epochs, batch
+
     t0 = time.perf_counter()
     pod = learned.generate_paths(G, base, modes, range(n_pod), ALM_OPTS, TRAIN_POINTS, workers=args.train_workers)
     Phi = learned.pod_modes(pod, 32)
-    rest = learned.generate_paths(G, base, modes, range(n_pod, n_train), ALM_OPTS, TRAIN_POINTS,
-                                  workers=args.train_workers, Phi=Phi) if n_train > n_pod else []
-    paths = [(U @ Phi.T, L) for U, L in pod] + rest
+    paths = [(U @ Phi.T, L) for U, L in pod]
     del pod
     t1 = time.perf_counter()
-    samples = sum(max(len(L) - 4, 0) for _, L in paths)
-    batch = 128 if samples < 20000 else 256
-    epochs = int(np.clip(np.ceil(args.train_updates / max(samples / batch, 1.0)), 10, 400))
-    chunk = max(1, epochs // 40)
-    tp = learned.train(G, paths, nm=32, hidden=256, epochs=epochs, batch=batch, lr=1e-3, chunk=chunk, Phi=Phi)
+    boot = None
+    if n_train > n_pod:
+        boot, _, _ = fit(paths, Phi)
+        paths += learned.generate_paths(G, base, modes, range(n_pod, n_train), ALM_OPTS, TRAIN_POINTS,
+                                        workers=args.train_workers, Phi=Phi, tp=boot)
+    t2 = time.perf_counter()
+    tp, epochs, batch = fit(paths, Phi)
+    points = int(sum(len(L) - 1 for _, L in paths))
     info = {"paths": n_train, "points_per_path": TRAIN_POINTS, "pod_paths": n_pod,
-            "points_generated": int(sum(len(L) - 1 for _, L in paths)), "samples": tp.nsamples,
-            "epochs": epochs, "batch": batch, "path_generation_s": t1 - t0,
-            "path_generation_points_per_s": sum(len(L) - 1 for _, L in paths) / (t1 - t0),
+            "points_generated": points, "samples": tp.nsamples, "epochs": epochs, "batch": batch,
+            "path_generation_s": (t1 - t0) + (t2 - t1) - (boot.seconds["train"] if boot else 0.0),
+            "path_generation_points_per_s": points / max((t2 - t0) - (boot.seconds["train"] if boot else 0.0), 1e-9),
+            "generation": (f"{n_pod} paths with placed cubic-extrapolation guesses, then {n_train - n_pod} with the "
+                           f"guesses of a bootstrap network trained on them (held-out error "
+                           f"{boot.val_rel_error:.3f} of the extrapolation's)") if boot else
+                          f"{n_pod} paths with placed cubic-extrapolation guesses",
             "generation_workers": args.train_workers, "training_s": tp.seconds["train"], "alpha": tp.alpha,
             "best_epoch": tp.best_epoch, "val_rel_error_vs_extrapolation": tp.val_rel_error,
             "seeds": f"0..{n_train - 1} (held out for early stopping: {n_train - 1})"}
@@ -834,20 +851,31 @@ def run_eigen(args):
     launches = G.launch_count() - l0
     st1, bv, bvec, st2, mv, mvec = res
     value = 2 * EIG_NEV * args.steps / (ms / 1e3)
-    # size-independent check in FP64 on the host: relative eigen-residuals of every pair
-    KL = gp.jacobian(np.zeros(gp.ndof), 1)
-    M = gp.mass()
+    # parity with the FP64 oracle's matrices (assembled on the host, rank 0): the pre-stress state
+    # solves the oracle's K_L u = s F, and the Rayleigh quotients of the GPU eigenvectors with the
+    # oracle's K_L, B = K(u_L) - K_L and M -- within the squared residual of an oracle eigenvalue --
+    # agree with the GPU eigenvalues
     sn = G.StaticNewton(gp, {"Solver": "SimplicialLDLT", "FrontPrecision": 64, "Refinement": 4, "RefineTol": 1e-15})
     sn.setLoad(EIG_SCALING)
     sn.solveLinear()
     uL = sn.solution()
-    Bm = gp.jacobian(uL, 1) - KL
-    rb = [float(np.linalg.norm(KL @ v - lam * (Bm @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(bv, bvec)]
-    rm = [float(np.linalg.norm(KL @ v - lam * (M @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(mv, mvec)]
-    # Rayleigh quotients of the returned vectors in FP64: second-order accurate in the vector error,
-    # so their agreement with the returned eigenvalues bounds the eigenvalue error
-    qb = [float(abs((v @ (KL @ v)) / (v @ (Bm @ v)) - lam) / abs(lam)) for lam, v in zip(bv, bvec)]
-    qm = [float(abs((v @ (KL @ v)) / (v @ (M @ v)) - lam) / abs(lam)) for lam, v in zip(mv, mvec)]
+    parity = None
+    if rank == 0 and not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build_oracle()
+        oa = O.OracleAssembler(prob, nthreads=host_cores())
+        KL, M, F = oa.linear(), oa.mass(), oa.force()
+        Bm = oa.jacobian(uL) - KL
+        rb = [float(np.linalg.norm(KL @ v - lam * (Bm @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(bv, bvec)]
+        rm = [float(np.linalg.norm(KL @ v - lam * (M @ v)) / np.linalg.norm(KL @ v)) for lam, v in zip(mv, mvec)]
+        qb = [float(abs((v @ (KL @ v)) / (v @ (Bm @ v)) - lam) / abs(lam)) for lam, v in zip(bv, bvec)]
+        qm = [float(abs((v @ (KL @ v)) / (v @ (M @ v)) - lam) / abs(lam)) for lam, v in zip(mv, mvec)]
+        parity = {"prestress_rel_residual_oracle": float(np.linalg.norm(KL @ uL - EIG_SCALING * F) /
+                                                          np.linalg.norm(EIG_SCALING * F)),
+                  "max_rayleigh_rel_diff_buckling": max(qb), "max_rayleigh_rel_diff_modal": max(qm),
+                  "max_rel_residual_buckling": max(rb), "max_rel_residual_modal": max(rm), "bound": 1e-6,
+                  "ok": bool(max(qb) <= 1e-6 and max(qm) <= 1e-6)}
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu = eigen_cpu_baseline()
@@ -860,12 +888,10 @@ def run_eigen(args):
                                "one step = both analyses",
                    "ndof_free": gp.ndof, "nnz": gp.nnz, "status": [int(st1), int(st2)],
                    "buckling_values": bv.tolist(), "modal_values": mv.tolist(),
-                   "max_rel_residual_buckling": max(rb), "max_rel_residual_modal": max(rm),
-                   "max_rayleigh_rel_diff_buckling": max(qb), "max_rayleigh_rel_diff_modal": max(qm),
                    "l2": "inputs larger than L2 (fronts %.1f GB)" % (gp.stats()["front_bytes"] / 1e9)},
         "e2e": {"value": value, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 8 * gp.ndof * 2 * EIG_NEV},
-        "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
+        "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu, "parity": parity,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -953,9 +979,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--predictor", default="learned", choices=["plain", "extrapolation", "learned"])
-    ap.add_argument("--train-paths", type=int, default=96, help="training paths (seeds 0..n-1), 200 points each")
+    ap.add_argument("--train-paths", type=int, default=512, help="training paths (seeds 0..n-1), 200 points each")
     ap.add_argument("--pod-paths", type=int, default=32, help="training paths whose full vectors give the POD basis")
-    ap.add_argument("--train-workers", type=int, default=8, help="paths generated concurrently (host threads)")
+    ap.add_argument("--train-workers", type=int, default=16, help="paths generated concurrently (host threads)")
     ap.add_argument("--train-updates", type=int, default=40000, help="Adam updates of the training (sets the epochs)")
     ap.add_argument("--test-problems", type=int, default=8, help="distinct held-out roofs the timed paths cycle over")
     ap.add_argument("--compare-paths", type=int, default=2, help="test paths the plain / extrapolation arms run")

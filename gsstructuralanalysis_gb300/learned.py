@@ -92,7 +92,7 @@ def generate_path(G, prob, alm_opts, nsteps):
     return np.array(Us), np.array(Ls)
 
 
-def generate_paths(G, base, modes, seeds, alm_opts, nsteps, workers=8, frozen=1, Phi=None, on_done=None):
+def generate_paths(G, base, modes, seeds, alm_opts, nsteps, workers=8, frozen=1, Phi=None, on_done=None, tp=None):
     """Converged Crisfield paths of the imperfect shells ``seeds``, generated concurrently: each
     host thread drives its own problem (own stream, own fronts) through ``nsteps`` points.
 
@@ -100,8 +100,10 @@ def generate_paths(G, base, modes, seeds, alm_opts, nsteps, workers=8, frozen=1,
     mode with ``frozen`` iterations on the held factorisation, plain tangent steps for the first
     points and whenever a placed start fails).  Every point meets the same arc-length constraint
     and the same TolF/TolU test as the plain predictor, so the paths are the same equilibrium
-    points.  With ``Phi`` each point is stored as its modal projection q = Phi U (nm numbers);
-    without, as the full vector.  Returns [(U or q, lambda)] in the order of ``seeds``."""
+    points.  With ``tp`` (a trained predictor) the placed start is the network-corrected
+    extrapolation instead.  With ``Phi`` each point is stored as its modal projection
+    q = Phi U (nm numbers); without, as the full vector.  Returns [(U or q, lambda)] in the order
+    of ``seeds``."""
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
@@ -113,7 +115,7 @@ def generate_paths(G, base, modes, seeds, alm_opts, nsteps, workers=8, frozen=1,
         gp = G.Problem(imperfect_problem(base, modes, seed))
         alm = G.ALMCrisfield(gp, opts)
         alm.initialize(stability=False)
-        pred = G.Predictor(gp, None, np.zeros((0, gp.ndof)))
+        pred = G.Predictor(gp, None, np.zeros((0, gp.ndof))) if tp is None else make_predictor(G, gp, tp)
         U0 = np.zeros(gp.ndof)
         Us = [U0 if Phi is None else Phi @ U0]
         Ls = [0.0]
