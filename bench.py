@@ -39,6 +39,7 @@ TRAIN_POINTS = 200        # arc-length steps per path, training and test
 COARSE_M = 16             # imperfection modes: buckling modes of the 16x16 roof, transferred exactly
 METRIC = "arc-length path points/s at 50k dofs, learned vs plain predictor, ||R||/||F||<=1e-8"
 MAX_RETRIES = 6
+QGEO = 25                 # FP64 values per Gauss point in the device geometry table
 
 
 def workload_problem(m=None, p=None):
@@ -419,8 +420,8 @@ def roofline(prof, stats, args):
                             2 * stats["flops_panel"] / max(stats["launches_panel"], 1)),
         "mf_fwd+bwd (solve)": (raw["solve"][0], raw["solve"][1], stats["solve_bytes"], 0.0),
         "kl_tangent+csr_gather": (raw["assembly"][0], raw["assembly"][1],
-                                  n_qp * 22 * 8 + 2 * nel * d * d * 4 + stats["nnz"] * 8, stats["tangent_flops"]),
-        "kl_fint+gather (FP64)": (raw["residual"][0], raw["residual"][1], n_qp * 22 * 8 + 2 * nel * d * 8, 0.0),
+                                  n_qp * QGEO * 8 + 2 * nel * d * d * 4 + stats["nnz"] * 8, stats["tangent_flops"]),
+        "kl_fint+gather (FP64)": (raw["residual"][0], raw["residual"][1], n_qp * QGEO * 8 + 2 * nel * d * 8, 0.0),
     }
     detail = {}
     for k, (ms, n, byts, fl) in kinds.items():
@@ -971,6 +972,77 @@ def run_pcg(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------------------------
+# the hot path's kernels one by one (50k-dof roof)
+# ---------------------------------------------------------------------------------------------
+KERNELS_METRIC = "Newton iterations/s from device phase times at 50k dofs (tangent + LDL^T, 2-RHS solve, FP64 residual)"
+
+
+def run_kernels(args):
+    """The three device phases of an arc-length iteration on the headline roof (degree 2,
+    128x128, 49,920 free dofs) at a deformed state, each timed alone with CUDA events over
+    ``steps`` repetitions on the problem's stream: the FP32 tangent with its LDL^T factorisation,
+    the two-right-hand-side triangular solve (one persistent launch) and the FP64 residual.
+    One step = one of each.  Inputs stay in HBM; the front pool (front_bytes in the config line)
+    is larger than L2.  The line is the committed command behind the per-kernel ncu captures."""
+    import gsstructuralanalysis_gb300 as G
+    from gsstructuralanalysis_gb300 import build as B
+    B.build()
+    G.load_library()
+    gp = G.Problem(workload_problem())
+    stats = gp.stats()
+    rng = np.random.default_rng(0)
+    x = 1e-4 * rng.standard_normal(gp.ndof)
+    S = G.SparseSolver(gp, "SimplicialLDLT", {"Refinement": 0})
+    b = rng.standard_normal((2, gp.ndof))
+    for _ in range(args.warmup):
+        S.compute_jacobian(x)
+        S.solve(b)
+        gp.al_residual(x, 0.5)
+    gp.sync()
+    G.profile_reset()
+    G.profile_enable(True)
+    l0 = G.launch_count()
+    for _ in range(args.steps):
+        S.compute_jacobian(x)
+        S.solve(b)
+        gp.al_residual(x, 0.5)
+    gp.sync()
+    G.profile_enable(False)
+    ph = G.profile_read()
+    launches = G.launch_count() - l0
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    ms_fac = ph["factorization"][0] / max(ph["factorization"][1], 1)
+    ms_tan = ph["assembly"][0] / max(ph["assembly"][1], 1)
+    ms_sol = ph["solve"][0] / max(ph["solve"][1], 1)
+    ms_res = ph["residual"][0] / max(ph["residual"][1], 1)
+    n_qp, nel, d = stats["gauss_points"], stats["elements"], 27
+    res_bytes = n_qp * QGEO * 8 + 2 * nel * d * 8
+    detail = {
+        "tangent_assembly": {"ms": ms_tan, "tflops_fp32": stats["tangent_flops"] / (ms_tan / 1e3) / 1e12},
+        "ldlt_factorisation": {"ms": ms_fac, "tflops_fp32": stats["factor_flops"] / (ms_fac / 1e3) / 1e12},
+        "solve_2rhs": {"ms": ms_sol, "algorithmic_bytes": stats["solve_bytes"],
+                       "gbs": stats["solve_bytes"] / (ms_sol / 1e3) / 1e9,
+                       "frac_of_hbm": stats["solve_bytes"] / (ms_sol / 1e3) / 1e9 / hbm},
+        "residual_fp64": {"ms": ms_res, "algorithmic_bytes": res_bytes, "gbs": res_bytes / (ms_res / 1e3) / 1e9},
+    }
+    total_ms = ms_tan + ms_fac + ms_sol + ms_res
+    line = {"metric": KERNELS_METRIC, "value": 1e3 / total_ms, "unit": "iterations/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "one tangent + factorisation, one 2-RHS solve and one residual of the degree-2 "
+                                   "128x128 roof (49,920 free dofs) at a small deformation",
+                       "l2": "inputs larger than L2 (fronts %.0f MB)" % (stats["front_bytes"] / 1e6),
+                       "hbm_peak_gbs": hbm},
+            "kernels": detail, "gpu_launches": int(launches)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -991,7 +1063,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--lean", action="store_true", help="timed leg only (no e2e / profile / CPU legs)")
-    ap.add_argument("--workload", default="arc-length", choices=["arc-length", "batched", "ramp", "eigen", "pcg"],
+    ap.add_argument("--workload", default="arc-length", choices=["arc-length", "batched", "ramp", "eigen", "pcg", "kernels"],
                     help="arc-length: the headline path-following workload; batched: 256 uneven Newton solves; "
                          "ramp: degree-3 static Newton load ramp; eigen: buckling + modal at 201k dofs")
     ap.add_argument("--batch", type=int, default=BATCH_N, help="instances per GPU of the batched workload")
@@ -1001,6 +1073,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "pcg":
         return run_pcg(args)
+    if args.workload == "kernels":
+        return run_kernels(args)
     if args.workload == "ramp":
         return run_ramp(args)
     if args.workload == "eigen":

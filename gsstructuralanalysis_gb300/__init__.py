@@ -113,6 +113,8 @@ SIGNATURES = {
     "klsa_predictor_create": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, ctypes.POINTER(_c_vp)]),
     "klsa_predictor_destroy": (_c_int, [_c_vp]),
     "klsa_predictor_reset": (_c_int, [_c_vp]),
+    "klsa_predictor_push": (_c_int, [_c_vp, _c_vp, _c_dbl]),
+    "klsa_predictor_guess": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "klsa_alm_step_learned": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "klsa_buckling": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_dbl, _c_vp, _c_vp]),
     "klsa_modal": (_c_int, [_c_vp, _c_vp, _c_int, _c_dbl, _c_vp, _c_vp]),
@@ -787,6 +789,19 @@ class Predictor:
 
     def reset(self):
         _check(_lib.klsa_predictor_reset(self.h))
+
+    def push(self, U, L):
+        """Record a converged point (public order)."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(_lib.klsa_predictor_push(self.h, _ptr(U), float(L)))
+
+    def guess(self):
+        """(U, L) of the predicted next point, or None while fewer than four points are recorded."""
+        U = np.zeros(self.problem.ndof)
+        L = np.zeros(1)
+        ok = np.zeros(1, dtype=np.int32)
+        _check(_lib.klsa_predictor_guess(self.h, _ptr(U), _ptr(L), _ptr(ok)))
+        return (U, float(L[0])) if ok[0] else None
 
     def step(self, alm, guess_max_iter=6):
         used = np.zeros(1, dtype=np.int32)

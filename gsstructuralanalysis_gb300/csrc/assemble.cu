@@ -65,7 +65,7 @@ __constant__ unsigned char c_pairB[4][325];
 // Gauss-point state shared by all lanes (computed redundantly per lane).
 template <class T> struct QPState {
     V3T<T> a1, a2, x11, x22, x12, a3, v, w;
-    T l, il, il2, c;
+    T il, il2, c;
     T n[3], m[3];
     T Cm[3][3], Cb[3][3];
     T dV;
@@ -80,12 +80,8 @@ __device__ __forceinline__ void qp_state(const double* __restrict__ geo, const T
     s.x11 = mk<T>(X11.x + du[6], X11.y + du[7], X11.z + du[8]);
     s.x22 = mk<T>(X22.x + du[9], X22.y + du[10], X22.z + du[11]);
     s.x12 = mk<T>(X12.x + du[12], X12.y + du[13], X12.z + du[14]);
-    V3T<T> At = cross3(A1, A2);
-    T J0 = sqrt(dot3(At, At));
-    V3T<T> A3 = mk<T>(At.x / J0, At.y / J0, At.z / J0);
     V3T<T> at = cross3(s.a1, s.a2);
-    s.l = sqrt(dot3(at, at));
-    s.il = T(1) / s.l;
+    s.il = rsqrt(dot3(at, at));
     s.il2 = s.il * s.il;
     s.a3 = mk<T>(at.x * s.il, at.y * s.il, at.z * s.il);
     // membrane strain from displacement-gradient terms (avoids cancellation a.a - A.A)
@@ -93,9 +89,10 @@ __device__ __forceinline__ void qp_state(const double* __restrict__ geo, const T
     T e0 = dot3(A1, d1) + T(0.5) * dot3(d1, d1);
     T e1 = dot3(A2, d2) + T(0.5) * dot3(d2, d2);
     T e2 = dot3(A1, d2) + dot3(d1, A2) + dot3(d1, d2);
-    T k0 = dot3(X11, A3) - dot3(s.x11, s.a3);
-    T k1 = dot3(X22, A3) - dot3(s.x22, s.a3);
-    T k2 = T(2) * (dot3(X12, A3) - dot3(s.x12, s.a3));
+    // reference curvature coefficients X,ab.A3 precomputed per Gauss point
+    T k0 = T(geo[22]) - dot3(s.x11, s.a3);
+    T k1 = T(geo[23]) - dot3(s.x22, s.a3);
+    T k2 = T(2) * (T(geo[24]) - dot3(s.x12, s.a3));
     T C00 = geo[15], C01 = geo[16], C02 = geo[17], C11 = geo[18], C12 = geo[19], C22 = geo[20];
     T C[3][3] = {{C00, C01, C02}, {C01, C11, C12}, {C02, C12, C22}};
 #pragma unroll
@@ -195,7 +192,7 @@ __device__ __forceinline__ void tangent_element(int e, int m1, int n1, int ncp, 
                         N22 * ux, N22 * uy, N22 * uz, N12 * ux, N12 * uy, N12 * uz};
 #pragma unroll
             for (int k = 0; k < 15; ++k) du[k] = warp_sum(du[k]);
-            const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * 22;
+            const double* geo = qpgeo + ((size_t)e * nq * nq + q2 * nq + q1) * QGEO;
             QPState<T> st;
             qp_state<P, T>(geo, du, tm, tb, st);
             if (own) cp_data<T>(st, N1, N2, N11, N22, N12, smw[lane], true);
@@ -343,7 +340,7 @@ __device__ __forceinline__ void fint_group(int grp, int nel, int m1, int n1, int
                 du[3 * g + 2] += Ns[g] * u[2];
             }
         }
-        const double* geo = qpgeo + ((size_t)e * nqp + idx) * 22;
+        const double* geo = qpgeo + ((size_t)e * nqp + idx) * QGEO;
         QPState<double> st;
         qp_state<P, double>(geo, du, tm, tb, st);
         // f_{A,i} = sum_qp [N1 G1 + N2 G2 - N11 S11 - N22 S22 - N12 S12]_i with
@@ -441,7 +438,7 @@ __device__ __forceinline__ void fint_group_df(int grp, int nel, int m1, int n1, 
         double dud[15];
 #pragma unroll
         for (int k = 0; k < 15; ++k) dud[k] = df_to_double(du[k]);
-        const double* geo = qpgeo + ((size_t)e * nqp + idx) * 22;
+        const double* geo = qpgeo + ((size_t)e * nqp + idx) * QGEO;
         QPState<double> st;
         qp_state<P, double>(geo, dud, tm, tb, st);
         const double dV = st.dV;
@@ -592,7 +589,7 @@ __global__ void __launch_bounds__(128) kl_mass_kernel(int nel, int m1, int nq, c
                 Ns[warp][lane] = t1[lane % NB1] * t2[lane / NB1];
             }
             __syncwarp();
-            double dV = qpgeo[((size_t)e * nq * nq + q2 * nq + q1) * 22 + 21];
+            double dV = qpgeo[((size_t)e * nq * nq + q2 * nq + q1) * QGEO + 21];
             for (int s = 0; s < NPS; ++s) {
                 int pi = lane + 32 * s;
                 if (pi < NPAIR) acc[s] += rhot * Ns[warp][c_pairA[P - 1][pi]] * Ns[warp][c_pairB[P - 1][pi]] * dV;

@@ -149,10 +149,12 @@ static int residual_impl(klsa_problem* prob, const double* x, double lambda, boo
         Problem& P = *prob->P;
         ensure(prob->x, P.nfree); ensure(prob->r, P.nfree); ensure(prob->f, P.nfree);
         P.upload_pub(x, prob->x.get());
+        cudaEvent_t ev = g_timer.begin(P.stream);
         P.set_displacement(prob->x.get());
         P.internal_force(prob->f.get());
         if (al) vec::lincomb(1.0, prob->f.get(), -lambda, P.d_F.get(), prob->r.get(), P.nfree, P.stream);
         else vec::lincomb(1.0, P.d_F.get(), -1.0, prob->f.get(), prob->r.get(), P.nfree, P.stream);
+        g_timer.end(P.stream, 3, ev);
         P.download_pub(prob->r.get(), R);
         return KLSA_SUCCESS;
     });
@@ -705,6 +707,29 @@ int klsa_predictor_reset(klsa_predictor* pr) {
     if (!pr) return KLSA_INVALID_ARGUMENT;
     pr->pred->reset();
     return KLSA_SUCCESS;
+}
+int klsa_predictor_push(klsa_predictor* pr, const double* U, double L) {
+    if (!pr || !U) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *pr->prob->P;
+        P.upload_pub(U, pr->ug.get());
+        pr->pred->push(pr->ug.get(), L);
+        return KLSA_SUCCESS;
+    });
+}
+int klsa_predictor_guess(klsa_predictor* pr, double* U, double* L, int* available) {
+    if (!pr || !U || !L) return KLSA_INVALID_ARGUMENT;
+    return guarded([&] {
+        Problem& P = *pr->prob->P;
+        double Lg = 0.0;
+        const bool ok = pr->pred->guess(pr->ug.get(), &Lg);
+        if (available) *available = ok ? 1 : 0;
+        if (ok) {
+            P.download_pub(pr->ug.get(), U);
+            *L = Lg;
+        }
+        return KLSA_SUCCESS;
+    });
 }
 int klsa_alm_step_learned(klsa_alm* a, klsa_predictor* pr, int guess_max_iter, int* used_guess) {
     if (!a || !pr || pr->prob != a->prob) return KLSA_INVALID_ARGUMENT;

@@ -51,9 +51,11 @@ __global__ void __launch_bounds__(DOT_THREADS) multidot_kernel(DotArgs args, int
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        double v = s[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[k][warp] = v;
+        if (k < npairs) {
+            double v = s[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[k][warp] = v;
+        }
     }
     __syncthreads();
     if (threadIdx.x < npairs) {

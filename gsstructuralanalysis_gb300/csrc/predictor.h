@@ -10,29 +10,33 @@
 namespace klsa {
 
 struct LearnedPredictor {
+    static constexpr int PCH = 16;  // chunks of the projection (partial sums per chunk and mode)
+
     Problem& P;
     MLP* net;                       // may be null: plain cubic extrapolation (ablation)
     int nm;
     DevBuf<double> Phi;             // n x nm, internal order, column j at j*n (orthonormal)
-    std::vector<double> in_mu, in_sd, out_mu, out_sd;
+    DevBuf<double> stats;           // in_mu | in_sd | out_mu | out_sd (4 (nm + 1) + 2 (nm + 1))
     DevBuf<double> hist;            // 4 x n ring of converged points
     double histL[4] = {0, 0, 0, 0};
-    std::vector<double> histq;      // 4 x nm projections
+    DevBuf<double> qpart;           // 4 x PCH x nm ring of the points' projection partial sums
+    DevBuf<double> corr;            // nm + 1: network correction (dq, dL), destandardised
+    double* corrL_host = nullptr;   // pinned copy of corr[nm]
     int count = 0, head = 0;
-    DevBuf<double> dq, part;        // device scratch for projections / GEMV coefficients
-    DevBuf<float> feat;
-    std::vector<double> hpart;
 
     LearnedPredictor(Problem& P, MLP* net, const double* modes_pub, int nm, const double* in_mu,
                      const double* in_sd, const double* out_mu, const double* out_sd);
+    ~LearnedPredictor();
+    LearnedPredictor(const LearnedPredictor&) = delete;
+    LearnedPredictor& operator=(const LearnedPredictor&) = delete;
     void reset() { count = 0; head = 0; }
-    // record a converged point (device vector, internal order)
+    // record a converged point (device vector, internal order); no host synchronisation
     void push(const double* dU, double L);
-    // guess for the next point (needs 4 points); writes the device vector Ug (internal order)
+    // guess for the next point (needs 4 points); writes the device vector Ug (internal order).
+    // With a network: one read of the load-factor correction (one stream synchronisation).
     bool guess(double* dUg, double* Lg);
 
 private:
-    void project(const double* dU, double* q);
     int slot(int back) const { return (head - 1 - back + 8) & 3; }   // back = 0: newest
 };
 

@@ -166,7 +166,7 @@ Problem::Problem(const klsa_patch_desc& d) {
     fill(U1, n1, m1, tab1, jw1);
     fill(U2, n2, m2, tab2, jw2);
 
-    std::vector<double> qpgeo((size_t)nqp * 22);
+    std::vector<double> qpgeo((size_t)nqp * QGEO);
     std::vector<double> F_full(3 * (size_t)ncp, 0.0);
     const double lam = E * nu / (1.0 - nu * nu), mu = E / (2.0 * (1.0 + nu));
     const bool has_surf = d.surface_load &&
@@ -193,7 +193,7 @@ Problem::Problem(const klsa_patch_desc& d) {
                     double det = g11 * g22 - g12 * g12;
                     double h11 = g22 / det, h22 = g11 / det, h12 = -g12 / det;   // contravariant metric
                     double dA = std::sqrt(dt(cr(A1, A2), cr(A1, A2))) * jw1[(size_t)e1 * nq + q1] * jw2[(size_t)e2 * nq + q2];
-                    double* g = &qpgeo[((size_t)e * nq * nq + q2 * nq + q1) * 22];
+                    double* g = &qpgeo[((size_t)e * nq * nq + q2 * nq + q1) * QGEO];
                     V3 vv[5] = {A1, A2, X11, X22, X12};
                     for (int k = 0; k < 5; ++k) { g[3 * k] = vv[k].x; g[3 * k + 1] = vv[k].y; g[3 * k + 2] = vv[k].z; }
                     g[15] = (lam + 2 * mu) * h11 * h11;                // C^{1111}
@@ -203,6 +203,12 @@ Problem::Problem(const klsa_patch_desc& d) {
                     g[19] = (lam + 2 * mu) * h22 * h12;                // C^{2212}
                     g[20] = lam * h12 * h12 + mu * (h11 * h22 + h12 * h12);   // C^{1212}
                     g[21] = dA;
+                    const V3 At = cr(A1, A2);
+                    const double J0 = std::sqrt(dt(At, At));
+                    const V3 A3{At.x / J0, At.y / J0, At.z / J0};
+                    g[22] = dt(X11, A3);
+                    g[23] = dt(X22, A3);
+                    g[24] = dt(X12, A3);
                     if (has_surf)
                         for (int b = 0; b < nb1; ++b)
                             for (int a = 0; a < nb1; ++a) {

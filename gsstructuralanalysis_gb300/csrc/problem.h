@@ -3,8 +3,10 @@
 // HBM layout (per problem)
 //   tab1/tab2   1-D B-spline values and 1st/2nd derivatives at the Gauss points of every
 //               element column/row: [m][nq][3][p+1] (FP64 and FP32 copies)
-//   qpgeo       per Gauss point: A1, A2, X,11, X,22, X,12 (reference, 15), the SVK material
-//               matrix in the contravariant reference metric (6) and the area weight (1), FP64
+//   qpgeo       per Gauss point (QGEO = 25 values): A1, A2, X,11, X,22, X,12 (reference, 15),
+//               the SVK material matrix in the contravariant reference metric (6), the area
+//               weight (1) and the reference curvature coefficients X,11.A3, X,22.A3, X,12.A3
+//               (3), FP64
 //   u_full      displacement in the component-blocked full layout, FP64
 //   elemK/elemR element tangents (d x d) and internal forces (d) of the last assembly
 //   CSR         rows = free dofs in internal (nested-dissection) order, int32 cols,
@@ -18,6 +20,10 @@
 #include <vector>
 
 #include "common.cuh"
+
+namespace klsa {
+constexpr int QGEO = 25;   // values per Gauss point in qpgeo
+}
 #include "multifrontal.h"
 #include "nd_symbolic.h"
 

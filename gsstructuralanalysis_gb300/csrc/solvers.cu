@@ -657,21 +657,35 @@ void ALMGPU::step_impl() {
     converged_ = false;
     num_it_ = 0;
     initiate_step();
-    bool use_guess = false;
-    if (has_guess_) {
-        double d;
-        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, P_.stream);
-        const double* a[1] = {tmp_.get()};
-        vec::multidot(1, a, a, n_, &d, P_.stream);
-        use_guess = d != 0 && (Lguess_ - L_) != 0;
+    // gsALMBase.hpp:365: the guess is used when (Uguess - U).norm() != 0 and Lguess != L.  A placed
+    // guess starts the corrector at DU = Uguess - U, whose norm comes back with the residual norms:
+    // the test is made there, and the step restarts from the tangent predictor if it fails.
+    bool use_guess = false, check_placed = false;
+    if (has_guess_ && (Lguess_ - L_) != 0) {
+        if (guess_place_) {
+            use_guess = check_placed = true;
+        } else {
+            double d;
+            vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, P_.stream);
+            const double* a[1] = {tmp_.get()};
+            vec::multidot(1, a, a, n_, &d, P_.stream);
+            use_guess = d != 0;
+        }
     }
     // frozen tangent: a placed guess, and the fronts still hold this solver's last Jacobian
-    const bool frozen = use_guess && guess_place_ && frozen_it_ > 0 && S_->has_ldlt() && !fact_stale_ &&
-                        jac_gen_ != 0 && jac_gen_ == S_->generation();
+    bool frozen = use_guess && guess_place_ && frozen_it_ > 0 && S_->has_ldlt() && !fact_stale_ &&
+                  jac_gen_ != 0 && jac_gen_ == S_->generation();
     if (use_guess) predictor_guess();
     else predictor();
     compute_residual();
     compute_residual_norms();
+    if (check_placed && basisU_ == 0) {   // Uguess == U
+        frozen = false;
+        initiate_step();
+        predictor();
+        compute_residual();
+        compute_residual_norms();
+    }
     if (quasi_) {
         // quasiNewtonPredictor (gsALMCrisfield.hpp:56-63, gsALMRiks.hpp:38-45,
         // gsALMLoadControl.hpp:23-29): the Jacobian at the predicted point U + DU, kept for the

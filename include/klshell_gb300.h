@@ -214,6 +214,12 @@ int klsa_predictor_create(klsa_problem* prob, klsa_mlp* net, const double* modes
                           const double* out_std, klsa_predictor** out);
 int klsa_predictor_destroy(klsa_predictor* pr);
 int klsa_predictor_reset(klsa_predictor* pr);
+/* Record a converged point (U: ndof, public order) in the predictor's history of four. */
+int klsa_predictor_push(klsa_predictor* pr, const double* U, double L);
+/* The predicted next point from the last four recorded ones (U: ndof, public order): the value a
+ * caller hands to gsALMBase::setInitialGuess (gsALMSolvers/gsALMBase.h:184).  available = 0 (and
+ * U, L untouched) while fewer than four points are recorded. */
+int klsa_predictor_guess(klsa_predictor* pr, double* U, double* L, int* available);
 /* One arc-length point with the learned guess placed as the corrector's start (at most
  * guess_max_iter iterations); on failure the step is redone with the plain tangent predictor.
  * Keeps the predictor's history of converged points.  used_guess (may be NULL) = 1 if the

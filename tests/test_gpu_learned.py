@@ -27,6 +27,73 @@ def test_mlp_gradient_matches_reference(lib):
     assert np.linalg.norm(g - gr) <= 1e-4 * np.linalg.norm(gr)
 
 
+def test_predictor_guess_matches_numpy_restatement(lib):
+    """Predictor.guess against a NumPy restatement of the learned guess: projections q = Phi U of
+    the last four recorded points (newest first), the 4 (nm + 1) standardised features, the
+    network (mlp_ref, FP64), the destandardised correction added to the cubic extrapolation
+    4 P_k - 6 P_{k-1} + 4 P_{k-2} - P_{k-3}.  Two predictors on two problems share one network
+    and run from two host threads at once, as the path-generation threads do."""
+    import threading
+    import gsstructuralanalysis_gb300 as G
+    import mlp_ref
+    prob = P.cylindrical_panel(m=8, p=2, load=1.0)
+    gps = [G.Problem(prob), G.Problem(prob)]
+    n, nm = gps[0].ndof, 6
+    rng = np.random.default_rng(3)
+    Phi = np.linalg.qr(rng.standard_normal((n, nm)))[0].T.copy()
+    shape = (4 * (nm + 1), 16, 16, nm + 1)
+    net = G.MLP(*shape, seed=5)
+    p = (0.3 * rng.standard_normal(net.nparams)).astype(np.float32)
+    net.set_params(p)
+    in_mu, in_sd = 0.1 * rng.standard_normal(shape[0]), 0.5 + rng.random(shape[0])
+    out_mu, out_sd = 0.1 * rng.standard_normal(shape[3]), 0.5 + rng.random(shape[3])
+    preds = [G.Predictor(g, net, Phi, in_mu, in_sd, out_mu, out_sd) for g in gps]
+    npts = 40
+    paths = [[(1e-2 * (k + 1) * rng.standard_normal(n), 0.1 * (k + 1) + 0.01 * j) for k in range(npts)]
+             for j in range(2)]
+    got = [[None] * npts for _ in range(2)]
+
+    def run(j):
+        for k in range(npts):
+            preds[j].push(*paths[j][k])
+            got[j][k] = preds[j].guess()
+
+    threads = [threading.Thread(target=run, args=(j,)) for j in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+
+    def reference(pts):
+        (U0, L0), (U1, L1), (U2, L2), (U3, L3) = pts[::-1][:4]
+        q = [Phi @ U for U in (U0, U1, U2, U3)]
+        L = [L0, L1, L2, L3]
+        f = np.concatenate([np.append(q[0], L[0])] + [np.append(q[b] - q[0], L[b] - L[0]) for b in (1, 2, 3)])
+        X = ((f - in_mu) / in_sd).astype(np.float32).astype(np.float64)
+        Y, _ = mlp_ref.forward(p.astype(np.float64), shape, X[None, :])
+        corr = Y[0] * out_sd + out_mu
+        Ug = 4 * U0 - 6 * U1 + 4 * U2 - U3 + Phi.T @ corr[:nm]
+        return Ug, 4 * L0 - 6 * L1 + 4 * L2 - L3 + corr[nm], Phi.T @ corr[:nm]
+
+    for j in range(2):
+        for k in range(npts):
+            g = got[j][k]
+            if k < 3:
+                assert g is None
+                continue
+            Ug, Lg, dU = reference(paths[j][:k + 1])
+            assert np.linalg.norm(g[0] - Ug) <= 1e-5 * np.linalg.norm(dU) + 1e-12 * np.linalg.norm(Ug), (k, j)
+            assert abs(g[1] - Lg) <= 1e-5 * max(1.0, abs(Lg)), (k, j)
+    # without a network: the plain cubic extrapolation
+    ext = G.Predictor(gps[0], None, Phi)
+    for U, L in paths[0][:4]:
+        ext.push(U, L)
+    (U0, L0), (U1, L1), (U2, L2), (U3, L3) = paths[0][:4][::-1]
+    Ug, Lg = ext.guess()
+    assert np.linalg.norm(Ug - (4 * U0 - 6 * U1 + 4 * U2 - U3)) <= 1e-14 * np.linalg.norm(Ug)
+    assert abs(Lg - (4 * L0 - 6 * L1 + 4 * L2 - L3)) <= 1e-15 * abs(Lg)
+
+
 def test_mlp_training_fits_a_smooth_map(lib):
     import gsstructuralanalysis_gb300 as G
     rng = np.random.default_rng(5)
