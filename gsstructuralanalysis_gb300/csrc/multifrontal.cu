@@ -744,11 +744,11 @@ __device__ __forceinline__ T mf_child_sum(const SolveArgs<T>& a, int nd, int pos
     T s = T(0);
     if (iv.x >= 0) {
         const int c = a.child0[nd];
-        s += a.upd[a.upd_off[c] + iv.x + (int64_t)(a.f[c] - a.k[c]) * q];
+        s += __ldcg(a.upd + a.upd_off[c] + iv.x + (int64_t)(a.f[c] - a.k[c]) * q);
     }
     if (iv.y >= 0) {
         const int c = a.child1[nd];
-        s += a.upd[a.upd_off[c] + iv.y + (int64_t)(a.f[c] - a.k[c]) * q];
+        s += __ldcg(a.upd + a.upd_off[c] + iv.y + (int64_t)(a.f[c] - a.k[c]) * q);
     }
     return s;
 }
@@ -810,7 +810,7 @@ __device__ __forceinline__ void mf_pt_halo(const SolveArgs<T>& a, int4 it, T (*v
     const int r0 = ab * NB, c0 = cb * NB;
     for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
         const int q = e / NB, m = e % NB, col = c0 + m;
-        vs[q][m] = col < kN ? a.z[o + col + (int64_t)n * q] : T(0);
+        vs[q][m] = col < kN ? __ldcg(a.z + o + col + (int64_t)n * q) : T(0);
     }
     __syncthreads();
     const T* F = a.pool + a.front_off[nd] + kN;
@@ -855,7 +855,7 @@ __device__ __forceinline__ void mf_pt_bwd_z(const SolveArgs<T>& a, int4 it, T (*
     const int* hl = a.halo + a.halo_off[nd];
     for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
         const int q = e / NB, rl = e % NB, r = r0 + rl;
-        vs[q][rl] = r < hN ? a.x[hl[r] + (int64_t)n * q] : T(0);
+        vs[q][rl] = r < hN ? __ldcg(a.x + hl[r] + (int64_t)n * q) : T(0);
     }
     __syncthreads();
     const T* F = a.pool + a.front_off[nd] + kN;
@@ -889,7 +889,7 @@ __device__ __forceinline__ void mf_pt_bwd_own(const SolveArgs<T>& a, int4 it, T 
     const int r0 = ib * NB, c0 = jb * NB;
     for (int e = threadIdx.x; e < NR * NB; e += blockDim.x) {
         const int q = e / NB, rl = e % NB, i = r0 + rl;
-        vs[q][rl] = i < kN ? a.z[o + i + (int64_t)n * q] / a.D[o + i] + a.w[o + i + (int64_t)n * q] : T(0);
+        vs[q][rl] = i < kN ? __ldcg(a.z + o + i + (int64_t)n * q) / a.D[o + i] + __ldcg(a.w + o + i + (int64_t)n * q) : T(0);
     }
     __syncthreads();
     const T* X = a.xinv + a.xinv_off[nd];
@@ -969,6 +969,212 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_solve_persistent_kernel(Solv
             __syncthreads();
         }
         if (L > 0) grid.sync();
+    }
+}
+
+// ---- the same tile products as a dataflow schedule ---------------------------------------------
+// One queue lists every tile of four phases in a topological order (forward: per level from the
+// leaves, A then B; backward: per level from the root, C then D).  The forward sweep fans out:
+// r starts as b, and a node's L21 z is subtracted straight from r at the node's halo rows (global
+// dofs), so a node reads its right-hand side r(own) without gathering its children's update
+// vectors:
+//   A  z(rows rb) += X(rb, cb) r(own cols cb)            waits for the children's A and B
+//   B  r(halo rows ab) -= L21(ab, cb) z(cb)              waits for the node's A
+//   C  w(cols cb) -= L21(ab, cb)^T x(halo rows ab)       waits for the parent's D
+//   D  x(cols jb) += X(ib, jb)^T (z / D + w)(ib)         waits for the node's A and C
+// A node's A finds every contribution to its own rows in r once its children are complete: each
+// child waited for its own children, so the whole subtree has subtracted.  The parent's D waited
+// for its C, which waited for the grandparent's D, so C reads final x on every halo row.
+// CTAs take tiles from the queue head in order; the earliest unfinished tile always has its
+// inputs complete and a cooperative launch keeps every CTA resident, so the schedule cannot
+// deadlock.  A tile loads its block of X or L21 (and its halo indices) before it waits: those do
+// not depend on the solve, so their memory latency hides behind the wait.  Completion counters
+// are raised with a fence + atomic add after the tile's __syncthreads and polled with ld.acquire;
+// data written by other CTAs is read through L2 (__ldcg).  Every wait is bounded (clock64
+// budget): on expiry the CTA writes NaN into the solution (NaN survives the later atomic
+// additions), counts the tile as done and goes on, so the launch always ends and the caller sees
+// a non-finite solution.
+struct DataflowArgs {
+    const int* queue;        // (phase << 29) | item index
+    int qtotal;
+    const int* own_tiles;    // per node: tiles of X (phases A, D)
+    const int* halo_tiles;   // per node: tiles of L21 (phases B, C)
+    const int* parent;
+    int* cnt;                // 4 x nnodes completion counters, then the queue head
+    int nnodes;
+    int stall_node;          // test hook: this node's A never counts as complete (-1: off)
+    long long wait_cycles;
+};
+
+__device__ __forceinline__ int mf_ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// spin until *p >= target; false when the budget ran out
+__device__ __forceinline__ bool mf_wait_count(const int* p, int target, long long t0, long long budget) {
+    for (unsigned it = 0;; ++it) {
+        if (mf_ld_acquire(p) >= target) return true;
+        if (clock64() - t0 > budget || it > (1u << 26)) return false;
+        __nanosleep(64);
+    }
+}
+
+__device__ __forceinline__ void mf_poison(float* p) { atomicExch(p, __int_as_float(0x7fffffff)); }
+__device__ __forceinline__ void mf_poison(double* p) {
+    atomicExch(reinterpret_cast<unsigned long long*>(p), 0x7fffffffffffffffULL);
+}
+
+template <class T, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS) mf_solve_dataflow_kernel(SolveArgs<T> a, DataflowArgs d, T* r) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ T vs[NR][NB];
+    __shared__ T part[8][NR][NB];
+    __shared__ int s_q;
+    const int64_t nn = (int64_t)a.n * NR;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+        r[e] = a.b[e];
+        a.z[e] = T(0);
+        a.w[e] = T(0);
+        a.x[e] = T(0);
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e <= 4 * d.nnodes; e += gridDim.x * blockDim.x) d.cnt[e] = 0;
+    grid.sync();
+    int* cntA = d.cnt;
+    int* cntB = d.cnt + d.nnodes;
+    int* cntC = d.cnt + 2 * d.nnodes;
+    int* cntD = d.cnt + 3 * d.nnodes;
+    int* head = d.cnt + 4 * d.nnodes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n = a.n;
+    for (;;) {
+        if (threadIdx.x == 0) s_q = atomicAdd(head, 1);
+        __syncthreads();
+        const int q = s_q;
+        if (q >= d.qtotal) break;
+        const int code = d.queue[q], phase = code >> 29;
+        const int4 it = a.items[code & ((1 << 29) - 1)];
+        const int nd = it.x, kN = a.k[nd], fN = a.f[nd], hN = fN - kN, o = a.own[nd];
+        const int r0 = it.y * NB, c0 = it.z * NB;
+        // 1. the tile's block of X (A, D) or L21 (B, C) and its halo indices, before the wait
+        T m[8][2];
+        int hrow = 0;
+        if (phase == 0 || phase == 3) {
+            const T* X = a.xinv + a.xinv_off[nd];
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int i = r0 + warp + 8 * s;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = c0 + lane + 32 * h;
+                    m[s][h] = (i < kN && j < kN && j <= i) ? X[(int64_t)i * kN + j] : T(0);
+                }
+            }
+        } else {
+            const T* F = a.pool + a.front_off[nd] + kN;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int j = c0 + warp + 8 * s;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int rr = r0 + lane + 32 * h;
+                    m[s][h] = (j < kN && rr < hN) ? F[(int64_t)j * fN + rr] : T(0);
+                }
+            }
+            const int rl = threadIdx.x % NB;
+            if (threadIdx.x < NR * NB && r0 + rl < hN) hrow = a.halo[a.halo_off[nd] + r0 + rl];
+        }
+        // 2. wait for the tiles this one reads
+        if (threadIdx.x == 0) {
+            const long long t0 = clock64();
+            bool ok = true;
+            if (phase == 0) {
+                const int c[2] = {a.child0[nd], a.child1[nd]};
+                for (int h = 0; h < 2; ++h)
+                    if (c[h] >= 0) {
+                        const int needA = d.own_tiles[c[h]] + (c[h] == d.stall_node ? 1 : 0);
+                        ok = ok && mf_wait_count(cntA + c[h], needA, t0, d.wait_cycles);
+                        ok = ok && mf_wait_count(cntB + c[h], d.halo_tiles[c[h]], t0, d.wait_cycles);
+                    }
+            } else if (phase == 1) {
+                ok = mf_wait_count(cntA + nd, d.own_tiles[nd], t0, d.wait_cycles);
+            } else if (phase == 2) {
+                const int p = d.parent[nd];   // a node with halo rows has a parent
+                ok = p >= 0 && mf_wait_count(cntD + p, d.own_tiles[p], t0, d.wait_cycles);
+            } else {
+                ok = mf_wait_count(cntA + nd, d.own_tiles[nd], t0, d.wait_cycles) &&
+                     mf_wait_count(cntC + nd, d.halo_tiles[nd], t0, d.wait_cycles);
+            }
+            if (!ok)
+#pragma unroll
+                for (int rr = 0; rr < NR; ++rr) mf_poison(a.x + (int64_t)n * rr);
+        }
+        __syncthreads();
+        // 3. the vector part, then the tile product
+        if (threadIdx.x < NR * NB) {
+            const int qq = threadIdx.x / NB, e = threadIdx.x % NB;
+            T v = T(0);
+            if (phase == 0) {
+                if (c0 + e < kN) v = __ldcg(r + o + c0 + e + (int64_t)n * qq);
+            } else if (phase == 1) {
+                if (c0 + e < kN) v = __ldcg(a.z + o + c0 + e + (int64_t)n * qq);
+            } else if (phase == 2) {
+                if (r0 + e < hN) v = __ldcg(a.x + hrow + (int64_t)n * qq);
+            } else {
+                const int i = r0 + e;
+                if (i < kN) v = __ldcg(a.z + o + i + (int64_t)n * qq) / a.D[o + i] + __ldcg(a.w + o + i + (int64_t)n * qq);
+            }
+            vs[qq][e] = v;
+        }
+        __syncthreads();
+        if (phase == 0 || phase == 2) {
+            // lanes over the tile's columns: one warp sum per row (A) or column (C) and right-hand side
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+#pragma unroll
+                for (int qq = 0; qq < NR; ++qq) {
+                    const T v = mf_warp_sum(m[s][0] * vs[qq][lane] + m[s][1] * vs[qq][lane + 32]);
+                    if (lane == 0) {
+                        if (phase == 0) {
+                            const int i = r0 + warp + 8 * s;
+                            if (i < kN) atomicAdd(a.z + o + i + (int64_t)n * qq, v);
+                        } else {
+                            const int j = c0 + warp + 8 * s;
+                            if (j < kN) atomicAdd(a.w + o + j + (int64_t)n * qq, -v);
+                        }
+                    }
+                }
+            }
+        } else {
+            // warps over the tile's rows (B: own columns j, D: rows i), partial sums in shared memory
+#pragma unroll
+            for (int qq = 0; qq < NR; ++qq)
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int s = 0; s < 8; ++s) acc += m[s][h] * vs[qq][warp + 8 * s];
+                    part[warp][qq][lane + 32 * h] = acc;
+                }
+            __syncthreads();
+            if (threadIdx.x < NR * NB) {
+                const int qq = threadIdx.x / NB, e = threadIdx.x % NB;
+                T acc = T(0);
+#pragma unroll
+                for (int w = 0; w < 8; ++w) acc += part[w][qq][e];
+                if (phase == 1) {
+                    if (r0 + e < hN) atomicAdd(r + hrow + (int64_t)n * qq, -acc);
+                } else {
+                    if (c0 + e < kN) atomicAdd(a.x + o + c0 + e + (int64_t)n * qq, acc);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd((phase == 0 ? cntA : phase == 1 ? cntB : phase == 2 ? cntC : cntD) + nd, 1);
+        }
     }
 }
 
@@ -1224,6 +1430,36 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
         // every node with a halo needs an own tile (0, 0) to start its update vector
         for (int i = 0; i < nnodes_; ++i)
             if (k[i] == 0 && f[i] > 0) persistent_ok_ = false;
+        // dataflow schedule: the queue in topological order and the tiles per node and phase
+        std::vector<int> queue, own_t(nnodes_, 0), halo_t(nnodes_, 0);
+        const SolveLevels& sl = *solve_levels_;
+        if (items.size() >= (size_t(1) << 29)) persistent_ok_ = false;
+        for (int L = 0; L < nlevels_; ++L) {
+            for (int q = sl.own_off[L]; q < sl.own_off[L] + sl.own_cnt[L]; ++q) {
+                queue.push_back(q);
+                ++own_t[items[q].x];
+            }
+            for (int q = sl.halo_off[L]; q < sl.halo_off[L] + sl.halo_cnt[L]; ++q) {
+                queue.push_back((1 << 29) | q);
+                ++halo_t[items[q].x];
+            }
+        }
+        for (int L = nlevels_ - 1; L >= 0; --L) {
+            for (int q = sl.halo_off[L]; q < sl.halo_off[L] + sl.halo_cnt[L]; ++q) queue.push_back((2 << 29) | q);
+            for (int q = sl.own_off[L]; q < sl.own_off[L] + sl.own_cnt[L]; ++q) queue.push_back((3 << 29) | q);
+        }
+        df_qtotal_ = (int)queue.size();
+        df_queue_.upload(queue, stream_);
+        df_own_t_.upload(own_t, stream_);
+        df_halo_t_.upload(halo_t, stream_);
+        df_cnt_.alloc((size_t)4 * nnodes_ + 1);
+        df_r_.alloc((size_t)std::max(n_, 1) * MF_MAX_RHS);
+        if (const char* e = std::getenv("KLSA_SOLVE_STALL_NODE")) {
+            // the k-th leaf of the elimination tree (a leaf has a parent unless the tree is one node)
+            const auto& leaves = level_nodes_[0];
+            const int kk = std::max(0, std::atoi(e));
+            if (!leaves.empty()) df_stall_node_ = leaves[std::min<size_t>(kk, leaves.size() - 1)];
+        }
     }
     d_f_.upload(f, stream_); d_k_.upload(k, stream_); d_own_.upload(own, stream_); d_parent_.upload(parent, stream_);
     d_child0_.upload(c0, stream_); d_child1_.upload(c1, stream_);
@@ -1280,12 +1516,17 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
         const void* fns[3] = {(const void*)mf_solve_persistent_kernel<T, 1>, (const void*)mf_solve_persistent_kernel<T, 2>,
                               (const void*)mf_solve_persistent_kernel<T, 4>};
         const int nrs[3] = {1, 2, 4};
+        const void* dfs[3] = {(const void*)mf_solve_dataflow_kernel<T, 1>, (const void*)mf_solve_dataflow_kernel<T, 2>,
+                              (const void*)mf_solve_dataflow_kernel<T, 4>};
         for (int v = 0; v < 3; ++v) {
             (void)nrs;
             ps_smem_[v] = 0;
             int bps = 0;
             KL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fns[v], SOLVE_THREADS, ps_smem_[v]));
             ps_grid_[v] = coop ? sms * std::min(bps, cap) : 0;
+            bps = 0;
+            KL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dfs[v], SOLVE_THREADS, 0));
+            df_grid_[v] = coop ? sms * std::min(bps, cap) : 0;
         }
     }
     const int gsm = (int)gemm_smem(sizeof(T));
@@ -1512,6 +1753,26 @@ void MultifrontalT<T>::solve_persistent(const T* d_b, T* d_x) {
     a.halo_off = d_halo_off_.get(); a.inv_off = d_inv_off_.get();
     a.pool = pool_.get(); a.xinv = xinv_.get(); a.D = D_.get(); a.b = d_b;
     a.x = d_x; a.z = z_.get(); a.w = y_.get(); a.upd = upd_.get();
+    const char* sel = std::getenv("KLSA_SOLVE_KERNEL");
+    const bool barrier = sel && std::string(sel) == "barrier";
+    if (!barrier && df_grid_[v] > 0) {
+        DataflowArgs d;
+        d.queue = df_queue_.get();
+        d.qtotal = df_qtotal_;
+        d.own_tiles = df_own_t_.get();
+        d.halo_tiles = df_halo_t_.get();
+        d.parent = d_parent_.get();
+        d.cnt = df_cnt_.get();
+        d.nnodes = nnodes_;
+        d.stall_node = df_stall_node_;
+        d.wait_cycles = 200000000LL;   // about 0.1 s at the GB300 SM clock
+        T* rws = df_r_.get();
+        void* args[3] = {&a, &d, &rws};
+        KL_CUDA(cudaLaunchCooperativeKernel((const void*)mf_solve_dataflow_kernel<T, NR>, dim3(df_grid_[v]),
+                                            dim3(SOLVE_THREADS), args, 0, stream_));
+        count_launch();
+        return;
+    }
     void* args[2] = {&a, solve_levels_};
     KL_CUDA(cudaLaunchCooperativeKernel((const void*)mf_solve_persistent_kernel<T, NR>, dim3(ps_grid_[v]),
                                         dim3(SOLVE_THREADS), args, ps_smem_[v], stream_));
@@ -1520,10 +1781,8 @@ void MultifrontalT<T>::solve_persistent(const T* d_b, T* d_x) {
 
 template <class T>
 bool MultifrontalT<T>::persistent_solve_enabled() const {
-    static const bool levels = [] {
-        const char* e = std::getenv("KLSA_SOLVE_KERNEL");
-        return e && std::string(e) == "levels";
-    }();
+    const char* e = std::getenv("KLSA_SOLVE_KERNEL");
+    const bool levels = e && std::string(e) == "levels";
     return !levels && persistent_ok_ && ps_grid_[0] > 0;
 }
 

@@ -91,6 +91,13 @@ private:
     DevBuf<int64_t> d_inv_off_;
     DevBuf<int> d_inv_;
     int ps_grid_[3] = {0, 0, 0};
+    // dataflow variant of the persistent solve (default; KLSA_SOLVE_KERNEL=barrier selects the
+    // level-barrier kernel): queue of (phase, tile), tiles per node, completion counters
+    DevBuf<int> df_queue_, df_own_t_, df_halo_t_, df_cnt_;
+    DevBuf<T> df_r_;             // fan-out right-hand side (n x MF_MAX_RHS)
+    int df_qtotal_ = 0;
+    int df_grid_[3] = {0, 0, 0};
+    int df_stall_node_ = -1;     // test hook (KLSA_SOLVE_STALL_NODE=k): the k-th leaf's first phase never completes
     bool persistent_ok_ = true;
     size_t ps_smem_[3] = {0, 0, 0};
     GraphSlot fact_graph_, solve_graph_[3];

@@ -46,37 +46,36 @@ struct InferArgs {
     int nm, in, h1, h2, out;
     const double* stats;   // in_mu[in] in_sd[in] out_mu[out] out_sd[out]
     const float *W1, *b1, *W2, *b2, *W3, *b3;
+    float *y1, *y2;        // hidden activations (predictor's own scratch)
     double* corr;          // out: destandardised network output
 };
 
-// one dense layer of the network for one input row: warp w owns outputs w, w + nwarps, ...; the
-// lanes read a weight row in consecutive 128-byte pieces and the warp sums their products
-template <bool GELU>
-__device__ __forceinline__ void dense_warp_layer(int nout, int nin, const float* __restrict__ W,
-                                                 const float* __restrict__ b, const float* x, float* y) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < nout; r += nw) {
-        const float* w = W + (size_t)r * nin;
-        float acc = 0.f;
-        for (int k = lane; k < nin; k += 32) acc = fmaf(x[k], w[k], acc);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            acc += b[r];
-            if (GELU) acc = 0.5f * acc * (1.f + erff(acc * 0.70710678118654752f));
-            y[r] = acc;
-        }
+constexpr int ROWS_PER_CTA = 8;   // one warp per output row
+
+// one output row of a dense layer: the lanes walk the weight row in 128-byte pieces with four
+// independent partial sums (four loads in flight per lane), then the warp adds them up
+__device__ __forceinline__ float dense_row(const float* __restrict__ w, const float* x, int nin, int lane) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = lane;
+    for (; k + 96 < nin; k += 128) {
+        s0 = fmaf(x[k], w[k], s0);
+        s1 = fmaf(x[k + 32], w[k + 32], s1);
+        s2 = fmaf(x[k + 64], w[k + 64], s2);
+        s3 = fmaf(x[k + 96], w[k + 96], s3);
     }
+    for (; k < nin; k += 32) s0 = fmaf(x[k], w[k], s0);
+    float acc = (s0 + s1) + (s2 + s3);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
 }
 
-// features of the last four points -> network -> corr (one CTA of 32 warps; the weights stay in L2)
-__global__ void __launch_bounds__(1024) infer_kernel(InferArgs a) {
-    extern __shared__ float sm[];
-    float* x = sm;
-    float* y1 = x + a.in;
-    float* y2 = y1 + a.h1;
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+
+// features of the last four points (every CTA builds them in shared memory) and the first layer
+__global__ void __launch_bounds__(256) infer_l1_kernel(InferArgs a) {
+    extern __shared__ float x[];
     const int M1 = a.nm + 1;
-    const double *in_mu = a.stats, *in_sd = a.stats + a.in, *out_mu = a.stats + 2 * a.in,
-                 *out_sd = a.stats + 2 * a.in + a.out;
+    const double *in_mu = a.stats, *in_sd = a.stats + a.in;
     for (int idx = threadIdx.x; idx < a.in; idx += blockDim.x) {
         const int b = idx / M1, j = idx % M1;
         double v;
@@ -95,14 +94,33 @@ __global__ void __launch_bounds__(1024) infer_kernel(InferArgs a) {
         x[idx] = (float)((v - in_mu[idx]) / in_sd[idx]);
     }
     __syncthreads();
-    dense_warp_layer<true>(a.h1, a.in, a.W1, a.b1, x, y1);
+    const int lane = threadIdx.x & 31, r = blockIdx.x * ROWS_PER_CTA + (threadIdx.x >> 5);
+    if (r < a.h1) {
+        const float acc = dense_row(a.W1 + (size_t)r * a.in, x, a.in, lane);
+        if (lane == 0) a.y1[r] = gelu(acc + a.b1[r]);
+    }
+}
+
+// a hidden or output layer: the input row staged in shared memory, one warp per output row
+template <int LAYER>
+__global__ void __launch_bounds__(256) infer_layer_kernel(InferArgs a) {
+    extern __shared__ float x[];
+    const int nin = LAYER == 2 ? a.h1 : a.h2, nout = LAYER == 2 ? a.h2 : a.out;
+    const float* src = LAYER == 2 ? a.y1 : a.y2;
+    for (int k = threadIdx.x; k < nin; k += blockDim.x) x[k] = src[k];
     __syncthreads();
-    dense_warp_layer<true>(a.h2, a.h1, a.W2, a.b2, y1, y2);
-    __syncthreads();
-    float* y3 = x;   // the features are no longer needed (in >= out)
-    dense_warp_layer<false>(a.out, a.h2, a.W3, a.b3, y2, y3);
-    __syncthreads();
-    for (int j = threadIdx.x; j < a.out; j += blockDim.x) a.corr[j] = (double)y3[j] * out_sd[j] + out_mu[j];
+    const int lane = threadIdx.x & 31, r = blockIdx.x * ROWS_PER_CTA + (threadIdx.x >> 5);
+    if (r >= nout) return;
+    const float* W = LAYER == 2 ? a.W2 : a.W3;
+    const float acc = dense_row(W + (size_t)r * nin, x, nin, lane);
+    if (lane == 0) {
+        if (LAYER == 2) {
+            a.y2[r] = gelu(acc + a.b2[r]);
+        } else {
+            const double *out_mu = a.stats + 2 * a.in, *out_sd = a.stats + 2 * a.in + a.out;
+            a.corr[r] = (double)(acc + a.b3[r]) * out_sd[r] + out_mu[r];
+        }
+    }
 }
 
 // Ug = 4 h0 - 6 h1 + 4 h2 - h3 + Phi dq (nm = 0: the plain cubic extrapolation)
@@ -149,6 +167,9 @@ LearnedPredictor::LearnedPredictor(Problem& P_, MLP* net_, const double* modes_p
     hist.alloc((size_t)4 * n);
     qpart.alloc((size_t)4 * PCH * std::max(nm, 1));
     corr.alloc(nout);
+    if (net) {
+        hid.alloc((size_t)net->h1 + net->h2);
+    }
     KL_CUDA(cudaMallocHost(&corrL_host, sizeof(double)));
     // the network's parameters are written on its own stream (training, set_params)
     if (net) KL_CUDA(cudaStreamSynchronize(net->stream));
@@ -198,9 +219,14 @@ bool LearnedPredictor::guess(double* dUg, double* Lg) {
         a.b2 = W + net->ob2();
         a.W3 = W + net->oW3();
         a.b3 = W + net->ob3();
+        a.y1 = hid.get();
+        a.y2 = hid.get() + a.h1;
         a.corr = corr.get();
-        const size_t smem = sizeof(float) * ((size_t)a.in + a.h1 + a.h2);
-        infer_kernel<<<1, 1024, smem, P.stream>>>(a);
+        infer_l1_kernel<<<ceil_div(a.h1, ROWS_PER_CTA), 256, sizeof(float) * a.in, P.stream>>>(a);
+        count_launch();
+        infer_layer_kernel<2><<<ceil_div(a.h2, ROWS_PER_CTA), 256, sizeof(float) * a.h1, P.stream>>>(a);
+        count_launch();
+        infer_layer_kernel<3><<<ceil_div(a.out, ROWS_PER_CTA), 256, sizeof(float) * a.h2, P.stream>>>(a);
         count_launch();
         KL_CHECK_LAUNCH();
     }

@@ -21,6 +21,7 @@ struct LearnedPredictor {
     double histL[4] = {0, 0, 0, 0};
     DevBuf<double> qpart;           // 4 x PCH x nm ring of the points' projection partial sums
     DevBuf<double> corr;            // nm + 1: network correction (dq, dL), destandardised
+    DevBuf<float> hid;              // hidden activations of the network (h1 + h2)
     double* corrL_host = nullptr;   // pinned copy of corr[nm]
     int count = 0, head = 0;
 

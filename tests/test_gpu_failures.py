@@ -7,6 +7,8 @@ a stiffness that is exactly zero, a NaN in a host input copy, a deliberately wro
 guess -- checks the status the library returns, and then checks that the same context still
 solves a good problem (the kernels returned normally).
 """
+import time
+
 import numpy as np
 import pytest
 
@@ -124,3 +126,27 @@ def test_poisoned_learned_guess_falls_back_to_tangent_predictor(lib):
         assert np.linalg.norm(U - Up) <= 1e-6 * np.linalg.norm(Up), k
         assert abs(L - Lp) <= 1e-6 * abs(Lp), k
     assert used == 0          # every placed start failed and the tangent predictor took over
+
+
+def test_solve_wait_budget_gives_non_finite_solution(lib, monkeypatch):
+    """Every wait of the dataflow triangular solve is bounded.  KLSA_SOLVE_STALL_NODE=k (read when
+    a problem's factorisation is set up) makes the k-th leaf's completion count unreachable: the
+    waits of its parent run out after about 0.1 s, the launch still ends, the solution comes
+    back non-finite (the library's error signal for an expired wait), and the context then
+    solves a good problem."""
+    import gsstructuralanalysis_gb300 as G
+    monkeypatch.setenv("KLSA_SOLVE_STALL_NODE", "0")
+    prob = P.cylindrical_panel(m=16, p=2)
+    gp = G.Problem(prob)
+    s = G.SparseSolver(gp, "SimplicialLDLT")
+    assert s.compute_jacobian(np.zeros(gp.ndof)) == 0
+    t0 = time.perf_counter()
+    y = s.solve(np.ones((2, gp.ndof)))
+    assert time.perf_counter() - t0 < 10.0
+    assert not np.isfinite(y).all()
+    monkeypatch.delenv("KLSA_SOLVE_STALL_NODE")
+    gp2 = G.Problem(prob)
+    s2 = G.SparseSolver(gp2, "SimplicialLDLT", {"Refinement": 8, "RefineTol": 1e-12})
+    assert s2.compute_jacobian(np.zeros(gp2.ndof)) == 0
+    assert np.isfinite(s2.solve(np.ones((2, gp2.ndof)))).all()
+    _context_still_solves(G)

@@ -84,6 +84,45 @@ def test_multifrontal_solve(lib, oracle_mod, name, make):
     assert np.linalg.norm(y2 - ref) / np.linalg.norm(ref) < 1e-9
 
 
+@pytest.mark.parametrize("m,p", [(32, 2), (20, 3)])
+def test_solve_schedules_agree(lib, oracle_mod, m, p, monkeypatch):
+    """The three schedules of the multifrontal triangular solve on one factorisation -- the
+    dataflow launch (default), the level-barrier launch (KLSA_SOLVE_KERNEL=barrier) and five
+    launches per level (KLSA_SOLVE_KERNEL=levels) -- with FP32 and FP64 fronts, two right-hand
+    sides, against SuperLU on the oracle's tangent.  The schedules add the same tile products in
+    different orders.  With FP32 fronts every result carries the FP32 factor's own error (1e-3 to
+    4e-2 relative on these thin shells): each schedule must stay within three times the error of
+    the five-launch solve.  With FP64 fronts a tile read before its inputs were complete would
+    show at O(1), against 1e-10 required."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=m, p=p)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    rng = np.random.default_rng(11)
+    x = 1e-3 * rng.standard_normal(gp.ndof)
+    Kr = oa.jacobian(x).tocsc()
+    b = rng.standard_normal((2, gp.ndof))
+    ref = np.stack([spla.spsolve(Kr, bi) for bi in b])
+
+    def rel(a, r):
+        return np.linalg.norm(a - r) / np.linalg.norm(r)
+
+    for prec in (32, 64):
+        s = G.SparseSolver(gp, "SimplicialLDLT", {"FrontPrecision": prec, "Refinement": 0})
+        assert s.compute_jacobian(x) == 0
+        ys = {}
+        for kern in ("dataflow", "barrier", "levels"):
+            if kern == "dataflow":
+                monkeypatch.delenv("KLSA_SOLVE_KERNEL", raising=False)
+            else:
+                monkeypatch.setenv("KLSA_SOLVE_KERNEL", kern)
+            ys[kern] = s.solve(b)
+        monkeypatch.delenv("KLSA_SOLVE_KERNEL", raising=False)
+        tol = 1e-10 if prec == 64 else 3.0 * rel(ys["levels"], ref)
+        assert prec == 64 or tol < 0.2
+        for kern, y in ys.items():
+            assert rel(y, ref) <= tol, (prec, kern, rel(y, ref), tol)
+
+
 def test_djacobian_matches(lib, oracle_mod):
     """dJacobian_t (gsStructuralAnalysisTypes.h:91-92), called with a solution update as
     gsALMBase::_computeJacobian does (gsALMBase.hpp:214-223): the oracle's tangent at x, for
