@@ -493,15 +493,17 @@ __device__ __forceinline__ bool fint_group_tiny(int grp, int nel, int m1, int n1
     const int lpe = NB > nq * nq ? NB : nq * nq;
     const int slot = lane / lpe, idx = lane % lpe;
     const int e = grp * (32 / lpe) + slot;
-    double m = 0.0;
+    // the largest |u| of the warp's elements, compared through the high words of the doubles
+    // (for non-negative doubles the bit patterns order as the values): integer pipes only
+    auto hiw = [](double v) { return static_cast<unsigned>(__double_as_longlong(v) >> 32) & 0x7fffffffu; };
+    unsigned m = 0;
     if (slot < 32 / lpe && e < nel && idx < NB) {
         const int e1 = e % m1, e2 = e / m1;
         const int A = (e2 + idx / NB1) * n1 + (e1 + idx % NB1);
-        m = fmax(fabs(ufull[A]), fmax(fabs(ufull[ncp + A]), fabs(ufull[2 * ncp + A])));
+        m = max(hiw(ufull[A]), max(hiw(ufull[ncp + A]), hiw(ufull[2 * ncp + A])));
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
-    return m > 0.0 && m < 1e-20;
+    m = __reduce_max_sync(0xffffffffu, m);
+    return m != 0u && m < 0x3BC79CA1u;   // 0 < max |u| < 1e-20 (high word of 1e-20)
 }
 
 // shared memory of one warp, for either variant of the element group
