@@ -643,7 +643,8 @@ __global__ void csr_gather_kernel(int nfree, int64_t nnz, int p, int n1, int m1,
 }
 
 __global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int ncp, const int* __restrict__ int2full,
-                                  const double* __restrict__ elemR, double* __restrict__ out) {
+                                  const double* __restrict__ elemR, double* __restrict__ out, double alpha = 0.0,
+                                  const double* __restrict__ y = nullptr) {
     int R = blockIdx.x * blockDim.x + threadIdx.x;
     if (R >= nfree) return;
     int fr = int2full[R];
@@ -656,13 +657,22 @@ __global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int 
             int la = (j - e2) * NB1 + (i - e1);
             s += elemR[(size_t)(e2 * m1 + e1) * D + 3 * la + ci];
         }
-    out[R] = s;
+    out[R] = y ? s + alpha * y[R] : s;
 }
 
 __global__ void scatter_free_kernel(int nfree, const int* __restrict__ int2full, const double* __restrict__ x,
                                     double* __restrict__ ufull) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < nfree) ufull[int2full[r]] = x[r];
+}
+
+__global__ void scatter_sum_kernel(int nfree, const int* __restrict__ int2full, const double* __restrict__ a,
+                                   const double* __restrict__ b, double* __restrict__ x, double* __restrict__ ufull) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nfree) return;
+    const double v = a[r] + b[r];
+    x[r] = v;
+    ufull[int2full[r]] = v;
 }
 
 __global__ void permute_kernel(int n, int nv, const int* __restrict__ map, const double* __restrict__ src,
@@ -780,6 +790,12 @@ void Problem::set_displacement(const double* d_x) {
     KL_CHECK_LAUNCH();
 }
 
+void Problem::set_displacement_sum(const double* a, const double* b, double* x) {
+    scatter_sum_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, d_int2full.get(), a, b, x, d_ufull.get());
+    count_launch();
+    KL_CHECK_LAUNCH();
+}
+
 void Problem::tangent_f32() {
     int D = 3 * (p + 1) * (p + 1);
     if (d_elemKf.size() < (size_t)nel * D * D) d_elemKf.alloc((size_t)nel * D * D);
@@ -818,7 +834,7 @@ void Problem::mass_f64() {
     KL_CHECK_LAUNCH();
 }
 
-void Problem::internal_force(double* d_out) {
+void Problem::internal_force(double* d_out, double alpha, const double* y) {
     int D = 3 * (p + 1) * (p + 1);
     if (d_elemR.size() < (size_t)nel * D) d_elemR.alloc((size_t)nel * D);
     int lpe = std::max((p + 1) * (p + 1), nq * nq);
@@ -838,7 +854,8 @@ void Problem::internal_force(double* d_out) {
         default: throw std::invalid_argument("unsupported degree");
     }
     count_launch();
-    vec_gather_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, p, n1, m1, m2, ncp, d_int2full.get(), d_elemR.get(), d_out);
+    vec_gather_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, p, n1, m1, m2, ncp, d_int2full.get(), d_elemR.get(), d_out,
+                                                                alpha, y);
     count_launch();
     KL_CHECK_LAUNCH();
 }

@@ -122,6 +122,50 @@ __global__ void block_apply_kernel(int nblk, const int* __restrict__ start, cons
         z[s0 + i] = v;
     }
 }
+// z = a x + b y; z2 = z when z2 is given; acc += z when acc is given
+__global__ void lincomb_ext_kernel(double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                                   double* __restrict__ z, double* __restrict__ z2, double* __restrict__ acc, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = a * x[i] + b * y[i];
+    z[i] = v;
+    if (z2) z2[i] = v;
+    if (acc) acc[i] += v;
+}
+// the end of an accepted step: uprev = u; u += d; dold = d when dold is given
+__global__ void step_finish_kernel(double* __restrict__ u, const double* __restrict__ d, double* __restrict__ uprev,
+                                   double* __restrict__ dold, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double ui = u[i], di = d[i];
+    uprev[i] = ui;
+    u[i] = ui + di;
+    if (dold) dold[i] = di;
+}
+__global__ void zero4_kernel(double* __restrict__ a, double* __restrict__ b, double* __restrict__ c,
+                             double* __restrict__ d, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (a) a[i] = 0.0;
+    if (b) b[i] = 0.0;
+    if (c) c[i] = 0.0;
+    if (d) d[i] = 0.0;
+}
+// the two right-hand sides [s0 b0, s1 b1] in FP32, and the two FP32 solutions back to FP64
+__global__ void to_f32_pair_kernel(const double* __restrict__ b0, double s0, const double* __restrict__ b1, double s1,
+                                   float* __restrict__ y, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    y[i] = (float)(s0 * b0[i]);
+    y[n + i] = (float)(s1 * b1[i]);
+}
+__global__ void to_f64_pair_kernel(const float* __restrict__ x, double* __restrict__ x0, double* __restrict__ x1,
+                                   int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x0[i] = (double)x[i];
+    x1[i] = (double)x[n + i];
+}
 __global__ void mul_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c, int64_t n) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) c[i] = a[i] * b[i];
@@ -145,6 +189,19 @@ void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream
 }
 void lincomb(double a, const double* x, double b, const double* y, double* z, int64_t n, cudaStream_t s) {
     lincomb_kernel<<<ceil_div(n, 256), 256, 0, s>>>(a, x, b, y, z, n);
+    count_launch();
+}
+void lincomb_ext(double a, const double* x, double b, const double* y, double* z, double* z2, double* acc, int64_t n,
+                 cudaStream_t s) {
+    lincomb_ext_kernel<<<ceil_div(n, 256), 256, 0, s>>>(a, x, b, y, z, z2, acc, n);
+    count_launch();
+}
+void step_finish(double* u, const double* d, double* uprev, double* dold, int64_t n, cudaStream_t s) {
+    step_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(u, d, uprev, dold, n);
+    count_launch();
+}
+void zero4(double* a, double* b, double* c, double* d, int64_t n, cudaStream_t s) {
+    zero4_kernel<<<ceil_div(n, 256), 256, 0, s>>>(a, b, c, d, n);
     count_launch();
 }
 
@@ -275,6 +332,22 @@ int MFSolver::solve(const double* d_b, double* d_x, int nrhs) {
         ++last_refine_its_;
     }
     return ST_SUCCESS;
+}
+
+bool MFSolver::solve_pair(const double* b0, double s0, const double* b1, double s1, double* x0, double* x1) {
+    // only the plain FP32-front solve: refinement and FP64 fronts take the generic path
+    if (fp64_ || (refine_ > 0 && has64_)) return false;
+    const int64_t n = P_.nfree;
+    cudaEvent_t ev = g_timer.begin(P_.stream);
+    to_f32_pair_kernel<<<ceil_div(n, 256), 256, 0, P_.stream>>>(b0, s0, b1, s1, b32_.get(), n);
+    count_launch();
+    P_.solver().solve(b32_.get(), x32_.get(), 2);
+    to_f64_pair_kernel<<<ceil_div(n, 256), 256, 0, P_.stream>>>(x32_.get(), x0, x1, n);
+    count_launch();
+    KL_CHECK_LAUNCH();
+    g_timer.end(P_.stream, 2, ev);
+    last_refine_its_ = 0;
+    return true;
 }
 
 void MFSolver::stability(double* min_d, int64_t* neg) {

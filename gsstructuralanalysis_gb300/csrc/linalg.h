@@ -19,6 +19,9 @@ public:
     virtual bool has_ldlt() const { return false; }
     virtual void stability(double* min_d, int64_t* neg) { *min_d = 0; *neg = 0; }
     virtual int last_iterations() const { return 0; }
+    // x0 = K^-1 (s0 b0), x1 = K^-1 (s1 b1) in one two-right-hand-side solve without staging
+    // copies; false when this solver has no such path (the caller stages the pair itself)
+    virtual bool solve_pair(const double*, double, const double*, double, double*, double*) { return false; }
     // identifies the factorisation the solver currently holds (0: none / not a factorisation)
     virtual uint64_t generation() const { return 0; }
 };
@@ -32,6 +35,7 @@ public:
     int compute_tangent() override;
     int factor_current(bool f64_for_refine);
     int solve(const double* d_b, double* d_x, int nrhs) override;
+    bool solve_pair(const double* b0, double s0, const double* b1, double s1, double* x0, double* x1) override;
     bool has_ldlt() const override { return true; }
     void stability(double* min_d, int64_t* neg) override;
     int last_iterations() const override { return last_refine_its_; }

@@ -1021,6 +1021,32 @@ __device__ __forceinline__ bool mf_wait_count(const int* p, int target, long lon
     }
 }
 
+// K partial sums per lane (K = 8, 16 or 32) reduced across the warp at once: at each exchange
+// step a lane keeps one half of its values and receives the partner's sums of that half, so the
+// K sums need K - 1 + log2(32 / K) shuffles instead of 5 K.  Afterwards lane l holds the warp
+// total of value l >> log2(32 / K).
+template <int K, class T>
+__device__ __forceinline__ T mf_transpose_reduce(T (&v)[K], int lane) {
+    static_assert(K == 8 || K == 16 || K == 32, "K must be 8, 16 or 32");
+#pragma unroll
+    for (int h = K / 2, o = 16; h >= 1; h >>= 1, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const T send = up ? v[i] : v[i + h];
+            const T keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    T r = v[0];
+#pragma unroll
+    for (int o = 16 / K; o >= 1; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    return r;
+}
+
+__device__ __forceinline__ float mf_rcp(float d) { return __frcp_rn(d); }
+__device__ __forceinline__ double mf_rcp(double d) { return __drcp_rn(d); }
+
 __device__ __forceinline__ void mf_poison(float* p) { atomicExch(p, __int_as_float(0x7fffffff)); }
 __device__ __forceinline__ void mf_poison(double* p) {
     atomicExch(reinterpret_cast<unsigned long long*>(p), 0x7fffffffffffffffULL);
@@ -1123,27 +1149,29 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_solve_dataflow_kernel(SolveA
                 if (r0 + e < hN) v = __ldcg(a.x + hrow + (int64_t)n * qq);
             } else {
                 const int i = r0 + e;
-                if (i < kN) v = __ldcg(a.z + o + i + (int64_t)n * qq) / a.D[o + i] + __ldcg(a.w + o + i + (int64_t)n * qq);
+                if (i < kN) v = __ldcg(a.z + o + i + (int64_t)n * qq) * mf_rcp(a.D[o + i]) + __ldcg(a.w + o + i + (int64_t)n * qq);
             }
             vs[qq][e] = v;
         }
         __syncthreads();
         if (phase == 0 || phase == 2) {
-            // lanes over the tile's columns: one warp sum per row (A) or column (C) and right-hand side
+            // lanes over the tile's columns: a warp sum per row (A) or column (C) of the warp's
+            // eight and right-hand side, all reduced together
+            constexpr int K = 8 * NR, SH = NR == 1 ? 2 : NR == 2 ? 1 : 0;
+            T pv[K];
 #pragma unroll
-            for (int s = 0; s < 8; ++s) {
+            for (int s = 0; s < 8; ++s)
 #pragma unroll
-                for (int qq = 0; qq < NR; ++qq) {
-                    const T v = mf_warp_sum(m[s][0] * vs[qq][lane] + m[s][1] * vs[qq][lane + 32]);
-                    if (lane == 0) {
-                        if (phase == 0) {
-                            const int i = r0 + warp + 8 * s;
-                            if (i < kN) atomicAdd(a.z + o + i + (int64_t)n * qq, v);
-                        } else {
-                            const int j = c0 + warp + 8 * s;
-                            if (j < kN) atomicAdd(a.w + o + j + (int64_t)n * qq, -v);
-                        }
-                    }
+                for (int qq = 0; qq < NR; ++qq) pv[s * NR + qq] = m[s][0] * vs[qq][lane] + m[s][1] * vs[qq][lane + 32];
+            const T v = mf_transpose_reduce<K>(pv, lane);
+            if ((lane & ((1 << SH) - 1)) == 0) {
+                const int idx = lane >> SH, s = idx / NR, qq = idx % NR;
+                if (phase == 0) {
+                    const int i = r0 + warp + 8 * s;
+                    if (i < kN) atomicAdd(a.z + o + i + (int64_t)n * qq, v);
+                } else {
+                    const int j = c0 + warp + 8 * s;
+                    if (j < kN) atomicAdd(a.w + o + j + (int64_t)n * qq, -v);
                 }
             }
         } else {
@@ -1172,7 +1200,9 @@ __global__ void __launch_bounds__(SOLVE_THREADS) mf_solve_dataflow_kernel(SolveA
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
+            // release: the CTA's atomics (ordered before this thread by the barrier) become visible
+            // at GPU scope before the count does
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
             atomicAdd((phase == 0 ? cntA : phase == 1 ? cntB : phase == 2 ? cntC : cntD) + nd, 1);
         }
     }

@@ -19,16 +19,22 @@ namespace {
 
 constexpr int PCH = LearnedPredictor::PCH;
 
-// qslot[c * nm + j] = sum over chunk c of Phi_j . u (fixed order within the chunk)
+// qslot[c * nm + j] = sum over chunk c of Phi_j . u (fixed order within the chunk); the blocks
+// of mode 0 also copy u into the history ring (copy)
 __global__ void __launch_bounds__(256) project_kernel(int n, int nm, const double* __restrict__ Phi,
-                                                      const double* __restrict__ u, double* __restrict__ qslot) {
+                                                      const double* __restrict__ u, double* __restrict__ qslot,
+                                                      double* __restrict__ copy) {
     __shared__ double red[8];
     const int j = blockIdx.y, c = blockIdx.x;
     const int len = (n + PCH - 1) / PCH, lo = c * len, hi = min(n, lo + len);
     const double* ph = Phi + (size_t)j * n;
     double s = 0.0;
 #pragma unroll 4
-    for (int i = lo + threadIdx.x; i < hi; i += 256) s += ph[i] * u[i];
+    for (int i = lo + threadIdx.x; i < hi; i += 256) {
+        const double ui = u[i];
+        s += ph[i] * ui;
+        if (j == 0) copy[i] = ui;
+    }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -183,11 +189,12 @@ LearnedPredictor::~LearnedPredictor() {
 void LearnedPredictor::push(const double* dU, double L) {
     const int n = P.nfree;
     double* h = hist.get() + (size_t)head * n;
-    KL_CUDA(cudaMemcpyAsync(h, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, P.stream));
     if (nm > 0) {
-        project_kernel<<<dim3(PCH, nm), 256, 0, P.stream>>>(n, nm, Phi.get(), h, qpart.get() + (size_t)head * PCH * nm);
+        project_kernel<<<dim3(PCH, nm), 256, 0, P.stream>>>(n, nm, Phi.get(), dU, qpart.get() + (size_t)head * PCH * nm, h);
         count_launch();
         KL_CHECK_LAUNCH();
+    } else {
+        KL_CUDA(cudaMemcpyAsync(h, dU, sizeof(double) * n, cudaMemcpyDeviceToDevice, P.stream));
     }
     histL[head] = L;
     head = (head + 1) & 3;

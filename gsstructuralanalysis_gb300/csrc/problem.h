@@ -69,9 +69,11 @@ struct Problem {
 
     // --- device operations (internal order, device pointers) ---------------------------
     void set_displacement(const double* d_x);           // u_full <- x (free dofs)
+    void set_displacement_sum(const double* a, const double* b, double* x);   // x = a + b; u_full <- x
     void tangent_f32();                                 // d_vals32 = K(u) (FP32 element integration)
     void tangent_f64();                                 // d_vals64 = K(u) (FP64)
-    void internal_force(double* d_out);                 // Fint(u), internal order, FP64
+    // Fint(u) + alpha y (y may be null), internal order, FP64
+    void internal_force(double* d_out, double alpha = 0.0, const double* y = nullptr);
     void internal_force_elements(double* elemR);        // element forces of u into elemR (nel*d), no allocation
     void mass_f64();                                    // d_vals64 = M
     Multifrontal& solver();                             // lazily built (FP32 fronts)
@@ -94,6 +96,11 @@ void to_f32(const double* x, float* y, int64_t n, cudaStream_t s);
 void to_f64(const float* x, double* y, int64_t n, cudaStream_t s);
 void axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t s);   // y = a x + b y
 void lincomb(double a, const double* x, double b, const double* y, double* z, int64_t n, cudaStream_t s);  // z = a x + b y
+// z = a x + b y, and also z2 = z (z2 given) and acc += z (acc given)
+void lincomb_ext(double a, const double* x, double b, const double* y, double* z, double* z2, double* acc, int64_t n,
+                 cudaStream_t s);
+void step_finish(double* u, const double* d, double* uprev, double* dold, int64_t n, cudaStream_t s);  // uprev = u; u += d; dold = d
+void zero4(double* a, double* b, double* c, double* d, int64_t n, cudaStream_t s);   // null pointers skipped
 // dots[i] = <x_i, y_i> for up to 8 pairs, FP64, result copied to host (synchronises)
 void multidot(int npairs, const double* const* xs, const double* const* ys, int64_t n, double* host_out,
               cudaStream_t s);

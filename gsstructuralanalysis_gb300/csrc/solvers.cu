@@ -273,8 +273,7 @@ void ALMGPU::set_initial_guess(const double* d_U, double L) {
 }
 
 void ALMGPU::compute_jacobian() {
-    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, P_.stream);
-    P_.set_displacement(x_.get());
+    P_.set_displacement_sum(U_.get(), DU_.get(), x_.get());
     ++n_jac;
     if (S_->compute_tangent() != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
     KL_CUDA(cudaMemcpyAsync(xjac_.get(), x_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
@@ -285,10 +284,8 @@ void ALMGPU::compute_jacobian() {
 
 void ALMGPU::compute_residual() {
     cudaEvent_t ev = g_timer.begin(P_.stream);
-    vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, P_.stream);
-    P_.set_displacement(x_.get());
-    P_.internal_force(fint_.get());
-    vec::lincomb(1.0, fint_.get(), -(L_ + DL_), P_.d_F.get(), R_.get(), n_, P_.stream);
+    P_.set_displacement_sum(U_.get(), DU_.get(), x_.get());
+    P_.internal_force(R_.get(), -(L_ + DL_), P_.d_F.get());   // ALResidual: Fint - (L + DL) F
     g_timer.end(P_.stream, 3, ev);
     ++n_res;
 }
@@ -312,7 +309,10 @@ void ALMGPU::compute_residual_norms() {
 // one factorisation, two right-hand sides: [F, -R] -> [dUt, dUbar]
 void ALMGPU::solve_ut_ubar(bool need_ut) {
     cudaStream_t s = P_.stream;
-    if (need_ut) {
+    if (need_ut && S_->solve_pair(P_.d_F.get(), 1.0, R_.get(), -1.0, dUt_.get(), dUbar_.get())) {
+        n_solve += 2;
+        ut_valid_ = true;
+    } else if (need_ut) {
         KL_CUDA(cudaMemcpyAsync(rhs2_.get(), P_.d_F.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
         vec::lincomb(-1.0, R_.get(), 0.0, R_.get(), rhs2_.get() + n_, n_, s);
         if (S_->solve(rhs2_.get(), sol2_.get(), 2) != ST_SUCCESS) throw Fail{ST_SOLVER_ERROR};
@@ -328,13 +328,9 @@ void ALMGPU::solve_ut_ubar(bool need_ut) {
 }
 
 void ALMGPU::initiate_step() {
-    DU_.zero(P_.stream);
-    dU_.zero(P_.stream);
-    if (method_ == Crisfield) {
-        dUbar_.zero(P_.stream);
-        dUt_.zero(P_.stream);
-        eta_ = 1.0;
-    }
+    const bool cr = method_ == Crisfield;
+    vec::zero4(DU_.get(), dU_.get(), cr ? dUbar_.get() : nullptr, cr ? dUt_.get() : nullptr, n_, P_.stream);
+    if (cr) eta_ = 1.0;
     DL_ = dL_ = 0.0;
 }
 
@@ -418,8 +414,7 @@ void ALMGPU::predictor_guess() {
     cudaStream_t s = P_.stream;
     if (guess_place_) {
         // start the corrector at the guess: no tangent at U, no u_t solve
-        vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), DU_.get(), n_, s);
-        KL_CUDA(cudaMemcpyAsync(dU_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+        vec::lincomb_ext(1.0, Uguess_.get(), -1.0, U_.get(), DU_.get(), dU_.get(), nullptr, n_, s);
         DL_ = dL_ = Lguess_ - L_;
         ut_valid_ = false;
         has_guess_ = false;
@@ -534,11 +529,13 @@ void ALMGPU::lambdas_crisfield() {
     double DOTfac = d[6] + phi_ * phi_ * DLold_;
     double al1 = a0, al2 = b0 + eta_ * b1, al3 = c0 + eta_ * c1 + eta_ * eta_ * c2;
     double disc = al2 * al2 - 4 * al1 * al3;
+    // the root's update dU = eta dUbar + dL dUt is formed by the caller (with DU += dU in the
+    // same pass); only the complex-root branch below forms dU itself (dU_formed_)
+    dU_formed_ = false;
     auto choose = [&](double r0, double r1) {
         double d0 = r0 * DOTfac, d1 = r1 * DOTfac;
         double r = (d0 < d1) ? r1 : r0;
         dL_ = r;
-        vec::lincomb(eta_, dUbar_.get(), r, dUt_.get(), dU_.get(), n_, s);
     };
     if (disc >= 0) {
         eta_ = 1.0;
@@ -581,6 +578,7 @@ void ALMGPU::lambdas_crisfield() {
     dL_ = mu * DLcr - DL_;
     // dU = mu (DU + dUbar) - DU
     vec::lincomb(mu - 1.0, DU_.get(), mu, dUbar_.get(), dU_.get(), n_, s);
+    dU_formed_ = true;
 }
 
 void ALMGPU::iteration() {
@@ -599,10 +597,13 @@ void ALMGPU::iteration() {
         double lamold = dL_;
         lambdas_crisfield();
         if ((lamold * dL_ < 0 && std::fabs(dL_) <= std::fabs(lamold)) && relax_ != 1.0) {
-            vec::lincomb(relax_ * dL_, dUt_.get(), relax_ * eta_, dUbar_.get(), dU_.get(), n_, s);
+            vec::lincomb_ext(relax_ * dL_, dUt_.get(), relax_ * eta_, dUbar_.get(), dU_.get(), nullptr, DU_.get(), n_, s);
             dL_ = relax_ * dL_;
+        } else if (!dU_formed_) {
+            vec::lincomb_ext(eta_, dUbar_.get(), dL_, dUt_.get(), dU_.get(), nullptr, DU_.get(), n_, s);
+        } else {
+            vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
         }
-        vec::axpby(1.0, dU_.get(), 1.0, DU_.get(), n_, s);
         DL_ += dL_;
         if (angle_ == 1) {
             KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
@@ -643,14 +644,11 @@ void ALMGPU::iteration() {
 void ALMGPU::iteration_finish() {
     cudaStream_t s = P_.stream;
     converged_ = true;
-    KL_CUDA(cudaMemcpyAsync(Uprev_.get(), U_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
+    const bool keep_old = (method_ == Crisfield && angle_ == 0) || method_ == ConsistentCrisfield;
+    vec::step_finish(U_.get(), DU_.get(), Uprev_.get(), keep_old ? DUold_.get() : nullptr, n_, s);   // Uprev = U; U += DU
     Lprev_ = L_;
-    vec::axpby(1.0, DU_.get(), 1.0, U_.get(), n_, s);
     L_ += DL_;
-    if ((method_ == Crisfield && angle_ == 0) || method_ == ConsistentCrisfield) {
-        KL_CUDA(cudaMemcpyAsync(DUold_.get(), DU_.get(), sizeof(double) * n_, cudaMemcpyDeviceToDevice, s));
-        DLold_ = DL_;
-    }
+    if (keep_old) DLold_ = DL_;
 }
 
 void ALMGPU::step_impl() {

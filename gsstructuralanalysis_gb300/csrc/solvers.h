@@ -144,6 +144,7 @@ private:
     void solve_ut_ubar(bool need_ut);
     void compute_lambda_mu();
     void lambdas_crisfield();
+    bool dU_formed_ = false;   // lambdas_crisfield formed dU itself (complex-root branch)
     void consistent_predictor(const double* prevU, double prevL);
     void stability_impl(bool jacobian, double shift);
     bool test_singular_point(bool jacobian);
