@@ -644,7 +644,7 @@ __global__ void csr_gather_kernel(int nfree, int64_t nnz, int p, int n1, int m1,
 
 __global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int ncp, const int* __restrict__ int2full,
                                   const double* __restrict__ elemR, double* __restrict__ out, double alpha = 0.0,
-                                  const double* __restrict__ y = nullptr) {
+                                  const double* __restrict__ y = nullptr, const double* __restrict__ alpha_sub = nullptr) {
     int R = blockIdx.x * blockDim.x + threadIdx.x;
     if (R >= nfree) return;
     int fr = int2full[R];
@@ -657,7 +657,11 @@ __global__ void vec_gather_kernel(int nfree, int p, int n1, int m1, int m2, int 
             int la = (j - e2) * NB1 + (i - e1);
             s += elemR[(size_t)(e2 * m1 + e1) * D + 3 * la + ci];
         }
-    out[R] = y ? s + alpha * y[R] : s;
+    if (y) {
+        const double a = alpha_sub ? alpha - *alpha_sub : alpha;
+        s += a * y[R];
+    }
+    out[R] = s;
 }
 
 __global__ void scatter_free_kernel(int nfree, const int* __restrict__ int2full, const double* __restrict__ x,
@@ -834,7 +838,7 @@ void Problem::mass_f64() {
     KL_CHECK_LAUNCH();
 }
 
-void Problem::internal_force(double* d_out, double alpha, const double* y) {
+void Problem::internal_force(double* d_out, double alpha, const double* y, const double* alpha_sub) {
     int D = 3 * (p + 1) * (p + 1);
     if (d_elemR.size() < (size_t)nel * D) d_elemR.alloc((size_t)nel * D);
     int lpe = std::max((p + 1) * (p + 1), nq * nq);
@@ -855,7 +859,7 @@ void Problem::internal_force(double* d_out, double alpha, const double* y) {
     }
     count_launch();
     vec_gather_kernel<<<ceil_div(nfree, 256), 256, 0, stream>>>(nfree, p, n1, m1, m2, ncp, d_int2full.get(), d_elemR.get(), d_out,
-                                                                alpha, y);
+                                                                alpha, y, alpha_sub);
     count_launch();
     KL_CHECK_LAUNCH();
 }

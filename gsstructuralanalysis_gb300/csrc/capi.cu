@@ -739,8 +739,9 @@ int klsa_alm_step_learned(klsa_alm* a, klsa_predictor* pr, int guess_max_iter, i
         if (used_guess) *used_guess = 0;
         if (L.count == 0) L.push(A.U(), A.L());
         double Lg = 0.0;
-        if (L.guess(pr->ug.get(), &Lg)) {
-            A.set_initial_guess(pr->ug.get(), Lg);
+        const double* Lcorr = nullptr;
+        if (L.guess_deferred(pr->ug.get(), &Lg, &Lcorr)) {
+            A.set_initial_guess_dev(pr->ug.get(), Lg, Lcorr);
             A.set_guess_place(true);
             int saved = A.max_iter();
             A.set_max_iter(guess_max_iter > 1 ? guess_max_iter : saved);

@@ -40,6 +40,17 @@ struct CudaError : std::runtime_error {
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// RAII page-locked host buffer
+template <class T>
+struct PinnedBuf {
+    T* ptr = nullptr;
+    explicit PinnedBuf(size_t count = 1) { KL_CUDA(cudaMallocHost(&ptr, count * sizeof(T))); }
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { if (ptr) cudaFreeHost(ptr); }
+    T* get() const { return ptr; }
+};
+
 // RAII device buffer
 template <class T>
 struct DevBuf {

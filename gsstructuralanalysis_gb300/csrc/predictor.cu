@@ -202,6 +202,23 @@ void LearnedPredictor::push(const double* dU, double L) {
 }
 
 bool LearnedPredictor::guess(double* dUg, double* Lg) {
+    if (!launch_guess(dUg, Lg)) return false;
+    if (net) {
+        KL_CUDA(cudaMemcpyAsync(corrL_host, corr.get() + nm, sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+        KL_CUDA(cudaStreamSynchronize(P.stream));
+        *Lg += *corrL_host;
+    }
+    return true;
+}
+
+bool LearnedPredictor::guess_deferred(double* dUg, double* Lg, const double** Lcorr) {
+    if (!launch_guess(dUg, Lg)) return false;
+    *Lcorr = net ? corr.get() + nm : nullptr;
+    return true;
+}
+
+// the network (if any) and the guess kernel; *Lcubic = the cubic extrapolation of the load factor
+bool LearnedPredictor::launch_guess(double* dUg, double* Lcubic) {
     if (count < 4) return false;
     const int n = P.nfree;
     const int s[4] = {slot(0), slot(1), slot(2), slot(3)};
@@ -244,13 +261,7 @@ bool LearnedPredictor::guess(double* dUg, double* Lg) {
         corr.get(), dUg);
     count_launch();
     KL_CHECK_LAUNCH();
-    double cL = 0.0;
-    if (net) {
-        KL_CUDA(cudaMemcpyAsync(corrL_host, corr.get() + nm, sizeof(double), cudaMemcpyDeviceToHost, P.stream));
-        KL_CUDA(cudaStreamSynchronize(P.stream));
-        cL = *corrL_host;
-    }
-    *Lg = 4.0 * Ls[0] - 6.0 * Ls[1] + 4.0 * Ls[2] - Ls[3] + cL;
+    *Lcubic = 4.0 * Ls[0] - 6.0 * Ls[1] + 4.0 * Ls[2] - Ls[3];
     return true;
 }
 

@@ -36,8 +36,12 @@ struct LearnedPredictor {
     // guess for the next point (needs 4 points); writes the device vector Ug (internal order).
     // With a network: one read of the load-factor correction (one stream synchronisation).
     bool guess(double* dUg, double* Lg);
+    // the same guess without waiting for the network: Lg without the network's load correction,
+    // which stays on the device at *Lcorr (null without a network)
+    bool guess_deferred(double* dUg, double* Lg, const double** Lcorr);
 
 private:
+    bool launch_guess(double* dUg, double* Lcubic);
     int slot(int back) const { return (head - 1 - back + 8) & 3; }   // back = 0: newest
 };
 

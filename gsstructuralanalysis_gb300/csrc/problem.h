@@ -72,8 +72,8 @@ struct Problem {
     void set_displacement_sum(const double* a, const double* b, double* x);   // x = a + b; u_full <- x
     void tangent_f32();                                 // d_vals32 = K(u) (FP32 element integration)
     void tangent_f64();                                 // d_vals64 = K(u) (FP64)
-    // Fint(u) + alpha y (y may be null), internal order, FP64
-    void internal_force(double* d_out, double alpha = 0.0, const double* y = nullptr);
+    // Fint(u) + (alpha - *alpha_sub) y (y and alpha_sub may be null), internal order, FP64
+    void internal_force(double* d_out, double alpha = 0.0, const double* y = nullptr, const double* alpha_sub = nullptr);
     void internal_force_elements(double* elemR);        // element forces of u into elemR (nel*d), no allocation
     void mass_f64();                                    // d_vals64 = M
     Multifrontal& solver();                             // lazily built (FP32 fronts)

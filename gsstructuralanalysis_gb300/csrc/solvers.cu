@@ -269,7 +269,21 @@ double ALMGPU::distance(const double* d_DU, double DL) {
 void ALMGPU::set_initial_guess(const double* d_U, double L) {
     KL_CUDA(cudaMemcpyAsync(Uguess_.get(), d_U, sizeof(double) * n_, cudaMemcpyDeviceToDevice, P_.stream));
     Lguess_ = L;
+    Lguess_dev_ = nullptr;
     has_guess_ = true;
+}
+
+void ALMGPU::set_initial_guess_dev(const double* d_U, double L, const double* d_Lcorr) {
+    set_initial_guess(d_U, L);
+    Lguess_dev_ = d_Lcorr;
+}
+
+void ALMGPU::resolve_guess_load() {
+    if (!Lguess_dev_) return;
+    KL_CUDA(cudaMemcpyAsync(Lguess_host_.get(), Lguess_dev_, sizeof(double), cudaMemcpyDeviceToHost, P_.stream));
+    KL_CUDA(cudaStreamSynchronize(P_.stream));
+    Lguess_ += *Lguess_host_.get();
+    Lguess_dev_ = nullptr;
 }
 
 void ALMGPU::compute_jacobian() {
@@ -285,7 +299,8 @@ void ALMGPU::compute_jacobian() {
 void ALMGPU::compute_residual() {
     cudaEvent_t ev = g_timer.begin(P_.stream);
     P_.set_displacement_sum(U_.get(), DU_.get(), x_.get());
-    P_.internal_force(R_.get(), -(L_ + DL_), P_.d_F.get());   // ALResidual: Fint - (L + DL) F
+    // ALResidual: Fint - (L + DL) F; a placed guess may still carry its load correction on the device
+    P_.internal_force(R_.get(), -(L_ + DL_), P_.d_F.get(), Lpending_);
     g_timer.end(P_.stream, 3, ev);
     ++n_res;
 }
@@ -293,7 +308,16 @@ void ALMGPU::compute_residual() {
 void ALMGPU::compute_residual_norms() {
     double d[3];
     const double* xs[3] = {R_.get(), dU_.get(), DU_.get()};
+    if (Lpending_)   // read with the norms (the reduction synchronises the stream)
+        KL_CUDA(cudaMemcpyAsync(Lguess_host_.get(), Lpending_, sizeof(double), cudaMemcpyDeviceToHost, P_.stream));
     vec::multidot(3, xs, xs, n_, d, P_.stream);
+    if (Lpending_) {
+        const double c = *Lguess_host_.get();
+        Lguess_ += c;
+        DL_ += c;
+        dL_ += c;
+        Lpending_ = nullptr;
+    }
     double nR = std::sqrt(d[0]), ndU = std::sqrt(d[1]), nDU = std::sqrt(d[2]);
     if (num_it_ == 0) {
         basisF_ = std::fabs(L_ + DL_) * std::sqrt(FF_);
@@ -659,9 +683,13 @@ void ALMGPU::step_impl() {
     // guess starts the corrector at DU = Uguess - U, whose norm comes back with the residual norms:
     // the test is made there, and the step restarts from the tangent predictor if it fails.
     bool use_guess = false, check_placed = false;
-    if (has_guess_ && (Lguess_ - L_) != 0) {
+    Lpending_ = nullptr;
+    if (has_guess_ && !guess_place_) resolve_guess_load();
+    if (has_guess_ && (Lguess_dev_ || (Lguess_ - L_) != 0)) {
         if (guess_place_) {
             use_guess = check_placed = true;
+            Lpending_ = Lguess_dev_;   // DL below lacks this correction until the first residual norms
+            Lguess_dev_ = nullptr;
         } else {
             double d;
             vec::lincomb(1.0, Uguess_.get(), -1.0, U_.get(), tmp_.get(), n_, P_.stream);
@@ -677,7 +705,7 @@ void ALMGPU::step_impl() {
     else predictor();
     compute_residual();
     compute_residual_norms();
-    if (check_placed && basisU_ == 0) {   // Uguess == U
+    if (check_placed && (basisU_ == 0 || DL_ == 0)) {   // Uguess == U or Lguess == L
         frozen = false;
         initiate_step();
         predictor();

@@ -94,6 +94,10 @@ public:
     void set_solution(const double* d_U, double L);
     void set_solution_step(const double* d_DU, double DL);
     void set_initial_guess(const double* d_U, double L);
+    // a guess whose load factor is L + *d_Lcorr, with the correction d_Lcorr still on the device:
+    // a placed guess (set_guess_place) reads it with the first residual norms, other uses read
+    // it at the start of the step
+    void set_initial_guess_dev(const double* d_U, double L, const double* d_Lcorr);
     // gsALMBase::setPrevious (gsALMBase.h:185-191): Uprev, Lprev and DUold = U - Uprev, DLold = L - Lprev
     void set_previous(const double* d_Uprev, double Lprev);
     // distance of a path increment in the method's norm: gsALMCrisfield.h:79-83
@@ -162,6 +166,10 @@ private:
     DevBuf<double> xjac_;          // point of the last Jacobian (m_jacMat's argument)
     double L_ = 0, DL_ = 0, dL_ = 0, DLold_ = 0, Lprev_ = 0, Lguess_ = 0;
     bool has_guess_ = false;
+    const double* Lguess_dev_ = nullptr;   // pending device correction of Lguess_
+    const double* Lpending_ = nullptr;     // the correction the current residual still carries
+    PinnedBuf<double> Lguess_host_;
+    void resolve_guess_load();             // Lguess_ += *Lguess_dev_ (synchronises)
     double FF_ = 0;
     // options
     int maxIt_ = 100;
