@@ -246,173 +246,6 @@ __global__ void __launch_bounds__(DIAG_THREADS) mf_diag_kernel(const int4* __res
     if (tid == 0 && bad) atomicExch(status, 1);
 }
 
-// Blocked variant of the diagonal tile (FP32 fronts), 256 threads.  The same LDL^T without
-// pivoting and the same outputs, with the 64 pivots in four panels of 16:
-//   1. warp 0 factorises the panel in registers: lane l owns rows ps + l and ps + 32 + l of the
-//      panel's 16 columns; the pivot and the entries A(c, j) of the panel's diagonal block come
-//      from lanes 0..15 by shuffles, so a pivot costs no block-wide barrier;
-//   2. all threads apply the rank-16 update A22 -= L21 D L21^T to the trailing lower triangle,
-//      one 4 x 4 block per thread;
-// then X = L^-1 by blocks: the 16 x 16 diagonal blocks by forward substitution (one warp each,
-// one column per lane), and block row i of the rest as X_ij = -X_ii sum_k L_ik X_kj.
-constexpr int DIAG_B_THREADS = 256;
-constexpr int DPAD = NB + 1;
-
-template <class T>
-__global__ void __launch_bounds__(DIAG_B_THREADS) mf_diag_blocked_kernel(const int4* __restrict__ items, int t,
-                                                                         const int* __restrict__ f, const int* __restrict__ k,
-                                                                         const int* __restrict__ own,
-                                                                         const int64_t* __restrict__ front_off,
-                                                                         const int64_t* __restrict__ linv_off, T* pool,
-                                                                         T* Dvec, T* linv, int* status) {
-    __shared__ T sA[NB][DPAD];
-    __shared__ T sX[NB][DPAD];
-    __shared__ T sT[16][3 * 16 + 1];
-    __shared__ int bad;
-    const int nd = items[blockIdx.x].x;
-    const int fN = f[nd], kN = k[nd];
-    const int c0 = t * NB;
-    const int kk = min(NB, kN - c0);
-    T* F = pool + front_off[nd];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) bad = 0;
-    // the tile's lower triangle (identity padding beyond kk); the front is column-major
-    for (int e = tid; e < NB * NB; e += DIAG_B_THREADS) {
-        const int r = e % NB, c = e / NB;
-        T v = T(0);
-        if (c <= r) v = r < kk ? F[(int64_t)(c0 + c) * fN + c0 + r] : (r == c ? T(1) : T(0));
-        sA[r][c] = v;
-        sX[r][c] = T(0);
-    }
-    __syncthreads();
-    const int npan = (kk + 15) / 16;
-    for (int pnl = 0; pnl < npan; ++pnl) {
-        const int ps = 16 * pnl, pe = ps + 16;
-        if (warp == 0) {
-            const int ra = ps + lane, rb = ps + 32 + lane;
-            T va[16], vb[16];
-#pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                va[c] = ra < NB ? sA[ra][ps + c] : T(0);
-                vb[c] = rb < NB ? sA[rb][ps + c] : T(0);
-            }
-            bool badl = false;
-#pragma unroll
-            for (int jj = 0; jj < 16; ++jj) {
-                const int j = ps + jj;
-                T d = __shfl_sync(0xffffffffu, va[jj], jj);
-                if (!(fabs(d) > T(0)) || !isfinite(d)) {
-                    if (j < kk) badl = true;
-                    d = T(1);
-                }
-                const T inv = pivot_recip(d);
-                T acj[16];
-#pragma unroll
-                for (int cc = jj + 1; cc < 16; ++cc) acj[cc] = __shfl_sync(0xffffffffu, va[jj], cc);
-                const T la = va[jj] * inv, lb = vb[jj] * inv;
-#pragma unroll
-                for (int cc = jj + 1; cc < 16; ++cc) {
-                    if (lane >= cc) va[cc] -= la * acj[cc];   // row ps + lane, column ps + cc <= row
-                    vb[cc] -= lb * acj[cc];
-                }
-                if (lane > jj) va[jj] = la;
-                else if (lane == jj) va[jj] = d;
-                vb[jj] = lb;
-            }
-            if (badl) bad = 1;
-#pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                if (ra < NB && ps + c <= ra) sA[ra][ps + c] = va[c];
-                if (rb < NB) sA[rb][ps + c] = vb[c];
-            }
-        }
-        __syncthreads();
-        // trailing update of rows and columns [pe, 64), lower triangle, 4 x 4 blocks
-        const int m = NB - pe;
-        if (pnl + 1 < npan && m > 0) {
-            const int nb4 = m / 4, nblk = nb4 * (nb4 + 1) / 2;
-            for (int b = tid; b < nblk; b += DIAG_B_THREADS) {
-                int bi = 0;
-                while ((bi + 1) * (bi + 2) / 2 <= b) ++bi;
-                const int bj = b - bi * (bi + 1) / 2;
-                const int r0 = pe + 4 * bi, q0 = pe + 4 * bj;
-                T acc[4][4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
-#pragma unroll 4
-                for (int jj = 0; jj < 16; ++jj) {
-                    const int j = ps + jj;
-                    const T dj = sA[j][j];
-                    T lr[4], lc[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        lr[u] = sA[r0 + u][j] * dj;
-                        lc[u] = sA[q0 + u][j];
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-#pragma unroll
-                        for (int v = 0; v < 4; ++v) acc[u][v] += lr[u] * lc[v];
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-#pragma unroll
-                    for (int v = 0; v < 4; ++v)
-                        if (q0 + v <= r0 + u) sA[r0 + u][q0 + v] -= acc[u][v];
-            }
-        }
-        __syncthreads();
-    }
-    // X = L^-1: diagonal 16 x 16 blocks, one warp each, lane c computes column c
-    if (warp < 4 && lane < 16) {
-        const int bs = 16 * warp, c = lane;
-        T x[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            T s = T(0);
-#pragma unroll
-            for (int j = 0; j < r; ++j) s += sA[bs + r][bs + j] * x[j];
-            x[r] = (r == c) ? T(1) : (r < c ? T(0) : -s);
-        }
-#pragma unroll
-        for (int r = 0; r < 16; ++r) sX[bs + r][bs + c] = x[r];
-    }
-    __syncthreads();
-    // block rows 1..3: T_ij = sum_{k=j}^{i-1} L_ik X_kj (j < i), then X_ij = -X_ii T_ij
-    for (int bi = 1; bi < 4; ++bi) {
-        const int rs = 16 * bi;
-        for (int e = tid; e < 16 * 16 * bi; e += DIAG_B_THREADS) {
-            const int rl = e / (16 * bi), col = e % (16 * bi);   // column col of [X_0 .. X_{bi-1}] blocks
-            T s = T(0);
-            for (int kc = (col / 16) * 16; kc < rs; ++kc) s += sA[rs + rl][kc] * sX[kc][col];
-            sT[rl][col] = s;
-        }
-        __syncthreads();
-        for (int e = tid; e < 16 * 16 * bi; e += DIAG_B_THREADS) {
-            const int rl = e / (16 * bi), col = e % (16 * bi);
-            T s = T(0);
-            for (int j = 0; j <= rl; ++j) s += sX[rs + rl][rs + j] * sT[j][col];
-            sX[rs + rl][col] = -s;
-        }
-        __syncthreads();
-    }
-    // outputs: L (strict lower) and D into the front, D into Dvec, X row-major into linv
-    for (int e = tid; e < NB * NB; e += DIAG_B_THREADS) {
-        const int r = e % NB, c = e / NB;
-        if (c <= r && r < kk) F[(int64_t)(c0 + c) * fN + c0 + r] = sA[r][c];
-    }
-    T* Li = linv + linv_off[nd] + (int64_t)t * NB * NB;
-    for (int e = tid; e < NB * NB; e += DIAG_B_THREADS) {
-        const int r = e / NB, c = e % NB;
-        Li[e] = (c <= r && r < kk) ? sX[r][c] : T(0);
-    }
-    if (tid < kk) Dvec[own[nd] + c0 + tid] = sA[tid][tid];
-    __syncthreads();
-    if (tid == 0 && bad) atomicExch(status, 1);
-}
-
 // Four consecutive shared-memory values (16-byte aligned) in one or two vector loads.
 __device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
     const float4 x = *reinterpret_cast<const float4*>(p);
@@ -1651,11 +1484,6 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
         df_halo_t_.upload(halo_t, stream_);
         df_cnt_.alloc((size_t)4 * nnodes_ + 1);
         df_r_.alloc((size_t)std::max(n_, 1) * MF_MAX_RHS);
-        {
-            // blocked diagonal tiles for FP32 fronts (KLSA_DIAG_KERNEL=pairs: the pivot-pair kernel)
-            const char* e = std::getenv("KLSA_DIAG_KERNEL");
-            diag_blocked_ = sizeof(T) == 4 && !(e && std::string(e) == "pairs");
-        }
         if (const char* e = std::getenv("KLSA_SOLVE_STALL_NODE")) {
             // the k-th leaf of the elimination tree (a leaf has a parent unless the tree is one node)
             const auto& leaves = level_nodes_[0];
@@ -1830,17 +1658,7 @@ void MultifrontalT<T>::factorize_launches(const T* d_vals) {
         for (Step& st : lv.steps) {
             if (st.diag.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                bool done = false;
-                if constexpr (sizeof(T) == 4) {
-                    if (diag_blocked_) {
-                        mf_diag_blocked_kernel<T><<<st.diag.count, DIAG_B_THREADS, 0, stream_>>>(
-                            st.diag.items, st.t, d_f_.get(), d_k_.get(), d_own_.get(), d_front_off_.get(),
-                            d_linv_off_.get(), pool_.get(), D_.get(), linv_.get(), status_.get());
-                        done = true;
-                    }
-                }
-                if (!done)
-                    mf_diag_kernel<T><<<st.diag.count, DIAG_THREADS, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
+                mf_diag_kernel<T><<<st.diag.count, DIAG_THREADS, 0, stream_>>>(st.diag.items, st.t, d_f_.get(), d_k_.get(),
                                                                        d_own_.get(), d_front_off_.get(),
                                                                        d_linv_off_.get(), pool_.get(), D_.get(),
                                                                        linv_.get(), status_.get());

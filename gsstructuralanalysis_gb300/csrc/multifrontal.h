@@ -97,7 +97,6 @@ private:
     DevBuf<T> df_r_;             // fan-out right-hand side (n x MF_MAX_RHS)
     int df_qtotal_ = 0;
     int df_grid_[3] = {0, 0, 0};
-    bool diag_blocked_ = false;  // blocked diagonal-tile kernel (FP32 fronts)
     int df_stall_node_ = -1;     // test hook (KLSA_SOLVE_STALL_NODE=k): the k-th leaf's first phase never completes
     bool persistent_ok_ = true;
     size_t ps_smem_[3] = {0, 0, 0};
