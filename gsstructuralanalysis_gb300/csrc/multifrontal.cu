@@ -9,6 +9,9 @@
 //      64x64 tile).
 // No pivoting (as Eigen's SimplicialLDLT); a zero or non-finite pivot sets the status word.
 #include "multifrontal.h"
+#include "tcgen05.cuh"
+
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
@@ -401,6 +404,112 @@ __global__ void __launch_bounds__(256) mf_update_kernel(const int4* __restrict__
             if (C < fN && R < fN && R >= C) F[(int64_t)C * fN + R] = old[i][j] - acc[i][j];
         }
     }
+}
+
+// The same trailing update on the 5th-generation tensor cores (FP32 fronts).  One CTA of 128
+// threads per 64 x 64 lower tile: the W and L blocks (K = kk <= 64, zero-padded to a multiple
+// of 8) are split into TF32 high and low parts, hi = tf32(x) and lo = x - hi, and staged
+// K-major in shared memory; one thread issues D = Wh Lh^T + Wh Ll^T + Wl Lh^T as tcgen05
+// kind::tf32 MMAs (M = 128, of which rows 0..63 are the tile; N = 64, K = 8 each) into a
+// 64-column FP32 accumulator in tensor memory, committed to an mbarrier.  Three-term TF32
+// splitting keeps the product at FP32 accuracy (the dropped lo*lo term is below 2^-22
+// relative).  Warps 0 and 1 read their 32 accumulator lanes each and subtract them from the
+// front.  The wait for the MMAs is bounded: on expiry the status flag is raised, the tile is
+// left unchanged and the tensor memory is still released.
+constexpr int TC_THREADS = 128;
+constexpr int TC_TILE_BYTES = NB * NB * 4;   // one 64 x 64 FP32 operand tile
+constexpr size_t TC_SMEM = 4 * (size_t)TC_TILE_BYTES;
+
+__global__ void __launch_bounds__(TC_THREADS) mf_update_tc_kernel(const int4* __restrict__ items, int t,
+                                                                  const int* __restrict__ f, const int* __restrict__ k,
+                                                                  const int64_t* __restrict__ front_off,
+                                                                  const int64_t* __restrict__ ws_off, float* pool,
+                                                                  const float* __restrict__ ws, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tholder;
+    // [Wh | Wl | Lh | Ll]; the M = 128 MMA reads 128 rows of Wh and Wl, the second half of which
+    // lies in the next operand tile and lands in accumulator rows 64..127, which are not used
+    float* Wh = reinterpret_cast<float*>(smem_raw);
+    float* Wl = Wh + NB * NB;
+    float* Lh = Wl + NB * NB;
+    float* Ll = Lh + NB * NB;
+    const int4 it = items[blockIdx.x];
+    const int nd = it.x;
+    const int fN = f[nd], kN = k[nd];
+    const int c0 = t * NB;
+    const int kk = min(NB, kN - c0);
+    const int k8 = (kk + 7) & ~7;
+    const int R0 = c0 + kk + it.y * NB, C0 = c0 + kk + it.z * NB;
+    float* F = pool + front_off[nd];
+    const float* W = ws + ws_off[nd];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tc::tmem_alloc(&tholder, 64);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    {
+        // every load in flight first (consecutive threads: consecutive rows of one column), then
+        // the split and the K-major stores
+        constexpr int PER = NB * NB / TC_THREADS;
+        float vw[PER], vl[PER];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = tid + TC_THREADS * q, r = e % NB, m = e / NB;
+            vw[q] = (m < kk && R0 + r < fN) ? W[(int64_t)m * fN + R0 + r] : 0.f;
+            vl[q] = (m < kk && C0 + r < fN) ? F[(int64_t)(c0 + m) * fN + C0 + r] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = tid + TC_THREADS * q, r = e % NB, m = e / NB;
+            if (m < k8) {
+                const float wh = tc::to_tf32(vw[q]), lh = tc::to_tf32(vl[q]);
+                const uint32_t o = tc::kmajor_offset(r, m, NB / 4) >> 2;
+                Wh[o] = wh;
+                Wl[o] = vw[q] - wh;
+                Lh[o] = lh;
+                Ll[o] = vl[q] - lh;
+            }
+        }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tholder;
+    if (tid == 0) {
+        constexpr uint32_t LBO = 128, SBO = 128 * (NB / 4);
+        const uint32_t idesc = tc::idesc_tf32(128, 64);
+        const uint32_t wh = tc::smem_u32(Wh), wl = tc::smem_u32(Wl), lh = tc::smem_u32(Lh), ll = tc::smem_u32(Ll);
+        for (int s8 = 0; s8 < k8 / 8; ++s8) {
+            const uint32_t o = 256u * s8;   // two core matrices along K per MMA
+            const uint64_t dwh = tc::smem_desc_kmajor(wh + o, LBO, SBO), dwl = tc::smem_desc_kmajor(wl + o, LBO, SBO);
+            const uint64_t dlh = tc::smem_desc_kmajor(lh + o, LBO, SBO), dll = tc::smem_desc_kmajor(ll + o, LBO, SBO);
+            tc::mma_tf32(taddr, dwh, dlh, idesc, s8 > 0);
+            tc::mma_tf32(taddr, dwh, dll, idesc, true);
+            tc::mma_tf32(taddr, dwl, dlh, idesc, true);
+        }
+        tc::commit(&mbar);
+    }
+    bool ok = tc::mbar_wait(&mbar, 0, 1u << 20);
+    if (!ok) ok = tc::mbar_wait(&mbar, 0, 1u << 20);
+    tc::fence_after_sync();
+    if (ok && warp < 2 && k8 > 0) {
+        const int r = 32 * warp + lane, R = R0 + r;
+#pragma unroll
+        for (int cc = 0; cc < NB; cc += 16) {
+            float v[16];
+            tc::ld_32x32b_x16(taddr + (static_cast<uint32_t>(32 * warp) << 16) + cc, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int C = C0 + cc + i;
+                if (C < fN && R < fN && R >= C) F[(int64_t)C * fN + R] -= v[i];
+            }
+        }
+    }
+    if (!ok && tid == 0) atomicExch(status, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(taddr, 64);
 }
 
 // ---- node inverses X = L11^-1 (k x k, row-major, lower) for the triangular solves -------------
@@ -1562,6 +1671,12 @@ MultifrontalT<T>::MultifrontalT(const NDTree& Tr, const std::vector<int>& rowptr
     const int gsm = (int)gemm_smem(sizeof(T));
     KL_CUDA(cudaFuncSetAttribute(mf_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
     KL_CUDA(cudaFuncSetAttribute(mf_update_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+    if constexpr (std::is_same<T, float>::value) {
+        const char* e = std::getenv("KLSA_UPDATE_KERNEL");
+        update_tc_ = e && std::string(e) == "tc";
+        if (update_tc_)
+            KL_CUDA(cudaFuncSetAttribute(mf_update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+    }
     KL_CUDA(cudaFuncSetAttribute(mf_xoff_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
     KL_CUDA(cudaStreamSynchronize(stream_));
 }
@@ -1630,6 +1745,21 @@ void MultifrontalT<T>::factorize_async(const T* d_vals) {
     replay(fact_graph_, d_vals, nullptr, [&] { factorize_launches(d_vals); });
 }
 
+// trailing-update tiles of one step: CUDA-core tiles; with KLSA_UPDATE_KERNEL=tc and FP32 fronts
+// the tensor-core tiles (tcgen05, 3xTF32)
+template <class T>
+void MultifrontalT<T>::launch_update(const MFWork& w, int t, const T* W, cudaStream_t s) {
+    if constexpr (std::is_same<T, float>::value) {
+        if (update_tc_) {
+            mf_update_tc_kernel<<<w.count, TC_THREADS, TC_SMEM, s>>>(w.items, t, d_f_.get(), d_k_.get(), d_front_off_.get(),
+                                                                   d_ws_off_.get(), pool_.get(), W, status_.get());
+            return;
+        }
+    }
+    mf_update_kernel<T><<<w.count, 256, gemm_smem(sizeof(T)), s>>>(w.items, t, d_f_.get(), d_k_.get(), d_front_off_.get(),
+                                                                  d_ws_off_.get(), pool_.get(), W);
+}
+
 template <class T>
 void MultifrontalT<T>::factorize_launches(const T* d_vals) {
     KL_CUDA(cudaMemsetAsync(pool_.get(), 0, pool_.size() * sizeof(T), stream_));
@@ -1695,9 +1825,7 @@ void MultifrontalT<T>::factorize_launches(const T* d_vals) {
                 KL_CUDA(cudaEventRecord(ev_panel_, stream_));
                 KL_CUDA(cudaStreamWaitEvent(side_, ev_panel_, 0));
                 cudaEvent_t evk = g_timer.begin(side_);
-                mf_update_kernel<T><<<st.upd_rest.count, 256, gemm_smem(sizeof(T)), side_>>>(
-                    st.upd_rest.items, st.t, d_f_.get(), d_k_.get(), d_front_off_.get(), d_ws_off_.get(), pool_.get(),
-                    W);
+                launch_update(st.upd_rest, st.t, W, side_);
                 g_timer.end(side_, 4, evk);
                 count_launch();
                 KL_CUDA(cudaEventRecord(ev_rest_, side_));
@@ -1705,9 +1833,7 @@ void MultifrontalT<T>::factorize_launches(const T* d_vals) {
             }
             if (st.upd_next.count) {
                 cudaEvent_t evk = g_timer.begin(stream_);
-                mf_update_kernel<T><<<st.upd_next.count, 256, gemm_smem(sizeof(T)), stream_>>>(
-                    st.upd_next.items, st.t, d_f_.get(), d_k_.get(), d_front_off_.get(), d_ws_off_.get(), pool_.get(),
-                    W);
+                launch_update(st.upd_next, st.t, W, stream_);
                 g_timer.end(stream_, 4, evk);
                 count_launch();
             }

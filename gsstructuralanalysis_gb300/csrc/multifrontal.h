@@ -97,7 +97,9 @@ private:
     DevBuf<T> df_r_;             // fan-out right-hand side (n x MF_MAX_RHS)
     int df_qtotal_ = 0;
     int df_grid_[3] = {0, 0, 0};
-    int df_stall_node_ = -1;     // test hook (KLSA_SOLVE_STALL_NODE=k): the k-th leaf's first phase never completes
+    int df_stall_node_ = -1;
+    bool update_tc_ = false;     // trailing updates on the tensor cores (FP32 fronts, KLSA_UPDATE_KERNEL=tc)
+    void launch_update(const MFWork& w, int t, const T* W, cudaStream_t s);     // test hook (KLSA_SOLVE_STALL_NODE=k): the k-th leaf's first phase never completes
     bool persistent_ok_ = true;
     size_t ps_smem_[3] = {0, 0, 0};
     GraphSlot fact_graph_, solve_graph_[3];

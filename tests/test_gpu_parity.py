@@ -123,6 +123,44 @@ def test_solve_schedules_agree(lib, oracle_mod, m, p, monkeypatch):
             assert rel(y, ref) <= tol, (prec, kern, rel(y, ref), tol)
 
 
+def test_tensor_core_trailing_update(lib, oracle_mod, monkeypatch):
+    """The trailing update of the factorisation on the tensor cores (tcgen05 kind::tf32 with a
+    three-term TF32 split; KLSA_UPDATE_KERNEL=tc, read when a problem's factorisation is set up)
+    against the CUDA-core tiles and SuperLU.  The TF32 split drops the lo*lo term and the tensor
+    core reads the lo parts as TF32, so the FP32 factor is somewhat less accurate than with FMA
+    tiles (measured 1.6e-2 against 4.9e-3 relative on this shell); FP64 refinement brings both to
+    1e-9."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=32, p=2)
+    oa = oracle_mod.OracleAssembler(prob)
+    rng = np.random.default_rng(5)
+    ys = {}
+    for mode in ("tc", "fma"):
+        if mode == "tc":
+            monkeypatch.setenv("KLSA_UPDATE_KERNEL", "tc")
+        else:
+            monkeypatch.delenv("KLSA_UPDATE_KERNEL", raising=False)
+        gp = G.Problem(prob)
+        if mode == "tc":
+            x = 1e-3 * rng.standard_normal(gp.ndof)
+            b = rng.standard_normal((2, gp.ndof))
+            Kr = oa.jacobian(x).tocsc()
+            ref = np.stack([spla.spsolve(Kr, bi) for bi in b])
+        s1 = G.SparseSolver(gp, "SimplicialLDLT", {"Refinement": 0})
+        assert s1.compute_jacobian(x) == 0
+        s2 = G.SparseSolver(gp, "SimplicialLDLT", {"Refinement": 10, "RefineTol": 1e-13})
+        assert s2.compute_jacobian(x) == 0
+        ys[mode] = (s1.solve(b), s2.solve(b))
+    monkeypatch.delenv("KLSA_UPDATE_KERNEL", raising=False)
+
+    def rel(a, r):
+        return np.linalg.norm(a - r) / np.linalg.norm(r)
+
+    e_tc, e_fma = rel(ys["tc"][0], ref), rel(ys["fma"][0], ref)
+    assert e_fma < 0.2 and e_tc <= 5.0 * e_fma + 1e-6, (e_tc, e_fma)
+    assert rel(ys["tc"][1], ref) < 1e-9 and rel(ys["fma"][1], ref) < 1e-9
+
+
 def test_djacobian_matches(lib, oracle_mod):
     """dJacobian_t (gsStructuralAnalysisTypes.h:91-92), called with a solution update as
     gsALMBase::_computeJacobian does (gsALMBase.hpp:214-223): the oracle's tangent at x, for
