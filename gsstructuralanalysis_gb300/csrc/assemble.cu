@@ -526,7 +526,7 @@ __device__ __forceinline__ void fint_group_auto(int grp, int nel, int m1, int n1
 }
 
 template <int P>
-__global__ void __launch_bounds__(128) kl_fint_df_kernel(int nel, int m1, int n1, int ncp, int nq,
+__global__ void __launch_bounds__(128, 6) kl_fint_df_kernel(int nel, int m1, int n1, int ncp, int nq,
                                                          const double* __restrict__ tab1,
                                                          const double* __restrict__ tab2,
                                                          const float2* __restrict__ tab1s,
