@@ -71,7 +71,9 @@ template <class T> struct QPState {
     T dV;
 };
 
-template <int P, class T>
+// WITH_C: also keep the scaled material tensors t C and t^3/12 C (the tangent needs them; the
+// residual needs only the stress resultants)
+template <int P, class T, bool WITH_C = true>
 __device__ __forceinline__ void qp_state(const double* __restrict__ geo, const T du[15], T tm, T tb, QPState<T>& s) {
     V3T<T> A1 = mk<T>(geo[0], geo[1], geo[2]), A2 = mk<T>(geo[3], geo[4], geo[5]);
     V3T<T> X11 = mk<T>(geo[6], geo[7], geo[8]), X22 = mk<T>(geo[9], geo[10], geo[11]), X12 = mk<T>(geo[12], geo[13], geo[14]);
@@ -95,14 +97,22 @@ __device__ __forceinline__ void qp_state(const double* __restrict__ geo, const T
     T k2 = T(2) * (T(geo[24]) - dot3(s.x12, s.a3));
     T C00 = geo[15], C01 = geo[16], C02 = geo[17], C11 = geo[18], C12 = geo[19], C22 = geo[20];
     T C[3][3] = {{C00, C01, C02}, {C01, C11, C12}, {C02, C12, C22}};
+    if constexpr (WITH_C) {
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) { s.Cm[a][b] = tm * C[a][b]; s.Cb[a][b] = tb * C[a][b]; }
+            for (int b = 0; b < 3; ++b) { s.Cm[a][b] = tm * C[a][b]; s.Cb[a][b] = tb * C[a][b]; }
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        s.n[a] = s.Cm[a][0] * e0 + s.Cm[a][1] * e1 + s.Cm[a][2] * e2;
-        s.m[a] = s.Cb[a][0] * k0 + s.Cb[a][1] * k1 + s.Cb[a][2] * k2;
+        for (int a = 0; a < 3; ++a) {
+            s.n[a] = s.Cm[a][0] * e0 + s.Cm[a][1] * e1 + s.Cm[a][2] * e2;
+            s.m[a] = s.Cb[a][0] * k0 + s.Cb[a][1] * k1 + s.Cb[a][2] * k2;
+        }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s.n[a] = tm * (C[a][0] * e0 + C[a][1] * e1 + C[a][2] * e2);
+            s.m[a] = tb * (C[a][0] * k0 + C[a][1] * k1 + C[a][2] * k2);
+        }
     }
     s.v = mk<T>(s.m[0] * s.x11.x + s.m[1] * s.x22.x + T(2) * s.m[2] * s.x12.x,
                 s.m[0] * s.x11.y + s.m[1] * s.x22.y + T(2) * s.m[2] * s.x12.y,
@@ -342,7 +352,7 @@ __device__ __forceinline__ void fint_group(int grp, int nel, int m1, int n1, int
         }
         const double* geo = qpgeo + ((size_t)e * nqp + idx) * QGEO;
         QPState<double> st;
-        qp_state<P, double>(geo, du, tm, tb, st);
+        qp_state<P, double, false>(geo, du, tm, tb, st);
         // f_{A,i} = sum_qp [N1 G1 + N2 G2 - N11 S11 - N22 S22 - N12 S12]_i with
         //   G1 = dV (n0 a1 + n2 a2 - (a2 x w)/l),  G2 = dV (n1 a2 + n2 a1 - (w x a1)/l),
         //   S11 = dV m0 a3, S22 = dV m1 a3, S12 = 2 dV m2 a3   (w = v - (v.a3) a3)
@@ -440,7 +450,7 @@ __device__ __forceinline__ void fint_group_df(int grp, int nel, int m1, int n1, 
         for (int k = 0; k < 15; ++k) dud[k] = df_to_double(du[k]);
         const double* geo = qpgeo + ((size_t)e * nqp + idx) * QGEO;
         QPState<double> st;
-        qp_state<P, double>(geo, dud, tm, tb, st);
+        qp_state<P, double, false>(geo, dud, tm, tb, st);
         const double dV = st.dV;
         V3T<double> u1 = cross3(st.a2, st.w), u2 = cross3(st.w, st.a1);
         df2* o = qsw[slot * nqp + idx];
