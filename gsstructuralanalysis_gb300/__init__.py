@@ -233,8 +233,17 @@ class Options:
             self.h = None
 
 
+def _reject_rational(prob):
+    """The device kernels evaluate a polynomial B-spline basis; a NURBS patch (weights other than
+    1) is assembled only by the FP64 oracle for now."""
+    w = getattr(prob, "weights", None)
+    if w is not None and not np.allclose(np.asarray(w, dtype=np.float64), 1.0):
+        raise NotImplementedError("rational (NURBS) patch: the device kernels evaluate a polynomial B-spline basis")
+
+
 def _patch_desc(prob, keep):
     """PatchDesc of a problems.PatchProblem; the arrays it points to are stored in ``keep``."""
+    _reject_rational(prob)
     k = dict(
         k1=np.ascontiguousarray(prob.knots1, dtype=np.float64),
         k2=np.ascontiguousarray(prob.knots2, dtype=np.float64),

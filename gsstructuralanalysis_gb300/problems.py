@@ -73,6 +73,7 @@ class PatchProblem:
     edge_loads: np.ndarray = field(default_factory=lambda: np.zeros((0, 4)))
     nq: int = 0                          # Gauss points per direction (0: p+1)
     name: str = ""
+    weights: np.ndarray | None = None    # NURBS weights (ncp,); None: B-spline
 
     @property
     def ncp(self) -> int:

@@ -3,7 +3,7 @@
 The reader follows what ``solvers/static_shell_XML.cpp:92-199`` takes from a file:
 
   id 0        the geometry: a ``MultiPatch`` whose ``patches`` name one ``Geometry``, or a
-              ``Geometry`` directly (``TensorBSpline2``; ``TensorNurbs2`` with unit weights)
+              ``Geometry`` directly (``TensorBSpline2`` or ``TensorNurbs2``)
   id 10       the material: ``MaterialMatrix type="Linear3"`` (Thickness, Density,
               Parameters E and nu), or the older ``Function`` ids 10-13 tagged ``Material``
               (thickness, E, nu, density)
@@ -20,13 +20,15 @@ Degree elevation and uniform refinement follow ``gsGeometry::degreeElevate`` (ev
 multiplicity grows by one, smoothness kept) and ``uniformRefine`` (one knot in the middle of every
 nonzero span), applied as in static_shell_XML.cpp:95-104 (elevate, then refine).  Control points
 of the elevated / refined patch come from interpolation at the Greville points of the new space,
-which reproduces the (nested) geometry exactly.
+which reproduces the (nested) geometry exactly; a rational (NURBS) patch is transferred in
+homogeneous coordinates (w X, w), which is exact as well.
 
 Side numbers are gismo's boxSide (1 west xi1=0, 2 east xi1=1, 3 south xi2=0, 4 north xi2=1) and
 corner numbers its boxCorner (1 (0,0), 2 (1,0), 3 (0,1), 4 (1,1)).  Anything the device path
-cannot represent (several patches, rational weights, unequal degrees, repeated interior knots,
-non-SVK materials, inhomogeneous or coupled conditions, pressure, non-constant functions) raises
-``NotImplementedError`` with the reason.
+cannot represent (several patches, unequal degrees, repeated interior knots, non-SVK materials,
+inhomogeneous or coupled conditions, pressure, non-constant functions) raises
+``NotImplementedError`` with the reason.  NURBS weights are read into ``PatchProblem.weights``:
+the FP64 oracle assembles rational patches, the device problem does not yet (it raises).
 """
 from __future__ import annotations
 
@@ -125,11 +127,29 @@ def transfer(U1, U2, p1, p2, ctrl, V1, V2, q1, q2) -> np.ndarray:
         T.append(np.linalg.solve(Af, Ac))
     n1c, n2c = len(U1) - p1 - 1, len(U2) - p2 - 1
     n1f, n2f = len(V1) - q1 - 1, len(V2) - q2 - 1
-    out = np.zeros((n1f * n2f, 3))
-    for c in range(3):
+    out = np.zeros((n1f * n2f, ctrl.shape[1]))
+    for c in range(ctrl.shape[1]):
         C = ctrl[:, c].reshape(n2c, n1c)
         out[:, c] = (T[1] @ C @ T[0].T).ravel()
     return out
+
+
+def _elevate_refine(U1, U2, p1, p2, ctrl, weights, elevate, refine):
+    """Degree elevation (``elevate`` times) and uniform refinement (``refine`` times); a rational
+    patch goes through its homogeneous net (w X, w)."""
+    net = ctrl if weights is None else np.hstack([ctrl * weights[:, None], weights[:, None]])
+    for _ in range(elevate):
+        V1, V2 = elevate_knots(U1), elevate_knots(U2)
+        net = transfer(U1, U2, p1, p2, net, V1, V2, p1 + 1, p2 + 1)
+        U1, U2, p1, p2 = V1, V2, p1 + 1, p2 + 1
+    for _ in range(refine):
+        V1, V2 = refine_knots(U1), refine_knots(U2)
+        net = transfer(U1, U2, p1, p2, net, V1, V2, p1, p2)
+        U1, U2 = V1, V2
+    if weights is None:
+        return U1, U2, p1, p2, net, None
+    w = net[:, 3].copy()
+    return U1, U2, p1, p2, net[:, :3] / w[:, None], w
 
 
 # -------------------------------------------------------------------------------------------
@@ -176,11 +196,11 @@ def _geometry(root, ids):
         raise ValueError("no geometry with id 0")
     typ = g.get("type")
     basis = g.find("Basis")
+    weights = None
     if typ == "TensorNurbs2":
         w = _numbers(basis.find("weights").text)
         if not np.allclose(w, 1.0):
-            raise NotImplementedError("rational (NURBS) geometry with non-unit weights: the device kernels "
-                                      "evaluate a polynomial B-spline basis")
+            weights = np.asarray(w, dtype=np.float64)
         basis = basis.find("Basis")
     elif typ != "TensorBSpline2":
         raise NotImplementedError(f"geometry type {typ}")
@@ -194,7 +214,9 @@ def _geometry(root, ids):
     if int(coefs.get("geoDim", "3")) != 3:
         raise NotImplementedError("planar geometry: the shell needs geoDim 3")
     ctrl = _numbers(coefs.text).reshape(-1, 3)
-    return kv[0], kv[1], deg[0], deg[1], ctrl
+    if weights is not None and len(weights) != len(ctrl):
+        raise ValueError(f"{len(weights)} weights for {len(ctrl)} control points")
+    return kv[0], kv[1], deg[0], deg[1], ctrl, weights
 
 
 def _material(ids):
@@ -268,24 +290,18 @@ def _parse(path: str):
     return ET.fromstring(re.sub(r"<\?xml[^>]*\?>", "", text))
 
 
-def read_geometry(path: str, elevate: int = 0, refine: int = 0):
+def read_geometry(path: str, elevate: int = 0, refine: int = 0, with_weights: bool = False):
     """The geometry of a file that holds only a surface (gsReadFile<>(file, mp) on a file with a
     ``Geometry`` or single-patch ``MultiPatch`` id 0, as benchmarks/benchmark_Roof.cpp:146-157
     reads filedata/surface/scordelis_lo_roof_shallow.xml), degree-elevated ``elevate`` times and
-    uniformly refined ``refine`` times.  Returns (p, knots1, knots2, ctrl (n1*n2, 3))."""
+    uniformly refined ``refine`` times.  Returns (p, knots1, knots2, ctrl (n1*n2, 3)), and the
+    NURBS weights (None for a B-spline) as a fifth item with ``with_weights``."""
     root = _parse(path)
-    U1, U2, p1, p2, ctrl = _geometry(root, _by_id(root))
-    for _ in range(elevate):
-        V1, V2 = elevate_knots(U1), elevate_knots(U2)
-        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1 + 1, p2 + 1)
-        U1, U2, p1, p2 = V1, V2, p1 + 1, p2 + 1
-    for _ in range(refine):
-        V1, V2 = refine_knots(U1), refine_knots(U2)
-        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1, p2)
-        U1, U2 = V1, V2
+    U1, U2, p1, p2, ctrl, w = _geometry(root, _by_id(root))
+    U1, U2, p1, p2, ctrl, w = _elevate_refine(U1, U2, p1, p2, ctrl, w, elevate, refine)
     if p1 != p2:
         raise NotImplementedError(f"degrees {p1} and {p2}: the device path takes equal degrees")
-    return p1, U1, U2, ctrl
+    return (p1, U1, U2, ctrl, w) if with_weights else (p1, U1, U2, ctrl)
 
 
 def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProblem:
@@ -293,15 +309,8 @@ def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProble
     XML solvers (static_shell_XML.cpp:95-104)."""
     root = _parse(path)
     ids = _by_id(root)
-    U1, U2, p1, p2, ctrl = _geometry(root, ids)
-    for _ in range(elevate):
-        V1, V2 = elevate_knots(U1), elevate_knots(U2)
-        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1 + 1, p2 + 1)
-        U1, U2, p1, p2 = V1, V2, p1 + 1, p2 + 1
-    for _ in range(refine):
-        V1, V2 = refine_knots(U1), refine_knots(U2)
-        ctrl = transfer(U1, U2, p1, p2, ctrl, V1, V2, p1, p2)
-        U1, U2 = V1, V2
+    U1, U2, p1, p2, ctrl, weights = _geometry(root, ids)
+    U1, U2, p1, p2, ctrl, weights = _elevate_refine(U1, U2, p1, p2, ctrl, weights, elevate, refine)
     if p1 != p2:
         raise NotImplementedError(f"degrees {p1} and {p2}: the device path takes equal degrees")
     p = p1
@@ -377,7 +386,7 @@ def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProble
     prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=np.ascontiguousarray(ctrl), E=E, nu=nu,
                           t=t, rho=rho, fixed=fixed.ravel(), surface_load=surface, point_loads=point_loads,
                           edge_loads=np.array(edge_loads, dtype=np.float64).reshape(-1, 4), nq=nq,
-                          name=f"xml:{path.rsplit('/', 1)[-1]}")
+                          name=f"xml:{path.rsplit('/', 1)[-1]}", weights=weights)
     out = XMLProblem(prob)
     for k in range(90, 96):
         for el in ids.get(k, []):

@@ -153,7 +153,37 @@ struct Patch {
     const double* U2;
     const double* X;   // ncp*3, cp-major (A*3+c)
     double E, nu, t, rho;
+    const double* W = nullptr;   // NURBS weights (ncp); null: B-spline (all weights 1)
 };
+
+// Rational basis of a NURBS patch from the tensor-product B-spline values at one point:
+// R_A = w_A N_A / W with W = sum_B w_B N_B, and by the quotient rule (o_a = W,a / W)
+//   R_A,a  = (w_A / W) (N_A,a - N_A o_a)
+//   R_A,ab = (w_A / W) (N_A,ab - N_A,a o_b - N_A,b o_a + N_A (2 o_a o_b - W,ab / W)).
+// N, N1, N2, N11, N22, N12 (nb values each) are replaced in place; w holds the nb weights.
+void rationalize(int nb, const double* w, double* N, double* N1, double* N2, double* N11, double* N22,
+                 double* N12) {
+    double W = 0, W1 = 0, W2 = 0, W11 = 0, W22 = 0, W12 = 0;
+    for (int k = 0; k < nb; ++k) {
+        W += w[k] * N[k];
+        W1 += w[k] * N1[k];
+        W2 += w[k] * N2[k];
+        W11 += w[k] * N11[k];
+        W22 += w[k] * N22[k];
+        W12 += w[k] * N12[k];
+    }
+    const double iW = 1.0 / W, o1 = W1 * iW, o2 = W2 * iW;
+    const double c11 = 2 * o1 * o1 - W11 * iW, c22 = 2 * o2 * o2 - W22 * iW, c12 = 2 * o1 * o2 - W12 * iW;
+    for (int k = 0; k < nb; ++k) {
+        const double c = w[k] * iW, n0 = N[k], n1 = N1[k], n2 = N2[k];
+        N[k] = c * n0;
+        N1[k] = c * (n1 - n0 * o1);
+        N2[k] = c * (n2 - n0 * o2);
+        N11[k] = c * (N11[k] - 2 * n1 * o1 + n0 * c11);
+        N22[k] = c * (N22[k] - 2 * n2 * o2 + n0 * c22);
+        N12[k] = c * (N12[k] - n1 * o2 - n2 * o1 + n0 * c12);
+    }
+}
 
 struct Elem {
     int s1, s2;          // knot spans
@@ -200,11 +230,18 @@ void eval_qp(const Patch& P, const Elem& e, double xi1, double xi2, double wq, Q
             q.N11[k] = b1[2][a] * b2[0][b];
             q.N22[k] = b1[0][a] * b2[2][b];
             q.N12[k] = b1[1][a] * b2[1][b];
-            const double* Xa = P.X + 3 * q.cp[k];
-            Vec3 XA{Xa[0], Xa[1], Xa[2]};
-            A1 = A1 + q.N1[k] * XA;
-            A2 = A2 + q.N2[k] * XA;
         }
+    if (P.W) {
+        double w[MAXB * MAXB];
+        for (int k = 0; k < q.nb; ++k) w[k] = P.W[q.cp[k]];
+        rationalize(q.nb, w, q.N, q.N1, q.N2, q.N11, q.N22, q.N12);
+    }
+    for (int k = 0; k < q.nb; ++k) {
+        const double* Xa = P.X + 3 * q.cp[k];
+        Vec3 XA{Xa[0], Xa[1], Xa[2]};
+        A1 = A1 + q.N1[k] * XA;
+        A2 = A2 + q.N2[k] * XA;
+    }
     (void)e;
     q.dA = std::sqrt(dot(cross(A1, A2), cross(A1, A2))) * wq;
 }
@@ -406,9 +443,10 @@ void klo_full_pattern(int p, int n1, int n2, int64_t* rowptr, int32_t* cols) {
 // (full layout, may be null) at full displacement u (component-blocked).
 int klo_assemble(int p, int n1, int n2, const double* U1, const double* U2, const double* X,
                  double E, double nu, double t, int nq, const double* ufull, double* Kvals, double* fint,
-                 int nthreads) {
+                 int nthreads, const double* weights) {
     if (p < 1 || p > MAXP) return -1;
     Patch P = make_patch(p, n1, n2, U1, U2, X, E, nu, t, 0.0, nq);
+    P.W = weights;
     Pattern pt{n1, n2, p, 0, {}};
     pt.build();
     int ncp = n1 * n2;
@@ -453,8 +491,9 @@ int klo_assemble(int p, int n1, int n2, const double* U1, const double* U2, cons
 
 // Consistent mass matrix M = int rho t N_A N_B dA (identity in the components) in the full pattern.
 int klo_mass(int p, int n1, int n2, const double* U1, const double* U2, const double* X, double rho, double t,
-             int nq, double* Mvals) {
+             int nq, double* Mvals, const double* weights) {
     Patch P = make_patch(p, n1, n2, U1, U2, X, 1.0, 0.0, t, rho, nq);
+    P.W = weights;
     Pattern pt{n1, n2, p, 0, {}};
     pt.build();
     std::memset(Mvals, 0, sizeof(double) * pt.rowptr.back());
@@ -483,8 +522,10 @@ int klo_mass(int p, int n1, int n2, const double* U1, const double* U2, const do
 // point loads (npl x [xi1, xi2, Px, Py, Pz]) and edge line loads (ned x [side, qx, qy, qz],
 // side 0: xi1=0, 1: xi1=1, 2: xi2=0, 3: xi2=1; per unit reference length).
 int klo_force(int p, int n1, int n2, const double* U1, const double* U2, const double* X, int nq,
-              const double* qsurf, int npl, const double* pl, int ned, const double* ed, double* F) {
+              const double* qsurf, int npl, const double* pl, int ned, const double* ed, double* F,
+              const double* weights) {
     Patch P = make_patch(p, n1, n2, U1, U2, X, 1.0, 0.0, 1.0, 0.0, nq);
+    P.W = weights;
     int ncp = n1 * n2;
     std::memset(F, 0, sizeof(double) * 3 * ncp);
     double gx[16], gw[16];
@@ -510,10 +551,17 @@ int klo_force(int p, int n1, int n2, const double* U1, const double* U2, const d
         double b1[3][MAXB], b2[3][MAXB];
         basis_ders(n1, p, U1, L[0], s1, b1);
         basis_ders(n2, p, U2, L[1], s2, b2);
+        double Wp = 1.0;
+        if (weights) {
+            Wp = 0.0;
+            for (int b = 0; b <= p; ++b)
+                for (int a = 0; a <= p; ++a) Wp += weights[(s2 - p + b) * n1 + (s1 - p + a)] * b1[0][a] * b2[0][b];
+        }
         for (int b = 0; b <= p; ++b)
             for (int a = 0; a <= p; ++a) {
                 int A = (s2 - p + b) * n1 + (s1 - p + a);
-                for (int c = 0; c < 3; ++c) F[(size_t)c * ncp + A] += b1[0][a] * b2[0][b] * L[2 + c];
+                const double R = (weights ? weights[A] / Wp : 1.0) * b1[0][a] * b2[0][b];
+                for (int c = 0; c < 3; ++c) F[(size_t)c * ncp + A] += R * L[2 + c];
             }
     }
     for (int k = 0; k < ned; ++k) {
@@ -533,18 +581,37 @@ int klo_force(int p, int n1, int n2, const double* U1, const double* U2, const d
                 double b1[3][MAXB], b2[3][MAXB];
                 basis_ders(n1, p, U1, xi1, s1, b1);
                 basis_ders(n2, p, U2, xi2, s2, b2);
+                // values and edge-direction derivatives of the (rational) basis
+                double Rv[MAXB * MAXB], Rt[MAXB * MAXB];
+                double We = 0.0, Wt = 0.0;
+                for (int b = 0; b <= p; ++b)
+                    for (int a = 0; a <= p; ++a) {
+                        const int k = b * (p + 1) + a, A = (s2 - p + b) * n1 + (s1 - p + a);
+                        Rv[k] = b1[0][a] * b2[0][b];
+                        Rt[k] = along1 ? b1[1][a] * b2[0][b] : b1[0][a] * b2[1][b];
+                        const double w = weights ? weights[A] : 1.0;
+                        We += w * Rv[k];
+                        Wt += w * Rt[k];
+                    }
+                if (weights)
+                    for (int b = 0; b <= p; ++b)
+                        for (int a = 0; a <= p; ++a) {
+                            const int k = b * (p + 1) + a, A = (s2 - p + b) * n1 + (s1 - p + a);
+                            const double c = weights[A] / We;
+                            Rt[k] = c * (Rt[k] - Rv[k] * Wt / We);
+                            Rv[k] = c * Rv[k];
+                        }
                 Vec3 T{0, 0, 0};
                 for (int b = 0; b <= p; ++b)
                     for (int a = 0; a <= p; ++a) {
                         int A = (s2 - p + b) * n1 + (s1 - p + a);
-                        double dN = along1 ? b1[1][a] * b2[0][b] : b1[0][a] * b2[1][b];
-                        T = T + dN * Vec3{X[3 * A], X[3 * A + 1], X[3 * A + 2]};
+                        T = T + Rt[b * (p + 1) + a] * Vec3{X[3 * A], X[3 * A + 1], X[3 * A + 2]};
                     }
                 double ds = std::sqrt(dot(T, T)) * jac * gw[qq];
                 for (int b = 0; b <= p; ++b)
                     for (int a = 0; a <= p; ++a) {
                         int A = (s2 - p + b) * n1 + (s1 - p + a);
-                        double Nv = b1[0][a] * b2[0][b];
+                        double Nv = Rv[b * (p + 1) + a];
                         for (int c = 0; c < 3; ++c) F[(size_t)c * ncp + A] += Nv * L[1 + c] * ds;
                     }
             }

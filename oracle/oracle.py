@@ -55,11 +55,13 @@ def lib():
         L.klo_full_nnz.argtypes = [ctypes.c_int] * 3
         L.klo_full_pattern.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_void_p]
         L.klo_assemble.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_double] * 3 +
-                                   [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int])
+                                   [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_void_p])
         L.klo_mass.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_double] * 2 +
-                               [ctypes.c_int, ctypes.c_void_p])
+                               [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p])
         L.klo_force.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_int, ctypes.c_void_p,
-                                ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p])
+                                ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p])
         L.klo_basis.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
         _lib = L
     return _lib
@@ -86,6 +88,8 @@ class OracleAssembler:
         self._U1 = np.ascontiguousarray(P.knots1, dtype=np.float64)
         self._U2 = np.ascontiguousarray(P.knots2, dtype=np.float64)
         self._X = np.ascontiguousarray(P.ctrl, dtype=np.float64)
+        w = getattr(P, "weights", None)
+        self._W = None if w is None else np.ascontiguousarray(w, dtype=np.float64)   # NURBS weights
         L = lib()
         nnz = L.klo_full_nnz(P.p, P.n1, P.n2)
         self.rowptr = np.zeros(3 * P.ncp + 1, dtype=np.int64)
@@ -95,6 +99,9 @@ class OracleAssembler:
         self.nfree = len(self.free)
         self._F = None
 
+    def _wptr(self):
+        return _ptr(self._W) if self._W is not None else None
+
     # -- full-space pieces ---------------------------------------------------------------
     def full_tangent_and_fint(self, ufull: np.ndarray, want_K: bool = True):
         P = self.prob
@@ -102,7 +109,8 @@ class OracleAssembler:
         vals = np.zeros(len(self.cols)) if want_K else None
         fint = np.zeros(3 * P.ncp)
         rc = lib().klo_assemble(P.p, P.n1, P.n2, _ptr(self._U1), _ptr(self._U2), _ptr(self._X), P.E, P.nu, P.t,
-                                P.nq, _ptr(u), _ptr(vals) if want_K else None, _ptr(fint), self.nthreads)
+                                P.nq, _ptr(u), _ptr(vals) if want_K else None, _ptr(fint), self.nthreads,
+                                self._wptr())
         if rc != 0:
             raise RuntimeError("oracle assembly failed")
         K = None
@@ -117,13 +125,14 @@ class OracleAssembler:
         pl = np.ascontiguousarray(P.point_loads, dtype=np.float64).reshape(-1, 5)
         ed = np.ascontiguousarray(P.edge_loads, dtype=np.float64).reshape(-1, 4)
         lib().klo_force(P.p, P.n1, P.n2, _ptr(self._U1), _ptr(self._U2), _ptr(self._X), P.nq, _ptr(qs),
-                        len(pl), _ptr(pl), len(ed), _ptr(ed), _ptr(F))
+                        len(pl), _ptr(pl), len(ed), _ptr(ed), _ptr(F), self._wptr())
         return F
 
     def full_mass(self):
         P = self.prob
         vals = np.zeros(len(self.cols))
-        lib().klo_mass(P.p, P.n1, P.n2, _ptr(self._U1), _ptr(self._U2), _ptr(self._X), P.rho, P.t, P.nq, _ptr(vals))
+        lib().klo_mass(P.p, P.n1, P.n2, _ptr(self._U1), _ptr(self._U2), _ptr(self._X), P.rho, P.t, P.nq, _ptr(vals),
+                       self._wptr())
         return sp.csr_matrix((vals, self.cols, self.rowptr), shape=(3 * P.ncp, 3 * P.ncp))
 
     # -- free-dof (eliminated) versions, the objects the reference's callbacks return -----
