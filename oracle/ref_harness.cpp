@@ -1,8 +1,10 @@
 // CPU oracle built from the reference's OWN solver headers (test infrastructure only).
 //
 // gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl, gsALMConsistentCrisfield,
-// gsModalSolver and gsBucklingSolver are compiled unchanged from the reference tree
-// (src/gsStaticSolvers, src/gsALMSolvers, src/gsEigenSolvers) against the test-only stand-in of
+// gsModalSolver, gsBucklingSolver and the time integrators gsDynamicNewmark, gsDynamicBathe,
+// gsDynamicWilson, gsDynamicExplicitEuler and gsDynamicRK4 are compiled unchanged from the
+// reference tree (src/gsStaticSolvers, src/gsALMSolvers, src/gsEigenSolvers,
+// src/gsDynamicSolvers) against the test-only stand-in of
 // gismo's linear algebra and option list in oracle/refshim/.  The operators they call -- the
 // reference's Jacobian_t, Residual_t and ALResidual_t callbacks
 // (src/gsStructuralAnalysisTools/gsStructuralAnalysisTypes.h:58-93) -- are C function pointers
@@ -24,6 +26,11 @@
 #include <gsStructuralAnalysis/src/gsEigenSolvers/gsBucklingSolver.h>
 #include <gsStructuralAnalysis/src/gsEigenSolvers/gsModalSolver.h>
 #include <gsStructuralAnalysis/src/gsStaticSolvers/gsStaticNewton.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicBathe.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicExplicitEuler.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicNewmark.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicRK4.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicWilson.h>
 
 using namespace gismo;
 
@@ -34,6 +41,9 @@ typedef int (*refh_jac_fn)(const double* x, double* vals);
 typedef int (*refh_alres_fn)(const double* x, double lambda, double* R);
 // F - Fint(x)  (Residual_t)
 typedef int (*refh_res_fn)(const double* x, double* R);
+// time-dependent operators of the integrators: x may be null (mass, stiffness, force)
+typedef int (*refh_tmat_fn)(const double* x, double t, double* vals);
+typedef int (*refh_tvec_fn)(const double* x, double t, double* out);
 }
 
 namespace {
@@ -85,6 +95,8 @@ int guard(F&& f) {
         return f();
     } catch (const std::exception& e) {
         g_err = e.what();
+    } catch (int) {                 // the integrators throw 2 when an operator callback fails
+        g_err = "operator failed";
     } catch (...) {
         g_err = "unknown error";
     }
@@ -100,6 +112,58 @@ struct RefNewton {
     RefProblem* P;
     std::unique_ptr<gsStaticNewton<real_t>> N;
 };
+
+struct RefDyn {
+    index_t n = 0;
+    std::vector<int64_t> rowptr;
+    std::vector<int32_t> cols;
+    refh_tmat_fn mass = nullptr, damping = nullptr, jac = nullptr;
+    refh_tvec_fn vec = nullptr;
+    std::unique_ptr<gsDynamicBase<real_t>> D;
+
+    bool matrix(refh_tmat_fn f, const double* x, double t, gsSparseMatrix<real_t>& K) const {
+        std::vector<double> v(cols.size());
+        if (f(x, t, v.data()) != 0) return false;
+        K = gsSparseMatrix<real_t>(n, n);
+        for (index_t i = 0; i < n; ++i)
+            for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k) K(i, cols[k]) = v[k];
+        return true;
+    }
+    bool vector(const double* x, double t, gsVector<real_t>& r) const {
+        r = gsVector<real_t>(n);
+        return vec(x, t, r.data()) == 0;
+    }
+};
+
+// One integrator of the reference with the linear constructor (Mass_t, Damping_t, Stiffness_t,
+// TForce_t) or the nonlinear one (Mass_t, Damping_t, Jacobian_t, TResidual_t), as
+// gsDynamicBase.h:58-130 defines them.
+template <template <class, bool> class Integrator>
+gsDynamicBase<real_t>* make_dynamic(RefDyn* D, bool nonlinear) {
+    typename gsStructuralAnalysisOps<real_t>::Mass_t M = [D](gsSparseMatrix<real_t>& m) {
+        return D->matrix(D->mass, nullptr, 0.0, m);
+    };
+    typename gsStructuralAnalysisOps<real_t>::Damping_t C = [D](gsVector<real_t> const& x, gsSparseMatrix<real_t>& m) {
+        return D->matrix(D->damping, x.data(), 0.0, m);
+    };
+    if (!nonlinear) {
+        typename gsStructuralAnalysisOps<real_t>::Stiffness_t K = [D](gsSparseMatrix<real_t>& m) {
+            return D->matrix(D->jac, nullptr, 0.0, m);
+        };
+        typename gsStructuralAnalysisOps<real_t>::TForce_t F = [D](const real_t t, gsVector<real_t>& r) {
+            return D->vector(nullptr, t, r);
+        };
+        return new Integrator<real_t, false>(M, C, K, F);
+    }
+    typename gsStructuralAnalysisOps<real_t>::Jacobian_t J = [D](gsVector<real_t> const& x, gsSparseMatrix<real_t>& m) {
+        return D->matrix(D->jac, x.data(), 0.0, m);
+    };
+    typename gsStructuralAnalysisOps<real_t>::TResidual_t R = [D](gsVector<real_t> const& x, const real_t t,
+                                                                  gsVector<real_t>& r) {
+        return D->vector(x.data(), t, r);
+    };
+    return new Integrator<real_t, true>(M, C, J, R);
+}
 
 }  // namespace
 
@@ -288,6 +352,68 @@ int refh_eigen_dense(int kind, int n, const double* A, const double* B, const ch
         std::memcpy(values, v.data(), sizeof(double) * v.size());
         std::memcpy(vectors, V.data(), sizeof(double) * V.size());
         return (int)st;
+    });
+}
+
+// ---- time integrators (gsDynamicBase and its subclasses) -------------------------------------
+void* refh_dyn_create(int n, int64_t nnz, const int64_t* rowptr, const int32_t* cols, const char* method,
+                      int nonlinear, refh_tmat_fn mass, refh_tmat_fn damping, refh_tmat_fn jac, refh_tvec_fn vec,
+                      const char* options) {
+    RefDyn* out = nullptr;
+    int st = guard([&] {
+        std::unique_ptr<RefDyn> D(new RefDyn());
+        D->n = n;
+        D->rowptr.assign(rowptr, rowptr + n + 1);
+        D->cols.assign(cols, cols + nnz);
+        D->mass = mass;
+        D->damping = damping;
+        D->jac = jac;
+        D->vec = vec;
+        const std::string m(method);
+        const bool nl = nonlinear != 0;
+        if (m == "Newmark") D->D.reset(make_dynamic<gsDynamicNewmark>(D.get(), nl));
+        else if (m == "Bathe") D->D.reset(make_dynamic<gsDynamicBathe>(D.get(), nl));
+        else if (m == "Wilson") D->D.reset(make_dynamic<gsDynamicWilson>(D.get(), nl));
+        else if (m == "ExplicitEuler") D->D.reset(make_dynamic<gsDynamicExplicitEuler>(D.get(), nl));
+        else if (m == "RK4") D->D.reset(make_dynamic<gsDynamicRK4>(D.get(), nl));
+        else throw std::runtime_error("unknown integrator " + m);
+        gsOptionList o;
+        apply_options(o, options);
+        D->D->setOptions(o);
+        out = D.release();
+        return 0;
+    });
+    return st == 0 ? out : nullptr;
+}
+void refh_dyn_destroy(void* h) { delete static_cast<RefDyn*>(h); }
+int refh_dyn_set_state(void* h, const double* U, const double* V, const double* A) {
+    return guard([&] {
+        RefDyn* D = static_cast<RefDyn*>(h);
+        gsVector<real_t> u(D->n), v(D->n), a(D->n);
+        std::memcpy(u.data(), U, sizeof(double) * D->n);
+        std::memcpy(v.data(), V, sizeof(double) * D->n);
+        std::memcpy(a.data(), A, sizeof(double) * D->n);
+        D->D->setU(u);
+        D->D->setV(v);
+        D->D->setA(a);
+        return 0;
+    });
+}
+// one step of size dt; returns the gsStatus, or -1
+int refh_dyn_step(void* h, double dt) {
+    return guard([&] { return (int)static_cast<RefDyn*>(h)->D->step(dt); });
+}
+// U, V, A (n each), time and the iteration count of the last step
+int refh_dyn_state(void* h, double* U, double* V, double* A, double* info) {
+    return guard([&] {
+        gsDynamicBase<real_t>& D = *static_cast<RefDyn*>(h)->D;
+        const gsVector<real_t>&u = D.solutionU(), &v = D.solutionV(), &a = D.solutionA();
+        std::memcpy(U, u.data(), sizeof(double) * u.rows());
+        std::memcpy(V, v.data(), sizeof(double) * v.rows());
+        std::memcpy(A, a.data(), sizeof(double) * a.rows());
+        info[0] = D.time();
+        info[1] = D.numIterations();
+        return 0;
     });
 }
 

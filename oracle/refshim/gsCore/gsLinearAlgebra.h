@@ -78,11 +78,14 @@ using std::max;
 using std::floor;
 using std::ceil;
 template <class T> inline T sign(T v) { return (T(0) < v) - (v < T(0)); }
+template <class T> inline bool isinf(T v) { return std::isinf(v); }
+template <class T> inline bool isnan(T v) { return std::isnan(v); }
 }  // namespace math
 
 template <class T = real_t> class gsMatrix;
 template <class T = real_t> class gsVector;
 template <class T = real_t> class gsSparseMatrix;
+template <class T> struct gsRowBlock;
 
 // Reference to a matrix's coefficients as an array (m.array() += s, m.array().abs()).
 template <class T>
@@ -165,6 +168,10 @@ public:
     gsColwise<T> colwise() const { return gsColwise<T>{*this}; }
     gsArrayRef<T> array() { return gsArrayRef<T>{*this}; }
     gsMatrix toDense() const { return *this; }
+    gsSparseMatrix<T> sparseView() const;
+    // rows [0, n) / [rows - n, rows) as an assignable block (Eigen's topRows / bottomRows)
+    gsRowBlock<T> topRows(index_t n) { return gsRowBlock<T>{*this, 0, n}; }
+    gsRowBlock<T> bottomRows(index_t n) { return gsRowBlock<T>{*this, r - n, n}; }
     gsMatrix inverse() const;
 
     gsMatrix& operator+=(const gsMatrix& o) { check_same(o); for (size_t i = 0; i < d.size(); ++i) d[i] += o.d[i]; return *this; }
@@ -319,6 +326,39 @@ public:
     void makeCompressed() {}
 };
 
+template <class T>
+gsSparseMatrix<T> gsMatrix<T>::sparseView() const { return gsSparseMatrix<T>(*this); }
+
+template <class T>
+struct gsRowBlock {
+    gsMatrix<T>& m;
+    index_t r0, n;
+    gsMatrix<T> value() const {
+        gsMatrix<T> out(n, m.cols());
+        for (index_t j = 0; j < m.cols(); ++j)
+            for (index_t i = 0; i < n; ++i) out(i, j) = m(r0 + i, j);
+        return out;
+    }
+    operator gsMatrix<T>() const { return value(); }
+    friend gsMatrix<T> operator*(const T& s, const gsRowBlock& b) { return s * b.value(); }
+    friend gsMatrix<T> operator*(const gsRowBlock& b, const T& s) { return b.value() * s; }
+    friend gsMatrix<T> operator*(const gsMatrix<T>& a, const gsRowBlock& b) { return a * b.value(); }
+    friend gsMatrix<T> operator+(const gsRowBlock& a, const gsMatrix<T>& b) { return a.value() + b; }
+    friend gsMatrix<T> operator-(const gsRowBlock& a, const gsMatrix<T>& b) { return a.value() - b; }
+    gsRowBlock& operator=(const gsMatrix<T>& b) {
+        GISMO_ASSERT(b.rows() == n && b.cols() == m.cols(), "row block size");
+        for (index_t j = 0; j < m.cols(); ++j)
+            for (index_t i = 0; i < n; ++i) m(r0 + i, j) = b(i, j);
+        return *this;
+    }
+    gsRowBlock& operator+=(const gsMatrix<T>& b) {
+        GISMO_ASSERT(b.rows() == n && b.cols() == m.cols(), "row block size");
+        for (index_t j = 0; j < m.cols(); ++j)
+            for (index_t i = 0; i < n; ++i) m(r0 + i, j) += b(i, j);
+        return *this;
+    }
+};
+
 // ---- sparse solvers -------------------------------------------------------------------------
 template <class T>
 class gsSparseSolverBase {
@@ -333,7 +373,7 @@ protected:
     gsEigen::ComputationInfo m_info = gsEigen::Success;
 };
 
-template <class T>
+template <class T = real_t>
 struct gsSparseSolver {
     typedef gsSparseSolverBase<T> Base;
     typedef std::unique_ptr<Base> uPtr;
@@ -419,6 +459,8 @@ struct gsSparseSolver {
 
     class SparseLU : public Base {
     public:
+        SparseLU() {}
+        explicit SparseLU(const gsMatrix<T>& A) { compute(A); }
         void compute(const gsMatrix<T>& A) override {
             LU = A;
             this->m_info = lu_factor(LU, piv) ? gsEigen::Success : gsEigen::NumericalIssue;
@@ -428,11 +470,18 @@ struct gsSparseSolver {
             lu_solve(LU, piv, x.data());
             return x;
         }
+        // several right-hand sides (the columns of B), as Eigen's solve of a matrix
+        gsMatrix<T> solve(const gsSparseMatrix<T>& B) const {
+            gsMatrix<T> X(B);
+            for (index_t j = 0; j < X.cols(); ++j) lu_solve(LU, piv, &X(0, j));
+            return X;
+        }
 
     private:
         gsMatrix<T> LU;
         std::vector<index_t> piv;
     };
+    typedef SparseLU LU;
 
     // Eigen::ConjugateGradient with the DiagonalPreconditioner and its defaults: tolerance =
     // machine epsilon on ||r|| / ||b||, at most 2n iterations, start at zero.

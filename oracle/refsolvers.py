@@ -1,7 +1,8 @@
 """Bindings of oracle/_ref/libref_solvers.so -- the reference's own solver classes compiled from
 its unchanged headers (gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl,
-gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver) against the test-only stand-in in
-oracle/refshim/.  TEST INFRASTRUCTURE ONLY: the tests use it to pin the Python restatement
+gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver, and the time integrators
+gsDynamicNewmark, gsDynamicBathe, gsDynamicWilson, gsDynamicExplicitEuler, gsDynamicRK4)
+against the test-only stand-in in oracle/refshim/.  TEST INFRASTRUCTURE ONLY: the tests use it to pin the Python restatement
 (oracle.py) and to write golden fixtures; the product never imports it.
 
 The library exists only where the reference tree is present (``make -C oracle ref``);
@@ -25,6 +26,9 @@ _JAC = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.PO
 _ALRES = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_double,
                           ctypes.POINTER(ctypes.c_double))
 _RES = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
+_TMAT = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                         ctypes.POINTER(ctypes.c_double))
+_TVEC = _TMAT
 _vp = ctypes.c_void_p
 _lib = None
 
@@ -77,6 +81,13 @@ def lib():
         L.refh_newton_solution.argtypes = [_vp, _vp]
         L.refh_newton_iterations.argtypes = [_vp]
         L.refh_eigen_dense.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_char_p, ctypes.c_int, _vp, _vp]
+        L.refh_dyn_create.restype = _vp
+        L.refh_dyn_create.argtypes = [ctypes.c_int, ctypes.c_int64, _vp, _vp, ctypes.c_char_p, ctypes.c_int, _TMAT,
+                                      _TMAT, _TMAT, _TVEC, ctypes.c_char_p]
+        L.refh_dyn_destroy.argtypes = [_vp]
+        L.refh_dyn_set_state.argtypes = [_vp, _vp, _vp, _vp]
+        L.refh_dyn_step.argtypes = [_vp, ctypes.c_double]
+        L.refh_dyn_state.argtypes = [_vp, _vp, _vp, _vp, _vp]
         _lib = L
     return _lib
 
@@ -262,3 +273,75 @@ def eigen_dense(kind: str, A, B, options: dict | None = None, power: bool = Fals
     if st < 0:
         raise RuntimeError(_err())
     return st, vals, vecs
+
+
+class Dynamic:
+    """gsDynamicNewmark / gsDynamicBathe / gsDynamicWilson / gsDynamicExplicitEuler / gsDynamicRK4
+    of the reference (template flag _NL = ``nonlinear``), built with the linear constructor
+    (Mass_t, Damping_t, Stiffness_t, TForce_t) or the nonlinear one (Mass_t, Damping_t,
+    Jacobian_t, TResidual_t) of gsDynamicBase.h:58-130.  The callbacks have the signatures of
+    oracle/dynamics.py: mass(), damping(U, t), jacobian(U, t), residual(U, t) = Fext(t) - Fint(U),
+    force(t); the reference calls mass, damping and the stiffness without a time (they get 0)."""
+
+    def __init__(self, method, nonlinear, n, mass, damping, jacobian, residual=None, force=None, options=None):
+        self.n = n
+        self.rowptr = np.arange(0, n * n + 1, n, dtype=np.int64)
+        self.cols = np.tile(np.arange(n, dtype=np.int32), n)
+        self.failures = 0
+
+        def dense(K):
+            return K.toarray() if hasattr(K, "toarray") else np.asarray(K)
+
+        def wrap_mat(fn):
+            def f(x, t, vals):
+                try:
+                    U = None if not x else np.ctypeslib.as_array(x, shape=(n,)).copy()
+                    np.ctypeslib.as_array(vals, shape=(n * n,))[:] = dense(fn(U, t)).ravel()
+                    return 0
+                except Exception:
+                    self.failures += 1
+                    return 1
+            return _TMAT(f)
+
+        def vec(x, t, out):
+            try:
+                if x:
+                    r = residual(np.ctypeslib.as_array(x, shape=(n,)).copy(), t)
+                else:
+                    r = force(t)
+                np.ctypeslib.as_array(out, shape=(n,))[:] = r
+                return 0
+            except Exception:
+                self.failures += 1
+                return 1
+
+        self._cb = (wrap_mat(lambda U, t: mass()), wrap_mat(damping),
+                    wrap_mat(lambda U, t: jacobian(np.zeros(n) if U is None else U, t)), _TVEC(vec))
+        h = lib().refh_dyn_create(n, n * n, _p(self.rowptr), _p(self.cols), method.encode(), int(bool(nonlinear)),
+                                  *self._cb, option_spec(options or {}))
+        if not h:
+            raise RuntimeError(_err())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.refh_dyn_destroy(self.h)
+            self.h = None
+
+    def set_state(self, U, V, A):
+        U, V, A = (np.ascontiguousarray(v, dtype=np.float64) for v in (U, V, A))
+        if lib().refh_dyn_set_state(self.h, _p(U), _p(V), _p(A)) < 0:
+            raise RuntimeError(_err())
+
+    def step(self, dt) -> int:
+        st = lib().refh_dyn_step(self.h, float(dt))
+        if st < 0:
+            raise RuntimeError(_err())
+        return st
+
+    def state(self):
+        """(U, V, A, time, iterations of the last step)."""
+        U, V, A, info = np.zeros(self.n), np.zeros(self.n), np.zeros(self.n), np.zeros(2)
+        if lib().refh_dyn_state(self.h, _p(U), _p(V), _p(A), _p(info)) < 0:
+            raise RuntimeError(_err())
+        return U, V, A, float(info[0]), int(info[1])
