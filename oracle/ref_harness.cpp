@@ -2,8 +2,8 @@
 //
 // gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl, gsALMConsistentCrisfield,
 // gsModalSolver, gsBucklingSolver and the time integrators gsDynamicNewmark, gsDynamicBathe,
-// gsDynamicWilson, gsDynamicExplicitEuler and gsDynamicRK4 are compiled unchanged from the
-// reference tree (src/gsStaticSolvers, src/gsALMSolvers, src/gsEigenSolvers,
+// gsDynamicWilson, gsDynamicExplicitEuler, gsDynamicImplicitEuler and gsDynamicRK4 are compiled
+// unchanged from the reference tree (src/gsStaticSolvers, src/gsALMSolvers, src/gsEigenSolvers,
 // src/gsDynamicSolvers) against the test-only stand-in of
 // gismo's linear algebra and option list in oracle/refshim/.  The operators they call -- the
 // reference's Jacobian_t, Residual_t and ALResidual_t callbacks
@@ -28,6 +28,7 @@
 #include <gsStructuralAnalysis/src/gsStaticSolvers/gsStaticNewton.h>
 #include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicBathe.h>
 #include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicExplicitEuler.h>
+#include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicImplicitEuler.h>
 #include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicNewmark.h>
 #include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicRK4.h>
 #include <gsStructuralAnalysis/src/gsDynamicSolvers/gsDynamicWilson.h>
@@ -375,6 +376,7 @@ void* refh_dyn_create(int n, int64_t nnz, const int64_t* rowptr, const int32_t* 
         else if (m == "Bathe") D->D.reset(make_dynamic<gsDynamicBathe>(D.get(), nl));
         else if (m == "Wilson") D->D.reset(make_dynamic<gsDynamicWilson>(D.get(), nl));
         else if (m == "ExplicitEuler") D->D.reset(make_dynamic<gsDynamicExplicitEuler>(D.get(), nl));
+        else if (m == "ImplicitEuler") D->D.reset(make_dynamic<gsDynamicImplicitEuler>(D.get(), nl));
         else if (m == "RK4") D->D.reset(make_dynamic<gsDynamicRK4>(D.get(), nl));
         else throw std::runtime_error("unknown integrator " + m);
         gsOptionList o;

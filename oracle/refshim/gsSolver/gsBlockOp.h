@@ -1,0 +1,3 @@
+// Test-only stand-in: see gsLinearOperator.h.
+#pragma once
+#include <gsSolver/gsLinearOperator.h>

@@ -1,7 +1,8 @@
 """Bindings of oracle/_ref/libref_solvers.so -- the reference's own solver classes compiled from
 its unchanged headers (gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl,
 gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver, and the time integrators
-gsDynamicNewmark, gsDynamicBathe, gsDynamicWilson, gsDynamicExplicitEuler, gsDynamicRK4)
+gsDynamicNewmark, gsDynamicBathe, gsDynamicWilson, gsDynamicExplicitEuler,
+gsDynamicImplicitEuler, gsDynamicRK4)
 against the test-only stand-in in oracle/refshim/.  TEST INFRASTRUCTURE ONLY: the tests use it to pin the Python restatement
 (oracle.py) and to write golden fixtures; the product never imports it.
 
@@ -276,8 +277,8 @@ def eigen_dense(kind: str, A, B, options: dict | None = None, power: bool = Fals
 
 
 class Dynamic:
-    """gsDynamicNewmark / gsDynamicBathe / gsDynamicWilson / gsDynamicExplicitEuler / gsDynamicRK4
-    of the reference (template flag _NL = ``nonlinear``), built with the linear constructor
+    """gsDynamicNewmark / gsDynamicBathe / gsDynamicWilson / gsDynamicExplicitEuler /
+    gsDynamicImplicitEuler / gsDynamicRK4 of the reference (template flag _NL = ``nonlinear``), built with the linear constructor
     (Mass_t, Damping_t, Stiffness_t, TForce_t) or the nonlinear one (Mass_t, Damping_t,
     Jacobian_t, TResidual_t) of gsDynamicBase.h:58-130.  The callbacks have the signatures of
     oracle/dynamics.py: mass(), damping(U, t), jacobian(U, t), residual(U, t) = Fext(t) - Fint(U),

@@ -1,12 +1,10 @@
 """The oracle's restatement (oracle/oracle.py) pinned against the reference's OWN solver code.
 
 oracle/_ref/libref_solvers.so is gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl,
-gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver and the time integrators
-gsDynamicNewmark, gsDynamicBathe, gsDynamicWilson, gsDynamicExplicitEuler and gsDynamicRK4
-compiled unchanged from the reference tree against the test-only linear-algebra stand-in
-(oracle/refshim/).  gsDynamicImplicitEuler is not compiled: its block GMRES needs the
-preconditioner and block-operator classes, which the stand-in does not restate; its
-restatement is pinned by the closed-form tests of the integrators instead.  Both sides get
+gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver and the six time integrators of
+gsDynamicSolvers compiled unchanged from the reference tree against the test-only
+linear-algebra stand-in (oracle/refshim/; its GMRES, used by gsDynamicImplicitEuler, solves the
+block operator exactly).  Both sides get
 the same FP64 KL-shell operators (oracle.OracleAssembler), so every difference would be a
 difference of solver logic.  The reference tree exists only where the library can be built;
 elsewhere these tests skip (the golden fixtures written from it, tests/golden/ref_solvers.npz,
@@ -211,7 +209,7 @@ def test_dense_eigen_compute_and_power_match_reference(oracle_mod):
     assert abs(val[0] - w[0]) <= 1e-8 * w[0]
 
 
-DYN_METHODS = ["Newmark", "Bathe", "Wilson", "ExplicitEuler", "RK4"]
+DYN_METHODS = ["Newmark", "Bathe", "Wilson", "ExplicitEuler", "ImplicitEuler", "RK4"]
 
 
 def _dyn_pair(callbacks, n, method, nonlinear, opts):
@@ -254,14 +252,14 @@ def test_integrator_matches_reference_on_spring_mass(method, nonlinear):
 @pytest.mark.parametrize("nonlinear", [False, True])
 @pytest.mark.parametrize("method", DYN_METHODS)
 def test_integrator_matches_reference_on_shell(oracle_mod, method, nonlinear):
-    """The cylindrical panel with Rayleigh damping under a load ramped in from zero (the KL-shell
+    """The cylindrical panel with Rayleigh damping under a load ramped from 0.2 to 1 (the KL-shell
     operators of the FP64 oracle, the same on both sides): 4 steps of each integrator, the
     restatement against the reference.  Explicit integrators take a step below their stability
     limit and mass-proportional damping only."""
     import dynamics as D
     A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=4, p=2, load=400.0))
     explicit = method in ("ExplicitEuler", "RK4")
-    cb = D.shell_callbacks(A, nonlinear, 0.5, 0.0 if explicit else 1e-4, D.load_table([0.0, 2e-3], [0.0, 1.0]))
+    cb = D.shell_callbacks(A, nonlinear, 0.5, 0.0 if explicit else 1e-4, D.load_table([0.0, 2e-3], [0.2, 1.0]))
     n = len(A.force())
     ora, ref = _dyn_pair(cb, n, method, nonlinear, {"TolF": 1e-10, "TolU": 1e-10})
     z = np.zeros(n)
