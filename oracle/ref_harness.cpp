@@ -1,6 +1,7 @@
 // CPU oracle built from the reference's OWN solver headers (test infrastructure only).
 //
 // gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl, gsALMConsistentCrisfield,
+// gsAPALM (the build without MPI: serialSolve, the one-process parallelSolve and solve),
 // gsModalSolver, gsBucklingSolver and the time integrators gsDynamicNewmark, gsDynamicBathe,
 // gsDynamicWilson, gsDynamicExplicitEuler, gsDynamicImplicitEuler and gsDynamicRK4 are compiled
 // unchanged from the reference tree (src/gsStaticSolvers, src/gsALMSolvers, src/gsEigenSolvers,
@@ -20,6 +21,10 @@
 #include <vector>
 
 #include <gsStructuralAnalysis/src/gsALMSolvers/gsALMConsistentCrisfield.h>
+// gsAPALMDataContainer.h names gsAPALMData without including it (gismo's module header
+// includes both); the data header comes first here for the same reason
+#include <gsStructuralAnalysis/src/gsALMSolvers/gsAPALMData.h>
+#include <gsStructuralAnalysis/src/gsALMSolvers/gsAPALM.h>
 #include <gsStructuralAnalysis/src/gsALMSolvers/gsALMCrisfield.h>
 #include <gsStructuralAnalysis/src/gsALMSolvers/gsALMLoadControl.h>
 #include <gsStructuralAnalysis/src/gsALMSolvers/gsALMRiks.h>
@@ -112,6 +117,17 @@ struct RefALM {
 struct RefNewton {
     RefProblem* P;
     std::unique_ptr<gsStaticNewton<real_t>> N;
+};
+
+// gsAPALM with read access to its flat solutions per branch (protected members)
+struct HarnessAPALM : public gsAPALM<real_t> {
+    HarnessAPALM(gsALMBase<real_t>* alm, const gsAPALMData<real_t, solution_t>& data) : gsAPALM<real_t>(alm, data) {}
+    size_t branches() const { return m_solutions.size(); }
+};
+
+struct RefAPALM {
+    RefALM* A;
+    std::unique_ptr<HarnessAPALM> P;
 };
 
 struct RefDyn {
@@ -353,6 +369,71 @@ int refh_eigen_dense(int kind, int n, const double* A, const double* B, const ch
         std::memcpy(values, v.data(), sizeof(double) * v.size());
         std::memcpy(vectors, V.data(), sizeof(double) * V.size());
         return (int)st;
+    });
+}
+
+// ---- gsAPALM over one of the arc-length methods above ------------------------------------------
+// options: gsAPALM's (SubIntervals, MaxIt, ...); data_options: gsAPALMData's (MaxLevel,
+// Tolerance), set on the empty data object the constructor takes
+void* refh_apalm_create(void* alm, const char* options, const char* data_options) {
+    RefAPALM* out = nullptr;
+    int st = guard([&] {
+        RefALM* A = static_cast<RefALM*>(alm);
+        gsAPALMData<real_t, HarnessAPALM::solution_t> data;
+        gsOptionList dopt;
+        apply_options(dopt, data_options);
+        data.options().update(dopt, gsOptionList::addIfUnknown);
+        std::unique_ptr<HarnessAPALM> P(new HarnessAPALM(A->alm.get(), data));
+        gsOptionList o;
+        apply_options(o, options);
+        P->options().update(o, gsOptionList::addIfUnknown);
+        out = new RefAPALM{A, std::move(P)};
+        return 0;
+    });
+    return st == 0 ? out : nullptr;
+}
+void refh_apalm_destroy(void* h) { delete static_cast<RefAPALM*>(h); }
+int refh_apalm_initialize(void* h) {
+    return guard([&] {
+        static_cast<RefAPALM*>(h)->P->initialize();
+        return 0;
+    });
+}
+int refh_apalm_serial_solve(void* h, int nsteps) {
+    return guard([&] {
+        static_cast<RefAPALM*>(h)->P->serialSolve(nsteps);
+        return 0;
+    });
+}
+int refh_apalm_parallel_solve(void* h) {
+    return guard([&] {
+        static_cast<RefAPALM*>(h)->P->parallelSolve();
+        return 0;
+    });
+}
+int refh_apalm_solve(void* h, int nsteps) {
+    return guard([&] {
+        static_cast<RefAPALM*>(h)->P->solve(nsteps);
+        return 0;
+    });
+}
+int refh_apalm_branches(void* h) {
+    return guard([&] { return (int)static_cast<RefAPALM*>(h)->P->branches(); });
+}
+// number of flat points of a branch (getFlatSolutions / getFlatTimes / getFlatLevels)
+int refh_apalm_points(void* h, int branch) {
+    return guard([&] { return (int)static_cast<RefAPALM*>(h)->P->getFlatTimes(branch).size(); });
+}
+int refh_apalm_point(void* h, int branch, int k, double* U, double* L, double* time, int* level) {
+    return guard([&] {
+        HarnessAPALM& P = *static_cast<RefAPALM*>(h)->P;
+        const std::vector<HarnessAPALM::solution_t> sols = P.getFlatSolutions(branch);   // returned by value
+        const auto& s = sols.at(k);
+        std::memcpy(U, s.first.data(), sizeof(double) * s.first.rows());
+        *L = s.second;
+        *time = P.getFlatTimes(branch).at(k);
+        *level = (int)P.getFlatLevels(branch).at(k);
+        return 0;
     });
 }
 

@@ -21,7 +21,9 @@
 #include <functional>
 #include <iostream>
 #include <limits>
+#include <map>
 #include <memory>
+#include <numeric>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -55,7 +57,10 @@ inline std::ostream& info() {
 #define gsDebugVar(x) ((void)0)
 #define GISMO_STRINGIFY_(x) #x
 #define GISMO_HPP_HEADER(x) GISMO_STRINGIFY_(x)
-#define GISMO_ERROR(msg) throw std::runtime_error(msg)
+#define GISMO_ERROR(msg)                                                   \
+    do {                                                                   \
+        std::ostringstream gs_os_; gs_os_ << msg; throw std::runtime_error(gs_os_.str()); \
+    } while (0)
 #define GISMO_ASSERT(cond, msg) \
     do {                         \
         if (!(cond)) {           \

@@ -21,6 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_ref", "libref_solvers.so")
+APALM_DATA_DRIVER = os.path.join(HERE, "_ref", "ref_apalm_data")   # gsAPALMData on a scripted job run
 REF_TREE = os.environ.get("KLSA_REFERENCE_TREE", "/root/reference")
 
 _JAC = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
@@ -82,6 +83,16 @@ def lib():
         L.refh_newton_solution.argtypes = [_vp, _vp]
         L.refh_newton_iterations.argtypes = [_vp]
         L.refh_eigen_dense.argtypes = [ctypes.c_int, ctypes.c_int, _vp, _vp, ctypes.c_char_p, ctypes.c_int, _vp, _vp]
+        L.refh_apalm_create.restype = _vp
+        L.refh_apalm_create.argtypes = [_vp, ctypes.c_char_p, ctypes.c_char_p]
+        L.refh_apalm_destroy.argtypes = [_vp]
+        L.refh_apalm_initialize.argtypes = [_vp]
+        L.refh_apalm_serial_solve.argtypes = [_vp, ctypes.c_int]
+        L.refh_apalm_parallel_solve.argtypes = [_vp]
+        L.refh_apalm_solve.argtypes = [_vp, ctypes.c_int]
+        L.refh_apalm_branches.argtypes = [_vp]
+        L.refh_apalm_points.argtypes = [_vp, ctypes.c_int]
+        L.refh_apalm_point.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
         L.refh_dyn_create.restype = _vp
         L.refh_dyn_create.argtypes = [ctypes.c_int, ctypes.c_int64, _vp, _vp, ctypes.c_char_p, ctypes.c_int, _TMAT,
                                       _TMAT, _TMAT, _TVEC, ctypes.c_char_p]
@@ -274,6 +285,57 @@ def eigen_dense(kind: str, A, B, options: dict | None = None, power: bool = Fals
     if st < 0:
         raise RuntimeError(_err())
     return st, vals, vecs
+
+
+class APALM:
+    """gsAPALM of the reference over an ``ALM`` (built without MPI: serialSolve, the one-process
+    parallelSolve, and solve).  ``options`` are gsAPALM's (SubIntervals, MaxIt, ...),
+    ``data_options`` gsAPALMData's (MaxLevel, Tolerance)."""
+
+    def __init__(self, alm: ALM, options: dict, data_options: dict):
+        self.alm = alm
+        h = lib().refh_apalm_create(alm.h, option_spec(options), option_spec(data_options))
+        if not h:
+            raise RuntimeError(_err())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.refh_apalm_destroy(self.h)
+            self.h = None
+
+    def _call(self, rc):
+        if rc < 0:
+            raise RuntimeError(_err())
+        return rc
+
+    def initialize(self):
+        self._call(lib().refh_apalm_initialize(self.h))
+
+    def serial_solve(self, nsteps):
+        self._call(lib().refh_apalm_serial_solve(self.h, int(nsteps)))
+
+    def parallel_solve(self):
+        self._call(lib().refh_apalm_parallel_solve(self.h))
+
+    def solve(self, nsteps):
+        self._call(lib().refh_apalm_solve(self.h, int(nsteps)))
+
+    def branches(self) -> int:
+        return self._call(lib().refh_apalm_branches(self.h))
+
+    def flat(self, branch=0):
+        """(U per point, L per point, times, levels) of getFlatSolutions / Times / Levels."""
+        n = self._call(lib().refh_apalm_points(self.h, int(branch)))
+        Us, Ls, ts, lvs = [], [], [], []
+        for k in range(n):
+            U, L, t, lv = np.zeros(self.alm.ops.n), np.zeros(1), np.zeros(1), np.zeros(1, dtype=np.int32)
+            self._call(lib().refh_apalm_point(self.h, int(branch), k, _p(U), _p(L), _p(t), _p(lv)))
+            Us.append(U)
+            Ls.append(float(L[0]))
+            ts.append(float(t[0]))
+            lvs.append(int(lv[0]))
+        return Us, Ls, ts, lvs
 
 
 class Dynamic:

@@ -1,7 +1,9 @@
 """The native gsAPALMData restatement (klsa::APALMData in csrc/apalm.cpp, host code of the built
-library) against the oracle's independent Python restatement (oracle/apalm.py), driven by the
-same scripted jobs: every popped job (interval length, start, previous and reference points,
-level) and the final flat solutions (curve times, points, levels) agree."""
+library) against the oracle's independent Python restatement (oracle/apalm.py), and the oracle
+against the reference's own gsAPALMData compiled unchanged (oracle/ref_apalm_data.cpp, built
+where the reference tree exists), all driven by the same scripted jobs: every popped job
+(interval length, start, previous and reference points, level) and the final flat solutions
+(curve times, points, levels) agree."""
 import os
 import shutil
 import subprocess
@@ -53,6 +55,23 @@ def _oracle_lines():
     return out
 
 
+def _compare(lines, expected):
+    assert len(lines) == len(expected) and len(lines) > 15
+    for a, b in zip(lines, expected):
+        assert a[0] == b[0] and len(a) == len(b), (a, b)
+        for x, y in zip(a[1:], b[1:]):
+            assert float(x) == pytest.approx(float(y), rel=1e-13, abs=1e-15), (a, b)
+
+
+def test_oracle_apalm_data_matches_reference():
+    RS = pytest.importorskip("refsolvers")
+    if not RS.available() or not os.path.exists(RS.APALM_DATA_DRIVER):
+        pytest.skip("reference tree not present: gsAPALMData not built")
+    r = subprocess.run([RS.APALM_DATA_DRIVER], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    _compare([ln.split() for ln in r.stdout.strip().splitlines()], _oracle_lines())
+
+
 def test_native_apalm_data_matches_oracle(lib, tmp_path):
     gxx = shutil.which("g++")
     if gxx is None:
@@ -69,10 +88,4 @@ def test_native_apalm_data_matches_oracle(lib, tmp_path):
     env["LD_LIBRARY_PATH"] = "/usr/local/cuda/lib64" + (":" + env["LD_LIBRARY_PATH"] if env.get("LD_LIBRARY_PATH") else "")
     r = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode == 0, r.stderr
-    native = [ln.split() for ln in r.stdout.strip().splitlines()]
-    expected = _oracle_lines()
-    assert len(native) == len(expected) and len(native) > 15
-    for a, b in zip(native, expected):
-        assert a[0] == b[0]
-        for x, y in zip(a[1:], b[1:]):
-            assert float(x) == pytest.approx(float(y), rel=1e-13, abs=1e-15), (a, b)
+    _compare([ln.split() for ln in r.stdout.strip().splitlines()], _oracle_lines())

@@ -273,3 +273,78 @@ def test_integrator_matches_reference_on_shell(oracle_mod, method, nonlinear):
         if not explicit:            # the explicit integrators carry A unchanged
             assert _close(ora.A, A_, 1e-9), k
     assert np.abs(U).max() > 0      # the ramped load has moved the shell
+
+
+try:
+    import pytest_timeout  # noqa: F401
+    # gsAPALM::_initiation retries a failed step with `while (diverged)` and no bound, so a
+    # mistake in the harness would hang the run: end it instead
+    _bounded = pytest.mark.timeout(300, method="thread")
+except ImportError:
+    def _bounded(f):
+        return f
+
+
+def _apalm_pair(oracle_mod, oa, method, alm_opts, ap_opts, data_opts):
+    """The reference's APALM and the restatement's over the same arc-length method, each ALM
+    initialised before the APALM is built, as the reference's APALM drivers do
+    (examples/snapping_example_shell_APALM.cpp:488-537)."""
+    import apalm as AP
+    ref_alm = RS.ALM(RS.Operators.from_assembler(oa), method, alm_opts)
+    ref_alm.initialize()
+    ref = RS.APALM(ref_alm, ap_opts, data_opts)
+    cls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks}[method]
+    ora_alm = cls(oa.jacobian, oa.al_residual, oa.force(), alm_opts)
+    ora_alm.initialize()
+    ora = AP.APALM(ora_alm, dict(ap_opts, **data_opts))
+    return ref, ora
+
+
+def _same_flat_path(ref, ora):
+    assert ref.branches() == len(ora.times) == 1
+    Us, Ls, ts, lvs = ref.flat(0)
+    assert len(ts) == len(ora.times[0]) > 8
+    assert lvs == list(ora.levels[0])
+    np.testing.assert_allclose(ora.times[0], ts, rtol=1e-12, atol=1e-15)
+    for U, L, (Uo, Lo) in zip(Us, Ls, ora.solutions[0]):
+        assert abs(Lo - L) <= 1e-12 * max(abs(L), 1.0)
+        assert _rel(Uo, U) < 1e-12 or np.abs(U).max() == np.abs(Uo).max() == 0
+
+
+@_bounded
+@pytest.mark.parametrize("schedule", ["serial_then_parallel", "solve"])
+def test_apalm_matches_reference(oracle_mod, schedule):
+    """gsAPALM (the build without MPI) over gsALMCrisfield: the coarse serial path, then the
+    interval corrections of two refinement levels with two sub-intervals each -- either
+    serialSolve + parallelSolve, or the interleaved solve() -- give the restatement's flat path:
+    the same points in the same order, the same levels, the same curve times."""
+    oa = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=2, load=1.0))
+    alm_opts = dict(ALM_BASE, Length=0.02)
+    ref, ora = _apalm_pair(oracle_mod, oa, "Crisfield", alm_opts, dict(SubIntervals=2, MaxIt=40),
+                           dict(MaxLevel=2, Tolerance=1e-3))
+    ref.initialize()
+    ora.initialize()
+    if schedule == "solve":
+        ref.solve(5)
+        ora.solve(5)
+    else:
+        ref.serial_solve(5)
+        ora.serial_solve(5)
+        ref.parallel_solve()
+        ora.parallel_solve()
+    _same_flat_path(ref, ora)
+
+
+@_bounded
+def test_apalm_over_riks_matches_reference(oracle_mod):
+    """gsAPALM over gsALMRiks, whose interval distances are measured in Riks's norm: three
+    sub-intervals, one refinement level."""
+    oa = oracle_mod.OracleAssembler(P.cylindrical_panel(m=5, p=2, load=1e5))
+    alm_opts = dict(TolF=1e-8, TolU=1e-6, MaxIter=30, BifurcationMethod=-1, Length=0.003)
+    ref, ora = _apalm_pair(oracle_mod, oa, "Riks", alm_opts, dict(SubIntervals=3, MaxIt=20),
+                           dict(MaxLevel=1, Tolerance=1e-4))
+    ref.initialize()
+    ora.initialize()
+    ref.solve(4)
+    ora.solve(4)
+    _same_flat_path(ref, ora)
