@@ -927,7 +927,7 @@ PCG_METRIC = "linear solves/s on shell tangents: preconditioned CG (Jacobi, noda
 
 
 def run_pcg(args):
-    """The solves the benchmark spec names for the Newton and Lanczos inner systems, measured on the
+    """The preconditioned-CG alternatives for the Newton and Lanczos inner systems, measured on the
     tangents of the ramp roof (degree 3, 64x64, K at zero and at the 10%-load solution) and of the
     headline roof (degree 2, 128x128, K at zero): CG to a relative residual of 1e-8 with the
     Jacobi (CGDiagonal) and nodal 3x3 block-Jacobi (GPUPCG) preconditioners, against the
