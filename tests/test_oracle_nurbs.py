@@ -7,7 +7,11 @@ quotient rule for first and second derivatives) is pinned by
   internal force (partition of unity through the quotient rule);
 * the Scordelis-Lo roof on an exact NURBS cylinder (R 25, L 50, 40 degree half-angle, E 4.32e8,
   nu 0, t 0.25, self-weight 90 per unit area, rigid diaphragms at the ends), whose free-edge
-  midpoint deflection converges to the published Kirchhoff-Love value 0.3006.
+  midpoint deflection converges to the published Kirchhoff-Love value 0.3006;
+* the pinched hemisphere of the reference's own problem file (filedata/pde/
+  kirchhoff_shell_hemisphere.xml, test case 3 of examples/gsThinShell_Static_XML.cpp) on an exact
+  NURBS quarter sphere with a collapsed pole, whose load-point displacement converges to the
+  published value 0.0924.
 The device problem does not take rational patches yet and says so.
 """
 import math
@@ -15,6 +19,7 @@ import os
 
 import numpy as np
 import pytest
+import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from gsstructuralanalysis_gb300 import problems as P, xmlio
@@ -143,6 +148,88 @@ def test_scordelis_lo_roof_matches_the_published_kirchhoff_love_value(tmp_path, 
         vals.append(u[2 * n1 * n2:].reshape(n2, n1)[0] @ N1)   # free edge xi2 = 0, weights 1 along it
     assert abs(vals[-1] + 0.3006) <= 0.003 * 0.3006
     assert abs(vals[-1] - vals[-2]) <= 0.005 * abs(vals[-1])
+
+
+def _quarter_hemisphere_xml(path, R=10.0):
+    """The closed quarter hemisphere as a TensorNurbs2 surface of revolution: direction 0 the
+    azimuth (0 to 90 degrees), direction 1 the latitude (equator to the pole, where the net
+    collapses to one point); both quarter circles rational quadratics with the middle weight
+    cos(45 degrees), the weights of the net their products."""
+    c = math.cos(math.pi / 4)
+    quarter = [(1.0, 0.0, 1.0), (1.0, 1.0, c), (0.0, 1.0, 1.0)]
+    coefs, w = [], []
+    for r, z, wj in quarter:                 # latitude profile (radius, height)
+        for ax, ay, wi in quarter:           # azimuth
+            coefs.append(f"{R * r * ax!r} {R * r * ay!r} {R * z!r}")
+            w.append(wi * wj)
+    with open(path, "w") as f:
+        f.write(f"""<?xml version="1.0" encoding="UTF-8"?>
+<xml>
+ <Geometry type="TensorNurbs2" id="0">
+  <Basis type="TensorNurbsBasis2">
+   <Basis type="TensorBSplineBasis2">
+    <Basis type="BSplineBasis" index="0"><KnotVector degree="2">0 0 0 1 1 1</KnotVector></Basis>
+    <Basis type="BSplineBasis" index="1"><KnotVector degree="2">0 0 0 1 1 1</KnotVector></Basis>
+   </Basis>
+   <weights>{' '.join(repr(v) for v in w)}</weights>
+  </Basis>
+  <coefs geoDim="3">{' '.join(coefs)}</coefs>
+ </Geometry>
+</xml>""")
+
+
+def _pinched_hemisphere(oracle_mod, path, elevate, refine):
+    """Linear solve of the pinched hemisphere with the conditions of
+    filedata/pde/kirchhoff_shell_hemisphere.xml: t 0.04, E 6.825e7, nu 0.3; unit point loads
+    +x at (0, 0) and -y at (1, 0); the pole (side 4) fixed; on the symmetry plane y = 0 (side 1)
+    u_y = 0 and the x and z components clamped, on x = 0 (side 2) u_x = 0 and y, z clamped.
+    "Clamped" on a component whose boundary row is free ties the second row of control points to
+    the boundary row (zero slope across the side); the ties and the fixed dofs enter as
+    u = T q, solved as T^T K T q = T^T F on the oracle's full K and F.
+    Returns the outward displacement at the +x load and the inward one at the -y load."""
+    p, U1, U2, ctrl, w = xmlio.read_geometry(path, elevate, refine, with_weights=True)
+    n1, n2 = len(U1) - p - 1, len(U2) - p - 1
+    ncp = n1 * n2
+    prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=ctrl, E=6.825e7, nu=0.3, t=0.04, rho=1.0,
+                          fixed=np.zeros(3 * ncp, dtype=bool), surface_load=np.zeros(3),
+                          point_loads=np.array([[0.0, 0.0, 1.0, 0.0, 0.0], [1.0, 0.0, 0.0, -1.0, 0.0]]), weights=w)
+    oa = oracle_mod.OracleAssembler(prob)
+    K, _ = oa.full_tangent_and_fint(np.zeros(3 * ncp))
+    F = oa.full_force()
+
+    def dof(c, i, j):
+        return c * ncp + j * n1 + i
+
+    master = np.arange(3 * ncp)              # the dof each dof equals; -1: fixed at zero
+    for j in range(n2):
+        master[dof(1, 0, j)] = -1
+        master[dof(0, 1, j)], master[dof(2, 1, j)] = dof(0, 0, j), dof(2, 0, j)
+        master[dof(0, n1 - 1, j)] = -1
+        master[dof(1, n1 - 2, j)], master[dof(2, n1 - 2, j)] = dof(1, n1 - 1, j), dof(2, n1 - 1, j)
+    for i in range(n1):
+        for c in range(3):
+            master[dof(c, i, n2 - 1)] = -1
+    tied = master >= 0
+    master[tied & (master[np.maximum(master, 0)] < 0)] = -1      # tied to a fixed dof: fixed
+    keep = np.unique(master[master >= 0])
+    col = np.full(3 * ncp, -1)
+    col[keep] = np.arange(len(keep))
+    rows = np.nonzero(master >= 0)[0]
+    T = sp.csr_matrix((np.ones(len(rows)), (rows, col[master[rows]])), shape=(3 * ncp, len(keep)))
+    u = T @ spla.spsolve((T.T @ K @ T).tocsc(), T.T @ F)
+    return u[dof(0, 0, 0)], -u[dof(1, n1 - 1, 0)]
+
+
+def test_pinched_hemisphere_matches_the_published_kirchhoff_love_value(tmp_path, oracle_mod):
+    path = os.path.join(tmp_path, "quarter_hemisphere.xml")
+    _quarter_hemisphere_xml(path)
+    vals = []
+    for refine in (4, 5):                    # degree 4, 16 x 16 and 32 x 32 elements
+        a, b = _pinched_hemisphere(oracle_mod, path, 2, refine)
+        assert abs(a - b) <= 1e-8 * a        # the two loads see the same displacement
+        vals.append(a)
+    assert abs(vals[-1] - 0.0924) <= 0.002 * 0.0924
+    assert abs(vals[-1] - vals[-2]) <= 0.001 * vals[-1]
 
 
 def test_device_problem_refuses_rational_patches(lib):
