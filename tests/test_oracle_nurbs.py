@@ -8,10 +8,11 @@ quotient rule for first and second derivatives) is pinned by
 * the Scordelis-Lo roof on an exact NURBS cylinder (R 25, L 50, 40 degree half-angle, E 4.32e8,
   nu 0, t 0.25, self-weight 90 per unit area, rigid diaphragms at the ends), whose free-edge
   midpoint deflection converges to the published Kirchhoff-Love value 0.3006;
-* the pinched hemisphere of the reference's own problem file (filedata/pde/
-  kirchhoff_shell_hemisphere.xml, test case 3 of examples/gsThinShell_Static_XML.cpp) on an exact
-  NURBS quarter sphere with a collapsed pole, whose load-point displacement converges to the
-  published value 0.0924.
+* the pinched hemisphere and the pinched cylinder of the reference's own problem files
+  (filedata/pde/kirchhoff_shell_hemisphere.xml and kirchhoff_shell_pinchedCylinder.xml, test
+  cases 3 and 4 of examples/gsThinShell_Static_XML.cpp) on exact NURBS geometry with the files'
+  symmetry conditions, whose load-point displacements converge to the published 0.0924 and
+  1.8248e-5.
 The device problem does not take rational patches yet and says so.
 """
 import math
@@ -178,21 +179,30 @@ def _quarter_hemisphere_xml(path, R=10.0):
 </xml>""")
 
 
-def _pinched_hemisphere(oracle_mod, path, elevate, refine):
-    """Linear solve of the pinched hemisphere with the conditions of
-    filedata/pde/kirchhoff_shell_hemisphere.xml: t 0.04, E 6.825e7, nu 0.3; unit point loads
-    +x at (0, 0) and -y at (1, 0); the pole (side 4) fixed; on the symmetry plane y = 0 (side 1)
-    u_y = 0 and the x and z components clamped, on x = 0 (side 2) u_x = 0 and y, z clamped.
-    "Clamped" on a component whose boundary row is free ties the second row of control points to
-    the boundary row (zero slope across the side); the ties and the fixed dofs enter as
-    u = T q, solved as T^T K T q = T^T F on the oracle's full K and F.
-    Returns the outward displacement at the +x load and the inward one at the -y load."""
+def _side_row(side, k, n1, n2):
+    """(i, j) of the control points in row k (0 the boundary row) from gismo side 1-4."""
+    if side == 1:
+        return [(k, j) for j in range(n2)]
+    if side == 2:
+        return [(n1 - 1 - k, j) for j in range(n2)]
+    if side == 3:
+        return [(i, k) for i in range(n1)]
+    return [(i, n2 - 1 - k) for i in range(n1)]
+
+
+def _solve_with_symmetry(oracle_mod, path, elevate, refine, material, point_loads, dirichlet, clamped):
+    """Linear solve with the boundary conditions of a reference problem file: ``dirichlet`` and
+    ``clamped`` map a component to its sides.  "Clamped" on a component whose boundary row is
+    free (a symmetry plane) ties the second row of control points to the boundary row (zero
+    slope across the side); ties and fixed dofs enter as u = T q, solved as T^T K T q = T^T F on
+    the oracle's full K and F.  Returns the displacement (ncp x 3) and the net's sizes."""
     p, U1, U2, ctrl, w = xmlio.read_geometry(path, elevate, refine, with_weights=True)
     n1, n2 = len(U1) - p - 1, len(U2) - p - 1
     ncp = n1 * n2
-    prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=ctrl, E=6.825e7, nu=0.3, t=0.04, rho=1.0,
+    E, nu, t = material
+    prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=ctrl, E=E, nu=nu, t=t, rho=1.0,
                           fixed=np.zeros(3 * ncp, dtype=bool), surface_load=np.zeros(3),
-                          point_loads=np.array([[0.0, 0.0, 1.0, 0.0, 0.0], [1.0, 0.0, 0.0, -1.0, 0.0]]), weights=w)
+                          point_loads=np.asarray(point_loads, dtype=np.float64), weights=w)
     oa = oracle_mod.OracleAssembler(prob)
     K, _ = oa.full_tangent_and_fint(np.zeros(3 * ncp))
     F = oa.full_force()
@@ -201,23 +211,39 @@ def _pinched_hemisphere(oracle_mod, path, elevate, refine):
         return c * ncp + j * n1 + i
 
     master = np.arange(3 * ncp)              # the dof each dof equals; -1: fixed at zero
-    for j in range(n2):
-        master[dof(1, 0, j)] = -1
-        master[dof(0, 1, j)], master[dof(2, 1, j)] = dof(0, 0, j), dof(2, 0, j)
-        master[dof(0, n1 - 1, j)] = -1
-        master[dof(1, n1 - 2, j)], master[dof(2, n1 - 2, j)] = dof(1, n1 - 1, j), dof(2, n1 - 1, j)
-    for i in range(n1):
-        for c in range(3):
-            master[dof(c, i, n2 - 1)] = -1
-    tied = master >= 0
-    master[tied & (master[np.maximum(master, 0)] < 0)] = -1      # tied to a fixed dof: fixed
+    for c, sides in clamped.items():
+        for side in sides:
+            for (i0, j0), (i1, j1) in zip(_side_row(side, 0, n1, n2), _side_row(side, 1, n1, n2)):
+                master[dof(c, i1, j1)] = dof(c, i0, j0)
+    for c, sides in dirichlet.items():
+        for side in sides:
+            for i, j in _side_row(side, 0, n1, n2):
+                master[dof(c, i, j)] = -1
+    while True:                              # resolve chains of ties; a tie to a fixed dof fixes
+        m = master >= 0
+        nxt = master.copy()
+        nxt[m] = master[master[m]]
+        if np.array_equal(nxt, master):
+            break
+        master = nxt
     keep = np.unique(master[master >= 0])
     col = np.full(3 * ncp, -1)
     col[keep] = np.arange(len(keep))
     rows = np.nonzero(master >= 0)[0]
     T = sp.csr_matrix((np.ones(len(rows)), (rows, col[master[rows]])), shape=(3 * ncp, len(keep)))
     u = T @ spla.spsolve((T.T @ K @ T).tocsc(), T.T @ F)
-    return u[dof(0, 0, 0)], -u[dof(1, n1 - 1, 0)]
+    return u.reshape(3, ncp).T, n1, n2
+
+
+def _pinched_hemisphere(oracle_mod, path, elevate, refine):
+    """filedata/pde/kirchhoff_shell_hemisphere.xml: t 0.04, E 6.825e7, nu 0.3; unit point loads
+    +x at (0, 0) and -y at (1, 0); Dirichlet x on sides 2 and 4, y on 1 and 4, z on 4 (the
+    pole); clamped x on side 1, y on side 2, z on sides 1 and 2.  Returns the outward
+    displacement at the +x load and the inward one at the -y load."""
+    u, n1, n2 = _solve_with_symmetry(oracle_mod, path, elevate, refine, (6.825e7, 0.3, 0.04),
+                                     [[0.0, 0.0, 1.0, 0.0, 0.0], [1.0, 0.0, 0.0, -1.0, 0.0]],
+                                     {0: [2, 4], 1: [1, 4], 2: [4]}, {0: [1], 1: [2], 2: [1, 2]})
+    return u[0, 0], -u[n1 - 1, 1]
 
 
 def test_pinched_hemisphere_matches_the_published_kirchhoff_love_value(tmp_path, oracle_mod):
@@ -230,6 +256,52 @@ def test_pinched_hemisphere_matches_the_published_kirchhoff_love_value(tmp_path,
         vals.append(a)
     assert abs(vals[-1] - 0.0924) <= 0.002 * 0.0924
     assert abs(vals[-1] - vals[-2]) <= 0.001 * vals[-1]
+
+
+def _cylinder_eighth_xml(path, R=300.0, L=600.0):
+    """One eighth of the pinched cylinder as a TensorNurbs2: direction 0 along the axis x from
+    the diaphragm (x = 0) to the mid-section (x = L / 2), direction 1 the quarter circle from
+    (y, z) = (R, 0) to (0, R) (rational quadratic, middle weight cos(45 degrees)).  This is the
+    orientation the conditions of filedata/pde/kirchhoff_shell_pinchedCylinder.xml describe:
+    side 1 the rigid diaphragm, side 2 the mid-section, sides 3 and 4 the planes z = 0 and
+    y = 0, the load at corner (1, 1)."""
+    c = math.cos(math.pi / 4)
+    coefs, w = [], []
+    for y, z, wj in [(R, 0.0, 1.0), (R, R, c), (0.0, R, 1.0)]:
+        for x in (0.0, L / 4, L / 2):
+            coefs.append(f"{x!r} {y!r} {z!r}")
+            w.append(wj)
+    with open(path, "w") as f:
+        f.write(f"""<?xml version="1.0" encoding="UTF-8"?>
+<xml>
+ <Geometry type="TensorNurbs2" id="0">
+  <Basis type="TensorNurbsBasis2">
+   <Basis type="TensorBSplineBasis2">
+    <Basis type="BSplineBasis" index="0"><KnotVector degree="2">0 0 0 1 1 1</KnotVector></Basis>
+    <Basis type="BSplineBasis" index="1"><KnotVector degree="2">0 0 0 1 1 1</KnotVector></Basis>
+   </Basis>
+   <weights>{' '.join(repr(v) for v in w)}</weights>
+  </Basis>
+  <coefs geoDim="3">{' '.join(coefs)}</coefs>
+ </Geometry>
+</xml>""")
+
+
+def test_pinched_cylinder_matches_the_published_value(tmp_path, oracle_mod):
+    """filedata/pde/kirchhoff_shell_pinchedCylinder.xml (test case 4 of
+    examples/gsThinShell_Static_XML.cpp): R 300, L 600, t 3, E 3e6, nu 0.3, rigid diaphragms,
+    a quarter of the unit pinching load at the one-eighth model's corner; Dirichlet x on side 2,
+    y on sides 1 and 4, z on sides 1 and 3; clamped x on sides 3 and 4, y on 2 and 3, z on 2
+    and 4.  The displacement under the load converges to the published 1.8248e-5."""
+    path = os.path.join(tmp_path, "pinched_cylinder.xml")
+    _cylinder_eighth_xml(path)
+    vals = []
+    for refine in (4, 5):                    # degree 4, 16 x 16 and 32 x 32 elements
+        u, n1, n2 = _solve_with_symmetry(oracle_mod, path, 2, refine, (3e6, 0.3, 3.0), [[1.0, 1.0, 0.0, 0.0, -0.25]],
+                                         {0: [2], 1: [1, 4], 2: [1, 3]}, {0: [3, 4], 1: [2, 3], 2: [2, 4]})
+        vals.append(-u[n1 * n2 - 1, 2])
+    assert abs(vals[-1] - 1.8248e-5) <= 0.003 * 1.8248e-5
+    assert abs(vals[-1] - vals[-2]) <= 0.005 * vals[-1]
 
 
 def test_device_problem_refuses_rational_patches(lib):
