@@ -241,9 +241,18 @@ def _reject_rational(prob):
         raise NotImplementedError("rational (NURBS) patch: the device kernels evaluate a polynomial B-spline basis")
 
 
+def _reject_ties(prob):
+    """The device problem eliminates fixed dofs only; dofs tied to others (clamped symmetry
+    sides) are solved by the FP64 oracle for now."""
+    t = getattr(prob, "ties", None)
+    if t is not None and len(t):
+        raise NotImplementedError("tied dofs (clamped symmetry sides): the device problem eliminates fixed dofs only")
+
+
 def _patch_desc(prob, keep):
     """PatchDesc of a problems.PatchProblem; the arrays it points to are stored in ``keep``."""
     _reject_rational(prob)
+    _reject_ties(prob)
     k = dict(
         k1=np.ascontiguousarray(prob.knots1, dtype=np.float64),
         k2=np.ascontiguousarray(prob.knots2, dtype=np.float64),

@@ -74,6 +74,7 @@ class PatchProblem:
     nq: int = 0                          # Gauss points per direction (0: p+1)
     name: str = ""
     weights: np.ndarray | None = None    # NURBS weights (ncp,); None: B-spline
+    ties: np.ndarray | None = None       # (k, 2) full-layout dofs [dof, equal to dof]; None: none
 
     @property
     def ncp(self) -> int:

@@ -7,9 +7,10 @@ The reader follows what ``solvers/static_shell_XML.cpp:92-199`` takes from a fil
   id 10       the material: ``MaterialMatrix type="Linear3"`` (Thickness, Density,
               Parameters E and nu), or the older ``Function`` ids 10-13 tagged ``Material``
               (thickness, E, nu, density)
-  id 20       ``boundaryConditions``: ``Dirichlet`` (homogeneous), ``Clamped`` (on a side whose
-              boundary row is Dirichlet-fixed in that component), ``Neumann`` (constant edge
-              load), corner values ``cv`` (zero)
+  id 20       ``boundaryConditions``: ``Dirichlet`` (homogeneous), ``Clamped`` (zero slope
+              across the side: the second row of control points is fixed where the boundary
+              row is fixed, and tied to the boundary row where it is free, as on a symmetry
+              plane), ``Neumann`` (constant edge load), corner values ``cv`` (zero)
   id 21 / 22  surface force (constant 3-vector) / pressure (must be zero: the device path has
               dead loads only)
   id 30-32    point loads: parametric points (2 x N), forces (3 x N), patch indices
@@ -26,9 +27,14 @@ homogeneous coordinates (w X, w), which is exact as well.
 Side numbers are gismo's boxSide (1 west xi1=0, 2 east xi1=1, 3 south xi2=0, 4 north xi2=1) and
 corner numbers its boxCorner (1 (0,0), 2 (1,0), 3 (0,1), 4 (1,1)).  Anything the device path
 cannot represent (several patches, unequal degrees, repeated interior knots, non-SVK materials,
-inhomogeneous or coupled conditions, pressure, non-constant functions) raises
-``NotImplementedError`` with the reason.  NURBS weights are read into ``PatchProblem.weights``:
-the FP64 oracle assembles rational patches, the device problem does not yet (it raises).
+inhomogeneous conditions, pressure, non-constant functions) raises ``NotImplementedError`` with
+the reason.  NURBS weights are read into ``PatchProblem.weights`` and the ties of clamped
+symmetry sides into ``PatchProblem.ties``; the FP64 oracle takes both, the device problem
+neither yet (it raises).
+
+As the reference's XML shell example (examples/gsThinShell_Static_XML.cpp:108-109), ``read``
+takes the geometry and the problem (material, conditions, loads, options) from one file or from
+two.
 """
 from __future__ import annotations
 
@@ -304,12 +310,14 @@ def read_geometry(path: str, elevate: int = 0, refine: int = 0, with_weights: bo
     return (p1, U1, U2, ctrl, w) if with_weights else (p1, U1, U2, ctrl)
 
 
-def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProblem:
+def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0, pde: str | None = None) -> XMLProblem:
     """Read a problem file; ``elevate`` / ``refine`` as the -e / -r arguments of the reference's
-    XML solvers (static_shell_XML.cpp:95-104)."""
-    root = _parse(path)
+    XML solvers (static_shell_XML.cpp:95-104).  With ``pde`` the geometry comes from ``path``
+    and everything else from ``pde``."""
+    groot = _parse(path)
+    U1, U2, p1, p2, ctrl, weights = _geometry(groot, _by_id(groot))
+    root = groot if pde is None else _parse(pde)
     ids = _by_id(root)
-    U1, U2, p1, p2, ctrl, weights = _geometry(root, ids)
     U1, U2, p1, p2, ctrl, weights = _elevate_refine(U1, U2, p1, p2, ctrl, weights, elevate, refine)
     if p1 != p2:
         raise NotImplementedError(f"degrees {p1} and {p2}: the device path takes equal degrees")
@@ -361,12 +369,15 @@ def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProble
             A = _corner(int(cv.get("corner")), n1, n2)
             for c in comps(cv):
                 fixed[c, A] = True
+    ties = []
     for s, c in clamped:
         # gsThinShellAssembler couples the second row to the boundary row (zero normal slope);
         # with the boundary row fixed that fixes the second row
-        if not fixed[c, _side_rows(s, n1, n2, 0)].all():
-            raise NotImplementedError("clamped side without a Dirichlet-fixed boundary row")
-        fixed[c, _side_rows(s, n1, n2, 1)] = True
+        rows0, rows1 = _side_rows(s, n1, n2, 0), _side_rows(s, n1, n2, 1)
+        if fixed[c, rows0].all():
+            fixed[c, rows1] = True
+        else:
+            ties += [(c * n1 * n2 + b, c * n1 * n2 + a) for a, b in zip(rows0, rows1)]
 
     surface = np.zeros(3)
     for el in ids.get(21, []):
@@ -386,7 +397,8 @@ def read(path: str, elevate: int = 0, refine: int = 0, nq: int = 0) -> XMLProble
     prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=np.ascontiguousarray(ctrl), E=E, nu=nu,
                           t=t, rho=rho, fixed=fixed.ravel(), surface_load=surface, point_loads=point_loads,
                           edge_loads=np.array(edge_loads, dtype=np.float64).reshape(-1, 4), nq=nq,
-                          name=f"xml:{path.rsplit('/', 1)[-1]}", weights=weights)
+                          name=f"xml:{path.rsplit('/', 1)[-1]}", weights=weights,
+                          ties=np.array(ties, dtype=np.int64).reshape(-1, 2) if ties else None)
     out = XMLProblem(prob)
     for k in range(90, 96):
         for el in ids.get(k, []):

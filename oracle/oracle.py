@@ -78,6 +78,29 @@ def basis(p: int, knots: np.ndarray, u: float) -> tuple[int, np.ndarray]:
     return span, out.reshape(3, p + 1)
 
 
+def constraint_matrix(fixed, ties):
+    """u = T q for fixed dofs (zero) and tied dofs (``ties`` rows [dof, equal to dof]): each dof
+    maps to the independent dof at the end of its chain of ties, or to nothing when the chain
+    reaches a fixed dof; the independent dofs are numbered in full-layout order."""
+    n = len(fixed)
+    master = np.arange(n)
+    ties = np.asarray(ties, dtype=np.int64).reshape(-1, 2)
+    master[ties[:, 0]] = ties[:, 1]
+    master[np.asarray(fixed, dtype=bool)] = -1
+    while True:
+        m = master >= 0
+        nxt = master.copy()
+        nxt[m] = master[master[m]]
+        if np.array_equal(nxt, master):
+            break
+        master = nxt
+    keep = np.unique(master[master >= 0])
+    col = np.full(n, -1)
+    col[keep] = np.arange(len(keep))
+    rows = np.flatnonzero(master >= 0)
+    return sp.csr_matrix((np.ones(len(rows)), (rows, col[master[rows]])), shape=(n, len(keep)))
+
+
 class OracleAssembler:
     """FP64 assembly of one patch problem; matrices/vectors in free-dof order."""
 
@@ -97,6 +120,12 @@ class OracleAssembler:
         L.klo_full_pattern(P.p, P.n1, P.n2, _ptr(self.rowptr), _ptr(self.cols))
         self.free = P.free_index()
         self.nfree = len(self.free)
+        # tied dofs (clamped symmetry sides): u = T q over the independent dofs instead of the
+        # selection of the free ones
+        ties = getattr(P, "ties", None)
+        self.T = None if ties is None or not len(ties) else constraint_matrix(P.fixed, ties)
+        if self.T is not None:
+            self.nfree = self.T.shape[1]
         self._F = None
 
     def _wptr(self):
@@ -137,16 +166,23 @@ class OracleAssembler:
 
     # -- free-dof (eliminated) versions, the objects the reference's callbacks return -----
     def to_full(self, x: np.ndarray) -> np.ndarray:
+        if self.T is not None:
+            return self.T @ x
         u = np.zeros(3 * self.prob.ncp)
         u[self.free] = x
         return u
 
     def restrict(self, A):
+        if self.T is not None:
+            return (self.T.T @ A @ self.T).tocsr()
         return A[self.free][:, self.free].tocsr()
+
+    def restrict_vector(self, v: np.ndarray) -> np.ndarray:
+        return self.T.T @ v if self.T is not None else v[self.free]
 
     def force(self) -> np.ndarray:
         if self._F is None:
-            self._F = self.full_force()[self.free]
+            self._F = self.restrict_vector(self.full_force())
         return self._F.copy()
 
     def jacobian(self, x: np.ndarray):
@@ -155,7 +191,7 @@ class OracleAssembler:
 
     def fint(self, x: np.ndarray) -> np.ndarray:
         _, f = self.full_tangent_and_fint(self.to_full(x), False)
-        return f[self.free]
+        return self.restrict_vector(f)
 
     def residual(self, x: np.ndarray) -> np.ndarray:
         """Residual_t convention: R = Fext - Fint (tutorials/nonlinear_shell_static.cpp:128-135)."""

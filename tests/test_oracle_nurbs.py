@@ -190,49 +190,42 @@ def _side_row(side, k, n1, n2):
     return [(i, n2 - 1 - k) for i in range(n1)]
 
 
-def _solve_with_symmetry(oracle_mod, path, elevate, refine, material, point_loads, dirichlet, clamped):
-    """Linear solve with the boundary conditions of a reference problem file: ``dirichlet`` and
-    ``clamped`` map a component to its sides.  "Clamped" on a component whose boundary row is
-    free (a symmetry plane) ties the second row of control points to the boundary row (zero
-    slope across the side); ties and fixed dofs enter as u = T q, solved as T^T K T q = T^T F on
-    the oracle's full K and F.  Returns the displacement (ncp x 3) and the net's sizes."""
+def _hand_problem(path, elevate, refine, material, point_loads, dirichlet, clamped):
+    """The problem of a reference problem file built by hand: ``dirichlet`` and ``clamped`` map a
+    component to its sides.  "Clamped" ties the second row of control points to the boundary
+    row (zero slope across the side); where the boundary row is fixed the tie fixes it too."""
     p, U1, U2, ctrl, w = xmlio.read_geometry(path, elevate, refine, with_weights=True)
     n1, n2 = len(U1) - p - 1, len(U2) - p - 1
     ncp = n1 * n2
-    E, nu, t = material
-    prob = P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=ctrl, E=E, nu=nu, t=t, rho=1.0,
-                          fixed=np.zeros(3 * ncp, dtype=bool), surface_load=np.zeros(3),
-                          point_loads=np.asarray(point_loads, dtype=np.float64), weights=w)
-    oa = oracle_mod.OracleAssembler(prob)
-    K, _ = oa.full_tangent_and_fint(np.zeros(3 * ncp))
-    F = oa.full_force()
-
-    def dof(c, i, j):
-        return c * ncp + j * n1 + i
-
-    master = np.arange(3 * ncp)              # the dof each dof equals; -1: fixed at zero
-    for c, sides in clamped.items():
-        for side in sides:
-            for (i0, j0), (i1, j1) in zip(_side_row(side, 0, n1, n2), _side_row(side, 1, n1, n2)):
-                master[dof(c, i1, j1)] = dof(c, i0, j0)
+    fixed = np.zeros((3, n2, n1), dtype=bool)
+    ties = []
     for c, sides in dirichlet.items():
         for side in sides:
             for i, j in _side_row(side, 0, n1, n2):
-                master[dof(c, i, j)] = -1
-    while True:                              # resolve chains of ties; a tie to a fixed dof fixes
-        m = master >= 0
-        nxt = master.copy()
-        nxt[m] = master[master[m]]
-        if np.array_equal(nxt, master):
-            break
-        master = nxt
-    keep = np.unique(master[master >= 0])
-    col = np.full(3 * ncp, -1)
-    col[keep] = np.arange(len(keep))
-    rows = np.nonzero(master >= 0)[0]
-    T = sp.csr_matrix((np.ones(len(rows)), (rows, col[master[rows]])), shape=(3 * ncp, len(keep)))
-    u = T @ spla.spsolve((T.T @ K @ T).tocsc(), T.T @ F)
-    return u.reshape(3, ncp).T, n1, n2
+                fixed[c, j, i] = True
+    for c, sides in clamped.items():
+        for side in sides:
+            for (i0, j0), (i1, j1) in zip(_side_row(side, 0, n1, n2), _side_row(side, 1, n1, n2)):
+                ties.append((c * ncp + j1 * n1 + i1, c * ncp + j0 * n1 + i0))
+    E, nu, t = material
+    return P.PatchProblem(p=p, n1=n1, n2=n2, knots1=U1, knots2=U2, ctrl=ctrl, E=E, nu=nu, t=t, rho=1.0,
+                          fixed=fixed.ravel(), surface_load=np.zeros(3),
+                          point_loads=np.asarray(point_loads, dtype=np.float64), weights=w,
+                          ties=np.array(ties, dtype=np.int64))
+
+
+def _linear_solution(oracle_mod, prob):
+    """K_L q = F over the independent dofs (the oracle's u = T q for fixed and tied dofs); the
+    displacement per control point (ncp x 3)."""
+    oa = oracle_mod.OracleAssembler(prob)
+    u = oa.to_full(spla.spsolve(oa.linear().tocsc(), oa.force()))
+    return u.reshape(3, prob.ncp).T
+
+
+HEMISPHERE = dict(material=(6.825e7, 0.3, 0.04), point_loads=[[0.0, 0.0, 1.0, 0.0, 0.0], [1.0, 0.0, 0.0, -1.0, 0.0]],
+                  dirichlet={0: [2, 4], 1: [1, 4], 2: [4]}, clamped={0: [1], 1: [2], 2: [1, 2]})
+CYLINDER = dict(material=(3e6, 0.3, 3.0), point_loads=[[1.0, 1.0, 0.0, 0.0, -0.25]],
+                dirichlet={0: [2], 1: [1, 4], 2: [1, 3]}, clamped={0: [3, 4], 1: [2, 3], 2: [2, 4]})
 
 
 def _pinched_hemisphere(oracle_mod, path, elevate, refine):
@@ -240,10 +233,9 @@ def _pinched_hemisphere(oracle_mod, path, elevate, refine):
     +x at (0, 0) and -y at (1, 0); Dirichlet x on sides 2 and 4, y on 1 and 4, z on 4 (the
     pole); clamped x on side 1, y on side 2, z on sides 1 and 2.  Returns the outward
     displacement at the +x load and the inward one at the -y load."""
-    u, n1, n2 = _solve_with_symmetry(oracle_mod, path, elevate, refine, (6.825e7, 0.3, 0.04),
-                                     [[0.0, 0.0, 1.0, 0.0, 0.0], [1.0, 0.0, 0.0, -1.0, 0.0]],
-                                     {0: [2, 4], 1: [1, 4], 2: [4]}, {0: [1], 1: [2], 2: [1, 2]})
-    return u[0, 0], -u[n1 - 1, 1]
+    prob = _hand_problem(path, elevate, refine, **HEMISPHERE)
+    u = _linear_solution(oracle_mod, prob)
+    return u[0, 0], -u[prob.n1 - 1, 1]
 
 
 def test_pinched_hemisphere_matches_the_published_kirchhoff_love_value(tmp_path, oracle_mod):
@@ -297,11 +289,48 @@ def test_pinched_cylinder_matches_the_published_value(tmp_path, oracle_mod):
     _cylinder_eighth_xml(path)
     vals = []
     for refine in (4, 5):                    # degree 4, 16 x 16 and 32 x 32 elements
-        u, n1, n2 = _solve_with_symmetry(oracle_mod, path, 2, refine, (3e6, 0.3, 3.0), [[1.0, 1.0, 0.0, 0.0, -0.25]],
-                                         {0: [2], 1: [1, 4], 2: [1, 3]}, {0: [3, 4], 1: [2, 3], 2: [2, 4]})
-        vals.append(-u[n1 * n2 - 1, 2])
+        u = _linear_solution(oracle_mod, _hand_problem(path, 2, refine, **CYLINDER))
+        vals.append(-u[-1, 2])
     assert abs(vals[-1] - 1.8248e-5) <= 0.003 * 1.8248e-5
     assert abs(vals[-1] - vals[-2]) <= 0.005 * vals[-1]
+
+
+REFERENCE_TREE = os.environ.get("KLSA_REFERENCE_TREE", "/root/reference")
+
+
+@pytest.mark.parametrize("case", ["hemisphere", "pinchedCylinder"])
+def test_reference_problem_files_through_the_reader(tmp_path, oracle_mod, case):
+    """The reference's own problem files read by xmlio.read(geometry, pde=file), as its XML shell
+    example reads them (a geometry file and a problem file): the material, the point loads, the
+    fixed dofs and the ties of the clamped symmetry sides are the hand-built problem's, and the
+    oracle solves it to the same displacement."""
+    from oracle import constraint_matrix
+    pde = os.path.join(REFERENCE_TREE, "filedata", "pde", f"kirchhoff_shell_{case}.xml")
+    if not os.path.exists(pde):
+        pytest.skip("reference tree not present")
+    geo = os.path.join(tmp_path, "geometry.xml")
+    (_quarter_hemisphere_xml if case == "hemisphere" else _cylinder_eighth_xml)(geo)
+    spec = HEMISPHERE if case == "hemisphere" else CYLINDER
+    r = xmlio.read(geo, elevate=2, refine=4, pde=pde)
+    hand = _hand_problem(geo, 2, 4, **spec)
+    got = r.problem
+    assert (got.E, got.nu, got.t) == spec["material"]
+    np.testing.assert_array_equal(got.point_loads, np.asarray(spec["point_loads"]))
+    assert got.ties is not None and len(got.ties)
+    Tg, Th = constraint_matrix(got.fixed, got.ties), constraint_matrix(hand.fixed, hand.ties)
+    assert Tg.shape == Th.shape and (Tg != Th).nnz == 0
+    ug, uh = _linear_solution(oracle_mod, got), _linear_solution(oracle_mod, hand)
+    assert np.abs(ug - uh).max() <= 1e-12 * np.abs(uh).max()
+
+
+def test_device_problem_refuses_tied_dofs(lib, tmp_path):
+    import gsstructuralanalysis_gb300 as G
+    geo = os.path.join(tmp_path, "cylinder.xml")
+    _cylinder_eighth_xml(geo)
+    prob = _hand_problem(geo, 0, 1, **CYLINDER)
+    prob.weights = None                      # keep only the ties to refuse
+    with pytest.raises(NotImplementedError, match="tied dofs"):
+        G.Problem(prob)
 
 
 def test_device_problem_refuses_rational_patches(lib):
