@@ -286,6 +286,25 @@ int refh_alm_reduce_length(void* a, double fac) {
         return 0;
     });
 }
+// gsALMBase::isBifurcation / computeSingularPoint / switchBranch (gsALMBase.hpp:421-512, 628-852)
+int refh_alm_is_bifurcation(void* a, int jacobian) {
+    return guard([&] { return static_cast<RefALM*>(a)->alm->isBifurcation(jacobian != 0) ? 1 : 0; });
+}
+int refh_alm_compute_singular_point(void* a, const double* U, double L, int switch_branch, int jacobian,
+                                    int test_point) {
+    return guard([&] {
+        RefALM* A = static_cast<RefALM*>(a);
+        gsVector<real_t> u(A->P->n);
+        std::memcpy(u.data(), U, sizeof(double) * A->P->n);
+        return (int)A->alm->computeSingularPoint(u, L, switch_branch != 0, jacobian != 0, test_point != 0);
+    });
+}
+int refh_alm_switch_branch(void* a) {
+    return guard([&] {
+        static_cast<RefALM*>(a)->alm->switchBranch();
+        return 0;
+    });
+}
 // out: [numIterations, indicator, stability, stabilityChange, getLength]
 int refh_alm_info(void* a, double* out) {
     return guard([&] {

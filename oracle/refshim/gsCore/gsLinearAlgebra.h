@@ -22,6 +22,13 @@
 #include <iostream>
 #include <limits>
 #include <map>
+// The reference calls abs() unqualified on floating-point values inside namespace gismo
+// (gsALMBase.hpp:496-497 and 808-811, gsALMCrisfield.hpp:85 and 281).  With <cstdlib> alone the
+// only global abs is C's int abs(int), and |x| is truncated to an integer.  The C++ wrappers
+// <stdlib.h> and <math.h> put std::abs's floating-point overloads in the global namespace, as a
+// translation unit that includes either of them anywhere gets them; that is the abs meant.
+#include <math.h>
+#include <stdlib.h>
 #include <memory>
 #include <numeric>
 #include <sstream>

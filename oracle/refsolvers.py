@@ -74,6 +74,9 @@ def lib():
         L.refh_alm_set_length.argtypes = [_vp, ctypes.c_double]
         L.refh_alm_reduce_length.argtypes = [_vp, ctypes.c_double]
         L.refh_alm_info.argtypes = [_vp, _vp]
+        L.refh_alm_is_bifurcation.argtypes = [_vp, ctypes.c_int]
+        L.refh_alm_compute_singular_point.argtypes = [_vp, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.refh_alm_switch_branch.argtypes = [_vp]
         L.refh_newton_create.restype = _vp
         L.refh_newton_create.argtypes = [_vp, ctypes.c_char_p]
         L.refh_newton_destroy.argtypes = [_vp]
@@ -229,6 +232,24 @@ class ALM:
 
     def reduce_length(self, fac=0.5):
         lib().refh_alm_reduce_length(self.h, float(fac))
+
+    def is_bifurcation(self, jacobian=False) -> bool:
+        r = lib().refh_alm_is_bifurcation(self.h, int(jacobian))
+        if r < 0:
+            raise RuntimeError(_err())
+        return bool(r)
+
+    def compute_singular_point(self, U, L, switch_branch=False, jacobian=False, test_point=True) -> int:
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        st = lib().refh_alm_compute_singular_point(self.h, _p(U), float(L), int(switch_branch), int(jacobian),
+                                                   int(test_point))
+        if st < 0:
+            raise RuntimeError(_err())
+        return st
+
+    def switch_branch(self):
+        if lib().refh_alm_switch_branch(self.h) < 0:
+            raise RuntimeError(_err())
 
     def info(self):
         out = np.zeros(5)

@@ -43,6 +43,10 @@ def run_alm(case, A):
         U_prev, L_prev = U, L
         U, L = alm.solution()
         info = alm.info()
+        if case["options"].get("BifurcationMethod", -1) < 0:
+            # without a stability method gsALMBase never sets m_indicator or m_stability
+            # (gsALMBase.hpp:97-103, 381, 613-614): the flags would be uninitialised memory
+            info["stability"] = info["stability_change"] = 0.0
         for key, v in (("U", U), ("L", L), ("iterations", info["iterations"]), ("status", st),
                        ("stability", info["stability"]), ("stability_change", info["stability_change"])):
             out[key].append(v)

@@ -348,3 +348,37 @@ def test_apalm_over_riks_matches_reference(oracle_mod):
     ref.solve(4)
     ora.solve(4)
     _same_flat_path(ref, ora)
+
+
+@pytest.mark.parametrize("tolB", [0.0, 1e-2])
+def test_singular_point_matches_reference(oracle_mod, tolB):
+    """At the roof's limit point (the step where the Determinant indicator changes sign):
+    isBifurcation (_testSingularPoint: inverse iteration, |V.F| against the tolerance),
+    computeSingularPoint without and with the bisection stage (SingularPointComputeTolB), and
+    switchBranch, of the compiled gsALMBase against the restatement (gsALMBase.hpp:421-512,
+    628-852).  The reference's unqualified abs() is the floating-point one here (the stand-in
+    sees the <stdlib.h> / <math.h> overloads)."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=8, p=2, load=1.0))
+    opts = dict(Length=0.004, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=8, BifurcationMethod=0,
+                SingularPointComputeTolB=tolB)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(12):
+        Ur, Lr = ref.solution()
+        Uo, Lo = ora.U.copy(), ora.L
+        assert ref.step() == ora.step() == 0, k
+        assert bool(ref.info()["stability_change"]) == ora.stability_change(), k
+        if ora.stability_change():
+            break
+    else:
+        pytest.fail("no stability change")
+    assert ref.is_bifurcation(False) == ora.is_bifurcation(False) is False      # a limit point
+    assert ref.compute_singular_point(Ur, Lr, False, False, False) == ora.compute_singular_point(Uo, Lo, False, False, False) == 0
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
+    ref.switch_branch()
+    ora.switch_branch()
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
