@@ -382,3 +382,33 @@ def test_singular_point_matches_reference(oracle_mod, tolB):
     ora.switch_branch()
     U, L = ref.solution()
     assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
+
+
+def test_eigenvalue_stability_indicator_against_reference_builds(oracle_mod):
+    """BifurcationMethod 1 (Eigenvalue) along a Crisfield path through the limit point.  The
+    reference has two builds (gsALMBase.hpp:_computeStability): with Spectra, a shift-invert
+    solve at the shift -100 that keeps the eigenvalues with the largest 1/(lambda + 100), so its
+    indicator is the smallest eigenvalue ABOVE the shift; without Spectra (as compiled here), a
+    dense SelfAdjointEigenSolver, the smallest eigenvalue.  The restatement (and the GPU) follow
+    the Spectra build.  So: wherever the dense indicator is above the shift the two agree, flags
+    included; where an eigenvalue lies below the shift the Spectra-build indicator stays above
+    it (the path is then called stable there)."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=5, p=2, load=1.0))
+    opts = dict(ALM_BASE, Length=0.006, BifurcationMethod=1)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    agree = below = 0
+    for k in range(10):
+        assert ref.step() == ora.step() == 0, k
+        U, L = ref.solution()
+        assert _rel(ora.U, U) < 1e-10, k
+        dense = ref.info()["indicator"]
+        if dense > -100.0:
+            assert abs(ora.indicator - dense) <= 1e-8 * abs(dense), k
+            agree += 1
+        else:
+            assert ora.indicator > -100.0, k
+            below += 1
+    assert agree >= 5 and below >= 1
