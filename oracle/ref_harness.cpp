@@ -519,4 +519,26 @@ int refh_dyn_state(void* h, double* U, double* V, double* A, double* info) {
     });
 }
 
+// gsBucklingSolver(K_L, F, Jacobian_t, scaling) (gsBucklingSolver.h:50-67, 127-149: u_L =
+// K_L^-1 scaling F through SimplicialLDLT, B = K(u_L) - K_L) followed by computePower
+// (gsEigenProblemBase.hpp:218-258).  value: 1, vector: n.  Returns the gsStatus, or -1.
+int refh_buckling_power(void* prob, double scaling, const char* options, double* value, double* vector) {
+    return guard([&] {
+        RefProblem* P = static_cast<RefProblem*>(prob);
+        typename gsStructuralAnalysisOps<real_t>::Jacobian_t J = [P](gsVector<real_t> const& x, gsSparseMatrix<real_t>& m) {
+            return P->jacobian(x, m);
+        };
+        gsSparseMatrix<real_t> KL = P->KL;
+        gsVector<real_t> F = P->F;
+        gsBucklingSolver<real_t> B(KL, F, J, scaling);
+        gsOptionList o;
+        apply_options(o, options);
+        B.options().update(o, gsOptionList::addIfUnknown);
+        const gsStatus st = B.computePower();
+        *value = B.values()(0, 0);
+        std::memcpy(vector, B.vectors().data(), sizeof(double) * P->n);
+        return (int)st;
+    });
+}
+
 }  // extern "C"

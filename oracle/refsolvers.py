@@ -96,6 +96,7 @@ def lib():
         L.refh_apalm_branches.argtypes = [_vp]
         L.refh_apalm_points.argtypes = [_vp, ctypes.c_int]
         L.refh_apalm_point.argtypes = [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp]
+        L.refh_buckling_power.argtypes = [_vp, ctypes.c_double, ctypes.c_char_p, _vp, _vp]
         L.refh_dyn_create.restype = _vp
         L.refh_dyn_create.argtypes = [ctypes.c_int, ctypes.c_int64, _vp, _vp, ctypes.c_char_p, ctypes.c_int, _TMAT,
                                       _TMAT, _TMAT, _TVEC, ctypes.c_char_p]
@@ -306,6 +307,15 @@ def eigen_dense(kind: str, A, B, options: dict | None = None, power: bool = Fals
     if st < 0:
         raise RuntimeError(_err())
     return st, vals, vecs
+
+
+def buckling_power(ops: Operators, scaling: float, options: dict | None = None):
+    """gsBucklingSolver(K_L, F, Jacobian_t, scaling).computePower(): (status, value, vector)."""
+    val, vec = np.zeros(1), np.zeros(ops.n)
+    st = lib().refh_buckling_power(ops.h, float(scaling), option_spec(options or {}), _p(val), _p(vec))
+    if st < 0:
+        raise RuntimeError(_err())
+    return st, float(val[0]), vec
 
 
 class APALM:

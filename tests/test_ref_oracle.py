@@ -412,3 +412,33 @@ def test_eigenvalue_stability_indicator_against_reference_builds(oracle_mod):
             assert ora.indicator > -100.0, k
             below += 1
     assert agree >= 5 and below >= 1
+
+
+@pytest.mark.parametrize("edge_load", [1.0, -1.0])
+def test_buckling_solver_power_matches_reference(oracle_mod, edge_load):
+    """gsBucklingSolver built from K_L, the load and the Jacobian callback (its own set-up: u_L =
+    K_L^-1 s F, B = K(u_L) - K_L), then computePower, on the simply supported square plate:
+    the eigenvalue of smallest |lambda| is the restatement's (the dense pencil's) and gives
+    q_cr = 4 pi^2 D / b^2.  Under tension the iterates converge (Success); under compression the
+    dominant eigenvalue of A^-1 B is negative, the iterates flip sign every step and the
+    reference stops NotConverged after its 100 steps -- with the same value."""
+    E, nu, t = 1.0, 0.3, 0.01
+    prob = P.flat_plate(m=8, p=3, E=E, nu=nu, t=t, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True
+    fixed[0, ii == 0] = True
+    fixed[1, 0] = True
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, edge_load, 0.0, 0.0]])
+    A = oracle_mod.OracleAssembler(prob)
+    s = 1e-8
+    st, val, vec = RS.buckling_power(RS.Operators.from_assembler(A), s, {"tolerance": 1e-12})
+    assert st == (0 if edge_load > 0 else 1)
+    lam, _, _ = oracle_mod.buckling_dense(A.linear(), A.force(), A.jacobian, nev=1, shift=0.0, scaling=s)
+    assert abs(val - lam[0]) <= 1e-8 * abs(lam[0])
+    D = E * t ** 3 / (12 * (1 - nu ** 2))
+    assert abs(abs(val) * s / (4 * np.pi ** 2 * D) - 1) < 1e-4
+    assert np.sign(val) == np.sign(edge_load)
