@@ -208,6 +208,52 @@ def test_singular_point_and_branch_switch(lib, oracle_mod, tolB):
     assert found
 
 
+def test_bifurcation_and_branch_switch(lib, oracle_mod):
+    """A genuine bifurcation (the flat plate under in-plane compression, no imperfection): the
+    singular-point test finds the null vector orthogonal to the load, the extended system
+    converges to the critical point, switchBranch steps onto the buckled branch and two steps
+    follow it, against the oracle (gsALMBase.hpp:421-512, 628-852); the oracle's points are the
+    compiled reference's (tests/test_ref_oracle.py)."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.flat_plate(m=6, p=2, E=1.0, nu=0.3, t=0.01, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True
+    fixed[0, ii == 0] = True
+    fixed[1, 0] = True
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, -1e-6, 0.0, 0.0]])
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    opts = dict(Length=2e-4, TolF=1e-9, TolU=1e-9, Scaling=0.0, MaxIter=20, BifurcationMethod=0,
+                SingularPointComputeTolB=0.0)
+    alm = G.ALMCrisfield(gp, dict(opts, FrontPrecision=64))
+    alm.initialize()
+    ref = oracle_mod.ALMCrisfield(oa.jacobian, oa.al_residual, oa.force(), opts)
+    ref.initialize()
+    for k in range(15):
+        Uold, Lold = alm.solutionU(), alm.solutionL()
+        Uref, Lref = ref.U.copy(), ref.L
+        assert alm.step() == 0 and ref.step() == 0, k
+        assert alm.stabilityChange() == ref.stability_change(), k
+        if ref.stability_change():
+            break
+    else:
+        pytest.fail("no stability change")
+    assert alm.isBifurcation(False) and ref.is_bifurcation(False)
+    assert alm.computeSingularPoint(Uold, Lold, False, False, False) == 0
+    assert ref.compute_singular_point(Uref, Lref, False, False, False) == 0
+    assert abs(alm.solutionL() - ref.L) <= 1e-8 * abs(ref.L)
+    assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-6 * np.linalg.norm(ref.U)
+    alm.switchBranch()
+    ref.switch_branch()
+    for k in range(2):
+        assert alm.step() == 0 and ref.step() == 0, k
+        assert abs(alm.solutionL() - ref.L) <= 1e-6 * abs(ref.L), k
+        assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-5 * np.linalg.norm(ref.U), k
+
+
 @pytest.mark.parametrize("method", ["Crisfield", "Riks"])
 def test_reference_predictor_guess(lib, oracle_mod, method):
     """setInitialGuess in the reference's own mode, step by step against the oracle.  Crisfield

@@ -442,3 +442,53 @@ def test_buckling_solver_power_matches_reference(oracle_mod, edge_load):
     D = E * t ** 3 / (12 * (1 - nu ** 2))
     assert abs(abs(val) * s / (4 * np.pi ** 2 * D) - 1) < 1e-4
     assert np.sign(val) == np.sign(edge_load)
+
+
+def test_bifurcation_and_branch_switch_match_reference(oracle_mod):
+    """A genuine bifurcation: the flat simply supported plate under in-plane compression (no
+    imperfection).  Crisfield with the Determinant indicator runs up the membrane path; at the
+    stability change the singular-point test finds the null vector orthogonal to the load
+    (isBifurcation true), the extended system converges to the critical point (within 1.2 % of
+    q_cr = 4 pi^2 D / b^2 on this 6 x 6 quadratic mesh), switchBranch steps onto the buckled
+    branch, and three steps follow it -- every point the restatement's."""
+    E, nu, t = 1.0, 0.3, 0.01
+    prob = P.flat_plate(m=6, p=2, E=E, nu=nu, t=t, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True
+    fixed[0, ii == 0] = True
+    fixed[1, 0] = True
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, -1e-6, 0.0, 0.0]])
+    A = oracle_mod.OracleAssembler(prob)
+    opts = dict(Length=2e-4, TolF=1e-9, TolU=1e-9, Scaling=0.0, MaxIter=20, BifurcationMethod=0,
+                SingularPointComputeTolB=0.0)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(15):
+        Ur, Lr = ref.solution()
+        Uo, Lo = ora.U.copy(), ora.L
+        assert ref.step() == ora.step() == 0, k
+        assert bool(ref.info()["stability_change"]) == ora.stability_change(), k
+        if ora.stability_change():
+            break
+    else:
+        pytest.fail("no stability change")
+    assert ref.is_bifurcation(False) is True and ora.is_bifurcation(False) is True
+    assert ref.compute_singular_point(Ur, Lr, False, False, False) == ora.compute_singular_point(Uo, Lo, False, False, False) == 0
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
+    D = E * t ** 3 / (12 * (1 - nu ** 2))
+    assert abs(L * 1e-6 / (4 * np.pi ** 2 * D) - 1) < 0.012
+    ref.switch_branch()
+    ora.switch_branch()
+    for k in range(3):
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10, k
+        assert ref.step() == ora.step() == 0, k
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
