@@ -282,7 +282,8 @@ uint64_t MFSolver::generation() const {
 
 int MFSolver::compute_tangent() {
     cudaEvent_t ev = g_timer.begin(P_.stream);
-    if (refine_ > 0 || fp64_) P_.tangent_f64();
+    tangent_f64_ = refine_ > 0 || fp64_;
+    if (tangent_f64_) P_.tangent_f64();
     else P_.tangent_f32();
     g_timer.end(P_.stream, 0, ev);
     return factor_current(refine_ > 0);

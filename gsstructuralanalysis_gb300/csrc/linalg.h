@@ -24,6 +24,8 @@ public:
     virtual bool solve_pair(const double*, double, const double*, double, double*, double*) { return false; }
     // identifies the factorisation the solver currently holds (0: none / not a factorisation)
     virtual uint64_t generation() const { return 0; }
+    // the tangent of the last compute_tangent() sits in the FP64 CSR values (else the FP32 ones)
+    virtual bool tangent_values_f64() const { return false; }
 };
 
 // Multifrontal LDL^T.  fp64 = false: FP32 fronts (FP32 or FP64-assembled values rounded), with
@@ -40,6 +42,7 @@ public:
     void stability(double* min_d, int64_t* neg) override;
     int last_iterations() const override { return last_refine_its_; }
     uint64_t generation() const override;
+    bool tangent_values_f64() const override { return tangent_f64_; }
     void set_refine(int r) { refine_ = r; }
 
 private:
@@ -49,6 +52,7 @@ private:
     double tol_;
     bool fp64_ = false;
     bool has64_ = false;
+    bool tangent_f64_ = false;     // precision of the last compute_tangent() assembly
     int last_refine_its_ = 0;
     DevBuf<float> b32_, x32_;
     DevBuf<double> r_, dx_;

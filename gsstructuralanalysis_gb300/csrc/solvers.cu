@@ -589,7 +589,7 @@ void ALMGPU::lambdas_crisfield() {
     // simplified complex-root solve (Lam 1992 eq. 13-17)
     eta_ = 1.0;
     vec::lincomb(1.0, U_.get(), 1.0, DU_.get(), x_.get(), n_, s);
-    spmv(P_, false, x_.get(), tmp_.get());            // Fint ~ K (U + DU)
+    spmv(P_, S_->tangent_values_f64(), x_.get(), tmp_.get());   // Fint ~ K (U + DU), the current tangent
     double fF;
     const double* fa[1] = {tmp_.get()};
     const double* fb[1] = {P_.d_F.get()};

@@ -254,6 +254,41 @@ def test_bifurcation_and_branch_switch(lib, oracle_mod):
         assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-5 * np.linalg.norm(ref.U), k
 
 
+def test_crisfield_complex_roots(lib, oracle_mod):
+    """Quasi-Newton Crisfield with a long step on the coarse roof, where the constraint
+    quadratic has no real root inside step 2: the corrector takes Lam's modified quadratic and
+    the complex-root fallback (gsALMCrisfield.hpp:236-330) and still converges.  FP64 fronts;
+    every step's status, iteration count and point (up to the panel's mirror symmetry) against
+    the oracle, whose points are the compiled reference's (tests/test_ref_oracle.py).  Before
+    the fix the complex-root branch multiplied by the FP32 CSR values, which FP64 fronts never
+    assemble, and the step ended in OtherError."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=4, p=2, load=1.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    opts = dict(Length=0.01, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=40, BifurcationMethod=-1, Quasi=True,
+                QuasiIterations=8)
+    alm = G.ALMCrisfield(gp, dict(opts, FrontPrecision=64))
+    alm.initialize(stability=False)
+    ref = oracle_mod.ALMCrisfield(oa.jacobian, oa.al_residual, oa.force(), opts)
+    ref.initialize()
+    # From step 2 on the path leaves the panel's symmetry about x = L / 2 (xi1 -> 1 - xi1,
+    # u_x -> -u_x; a mirrored equilibrium point stays one), and rounding picks the side: the
+    # device may follow the mirror image of the oracle's branch, with the same load factor.
+    free = prob.free_index()
+    pos = np.full(3 * prob.ncp, -1)
+    pos[free] = np.arange(len(free))
+    comp, cp = free // prob.ncp, free % prob.ncp
+    mirror = pos[comp * prob.ncp + (cp // prob.n1) * prob.n1 + (prob.n1 - 1 - cp % prob.n1)]
+    sign = np.where(comp == 0, -1.0, 1.0)
+    for k in range(5):
+        assert alm.step() == 0 and ref.step() == 0, k
+        assert int(alm.info()["iterations"]) == ref.num_iterations, k
+        assert abs(alm.solutionL() - ref.L) <= 1e-8 * abs(ref.L), k
+        U = alm.solutionU()
+        err = min(np.linalg.norm(U - ref.U), np.linalg.norm(U - sign * ref.U[mirror]))
+        assert err <= 1e-7 * np.linalg.norm(ref.U), k
+
+
 @pytest.mark.parametrize("method", ["Crisfield", "Riks"])
 def test_reference_predictor_guess(lib, oracle_mod, method):
     """setInitialGuess in the reference's own mode, step by step against the oracle.  Crisfield

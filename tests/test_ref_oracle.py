@@ -492,3 +492,43 @@ def test_bifurcation_and_branch_switch_match_reference(oracle_mod):
         assert ref.step() == ora.step() == 0, k
     U, L = ref.solution()
     assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-10
+
+
+def test_crisfield_complex_roots_match_reference(oracle_mod):
+    """Quasi-Newton Crisfield (the tangent refreshed every 8 iterations) with a long step on the
+    coarse roof: in step 2 the constraint quadratic has no real root, so the corrector takes Lam's
+    modified quadratic for eta with the 0.05 |eta2 - eta1| shift and, where that fails too, the
+    complex-root fallback (gsALMCrisfield.hpp:236-330); the step still converges, after 25
+    iterations.  Every step -- its status, iteration count and point -- is the reference's, and
+    the restatement is seen to take both paths."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=4, p=2, load=1.0))
+    opts = dict(Length=0.01, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=40, BifurcationMethod=-1, Quasi=True,
+                QuasiIterations=8)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    calls = {"modified": 0, "complex": 0}
+    modified, complex_ = ora._lambdas_modified, ora._lambdas_complex
+
+    def count(name, fn):
+        def wrapped():
+            calls[name] += 1
+            return fn()
+        return wrapped
+
+    ora._lambdas_modified = count("modified", modified)
+    ora._lambdas_complex = count("complex", complex_)
+    converged_with = 0
+    for k in range(6):
+        before = dict(calls)
+        st = ref.step()
+        assert ora.step() == st, k
+        assert int(ref.info()["iterations"]) == ora.num_iterations, k
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
+        if st == 0 and calls["modified"] > before["modified"] and calls["complex"] > before["complex"]:
+            converged_with += 1
+        if st != 0:
+            break
+    assert converged_with >= 1
