@@ -289,6 +289,34 @@ def test_crisfield_complex_roots(lib, oracle_mod):
         assert err <= 1e-7 * np.linalg.norm(ref.U), k
 
 
+@pytest.mark.parametrize("variant", ["Relaxation", "AutoScaling"])
+def test_crisfield_relaxation_and_scaling(lib, oracle_mod, variant):
+    """Relaxation 0.7 (gsALMCrisfield.hpp:84-90) on ten converging steps, and the default Scaling
+    -1 (phi from the first predictor) up to the step that ends NotConverged: FP64 fronts, every
+    status, iteration count and point against the oracle (which matches the compiled
+    reference, tests/test_ref_oracle.py)."""
+    import gsstructuralanalysis_gb300 as G
+    prob = P.cylindrical_panel(m=6, p=2, load=1.0)
+    gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
+    extra = {"Relaxation": dict(Relaxation=0.7, Scaling=0.0), "AutoScaling": dict(Scaling=-1.0)}[variant]
+    opts = dict(Length=0.01, TolF=1e-8, TolU=1e-6, MaxIter=40, BifurcationMethod=-1, **extra)
+    alm = G.ALMCrisfield(gp, dict(opts, FrontPrecision=64))
+    alm.initialize(stability=False)
+    ref = oracle_mod.ALMCrisfield(oa.jacobian, oa.al_residual, oa.force(), opts)
+    ref.initialize()
+    statuses = []
+    for k in range(10):
+        st = ref.step()
+        assert alm.step() == st, k
+        assert int(alm.info()["iterations"]) == ref.num_iterations, k
+        assert abs(alm.solutionL() - ref.L) <= 1e-8 * abs(ref.L), k
+        assert np.linalg.norm(alm.solutionU() - ref.U) <= 1e-7 * np.linalg.norm(ref.U), k
+        statuses.append(st)
+        if st != 0:
+            break
+    assert statuses == ([0] * 10 if variant == "Relaxation" else [0] * 6 + [1])
+
+
 @pytest.mark.parametrize("method", ["Crisfield", "Riks"])
 def test_reference_predictor_guess(lib, oracle_mod, method):
     """setInitialGuess in the reference's own mode, step by step against the oracle.  Crisfield

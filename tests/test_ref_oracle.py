@@ -188,6 +188,32 @@ def test_stability_determinant_matches_reference(oracle_mod):
     assert changes >= 1
 
 
+@pytest.mark.parametrize("variant", ["Relaxation", "AutoScaling"])
+def test_crisfield_relaxation_and_scaling_match_reference(oracle_mod, variant):
+    """Relaxation 0.7 (the corrector's load-factor update is damped when it changes sign and
+    shrinks, gsALMCrisfield.hpp:84-90) on ten converging steps, and the default Scaling -1 (phi
+    from the first predictor, gsALMCrisfield.hpp:111-164) up to the step where both stop
+    NotConverged: every status, iteration count and point is the reference's."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=2, load=1.0))
+    extra = {"Relaxation": dict(Relaxation=0.7, Scaling=0.0), "AutoScaling": dict(Scaling=-1.0)}[variant]
+    opts = dict(ALM_BASE, Length=0.01, MaxIter=40, **extra)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    statuses = []
+    for k in range(10):
+        st = ref.step()
+        assert ora.step() == st, k
+        assert int(ref.info()["iterations"]) == ora.num_iterations, k
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
+        statuses.append(st)
+        if st != 0:
+            break
+    assert statuses == ([0] * 10 if variant == "Relaxation" else [0] * 6 + [1])
+
+
 def test_dense_eigen_compute_and_power_match_reference(oracle_mod):
     """gsEigenProblemBase::compute (dense generalized solver, all pairs, with and without a shift)
     and ::computePower (power iteration on A^-1 B: the pair of smallest |lambda|) of
