@@ -730,7 +730,9 @@ void ALMGPU::step_impl() {
         if (residueF_ < tolF_ && residueU_ < tolU_) {
             iteration_finish();
             if (adaptive_) {
-                double fac = (double)desiredIt_ / num_it_;
+                // gsALMBase::computeLength (gsALMBase.hpp:105-116): a quotient of two index_t,
+                // so an integer division, then clamped to [0.5, 2]
+                double fac = (double)(desiredIt_ / num_it_);
                 fac = std::min(std::max(fac, 0.5), 2.0);
                 arcLength_prev_ = arcLength_;
                 arcLength_ = arcLength_ * fac;

@@ -594,7 +594,9 @@ class _ALMBase:
         return self.arcLength
 
     def compute_length(self):
-        fac = float(self.desiredIt) / self.num_iterations
+        """gsALMBase::computeLength (gsALMBase.hpp:105-116): the factor is the quotient of two
+        index_t, an integer division, clamped to [0.5, 2]."""
+        fac = float(self.desiredIt // self.num_iterations)
         fac = min(max(fac, 0.5), 2.0)
         self.arcLength_prev = self.arcLength
         self.arcLength = self.arcLength * fac

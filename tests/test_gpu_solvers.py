@@ -144,19 +144,21 @@ def test_fp64_fronts(lib, oracle_mod):
     assert st.iterations() == ref.num_iterations
 
 
-@pytest.mark.parametrize("method", ["Crisfield", "Riks", "LoadControl"])
+@pytest.mark.parametrize("method", ["Crisfield", "Riks", "LoadControl", "ConsistentCrisfield"])
 def test_quasi_newton_adaptive_length(lib, oracle_mod, method):
     """Quasi-Newton corrector (Jacobian refreshed every QuasiIterations) with adaptive arc length
-    (gsALMBase.hpp:106-117, 376-387) against the oracle step by step."""
+    (gsALMBase.hpp:106-117, 376-387; the factor an integer quotient) against the oracle step by
+    step; the oracle's lengths are the compiled reference's (tests/test_ref_oracle.py)."""
     import gsstructuralanalysis_gb300 as G
     prob = P.cylindrical_panel(m=8, p=2, load=1e5 if method == "Riks" else 1.0)
     gp, oa = G.Problem(prob), oracle_mod.OracleAssembler(prob)
-    length = {"Crisfield": 0.004, "Riks": 0.003, "LoadControl": 100.0}[method]
+    length = {"Crisfield": 0.004, "Riks": 0.003, "LoadControl": 100.0, "ConsistentCrisfield": 0.004}[method]
     opts = dict(Length=length, TolF=1e-8, TolU=1e-6, Scaling=0.0, MaxIter=60, Quasi=1, QuasiIterations=2,
                 AdaptiveLength=1, AdaptiveIterations=4, BifurcationMethod=-1)
-    cls = {"Crisfield": G.ALMCrisfield, "Riks": G.ALMRiks, "LoadControl": G.ALMLoadControl}[method]
+    cls = {"Crisfield": G.ALMCrisfield, "Riks": G.ALMRiks, "LoadControl": G.ALMLoadControl,
+           "ConsistentCrisfield": G.ALMConsistentCrisfield}[method]
     rcls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks,
-            "LoadControl": oracle_mod.ALMLoadControl}[method]
+            "LoadControl": oracle_mod.ALMLoadControl, "ConsistentCrisfield": oracle_mod.ALMConsistentCrisfield}[method]
     alm = cls(gp, opts)
     alm.initialize()
     ref = rcls(oa.jacobian, oa.al_residual, oa.force(), opts)

@@ -558,3 +558,30 @@ def test_crisfield_complex_roots_match_reference(oracle_mod):
         if st != 0:
             break
     assert converged_with >= 1
+
+
+@pytest.mark.parametrize("method,variant", [(m, v) for m in ("Riks", "LoadControl", "ConsistentCrisfield")
+                                            for v in ("Quasi", "AdaptiveLength")])
+def test_method_variants_match_reference(oracle_mod, method, variant):
+    """Quasi-Newton and AdaptiveLength for Riks, LoadControl and ConsistentCrisfield.  The
+    adaptive factor is AdaptiveIterations / iterations as a quotient of two index_t, an integer
+    division (gsALMBase.hpp:105-116): after a 5-iteration Riks step with 3 desired iterations it
+    is 0, clamped to 0.5 (a real division would give 0.6)."""
+    load, length = {"Riks": (1e5, 0.003), "LoadControl": (1.0, 100.0), "ConsistentCrisfield": (1.0, 0.004)}[method]
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=2, load=load))
+    extra = dict(Quasi=True, QuasiIterations=2) if variant == "Quasi" else dict(AdaptiveLength=True, AdaptiveIterations=3)
+    opts = dict(ALM_BASE, Length=length, **extra)
+    ref = RS.ALM(RS.Operators.from_assembler(A), method, opts)
+    ref.initialize()
+    cls = {"Riks": oracle_mod.ALMRiks, "LoadControl": oracle_mod.ALMLoadControl,
+           "ConsistentCrisfield": oracle_mod.ALMConsistentCrisfield}[method]
+    ora = cls(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(6):
+        assert ref.step() == ora.step() == 0, k
+        assert int(ref.info()["iterations"]) == ora.num_iterations, k
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
+        assert abs(ora.arcLength - ref.info()["length"]) <= 1e-12 * abs(ora.arcLength), k
+    if method == "Riks" and variant == "AdaptiveLength":
+        assert ref.info()["length"] == 0.5 * length
