@@ -585,3 +585,34 @@ def test_method_variants_match_reference(oracle_mod, method, variant):
         assert abs(ora.arcLength - ref.info()["length"]) <= 1e-12 * abs(ora.arcLength), k
     if method == "Riks" and variant == "AdaptiveLength":
         assert ref.info()["length"] == 0.5 * length
+
+
+@pytest.mark.parametrize("solver", ["SimplicialLDLT", "CGDiagonal"])
+def test_static_newton_relaxation_matches_reference(oracle_mod, solver):
+    """gsStaticNewton with Relaxation 0.7 (the update scaled, gsStaticNewton.hpp:160-185): the
+    same iteration count (16, against 4 unrelaxed) and the same solution."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=3, load=800.0))
+    opts = dict(tol=1e-8, maxIt=60, Relaxation=0.7)
+    ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(opts, Solver=solver))
+    ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, opts)
+    assert ref.solve() == ora.solve() == 0
+    assert ref.iterations() == ora.num_iterations == 16
+    assert _rel(ora.U, ref.solution()) < 1e-12
+
+
+@pytest.mark.parametrize("method", ["Newmark", "Bathe", "Wilson", "ImplicitEuler"])
+def test_quasi_newton_integrators_match_reference(oracle_mod, method):
+    """The nonlinear integrators with Quasi (the tangent refreshed every QuasiIterations = 2
+    corrector iterations) on the damped shell under a ramped load: 4 steps, U to 1e-12."""
+    import dynamics as D
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=4, p=2, load=400.0))
+    cb = D.shell_callbacks(A, True, 0.5, 1e-4, D.load_table([0.0, 2e-3], [0.2, 1.0]))
+    n = len(A.force())
+    ora, ref = _dyn_pair(cb, n, method, True, {"TolF": 1e-10, "TolU": 1e-10, "Quasi": 1, "QuasiIterations": 2})
+    z = np.zeros(n)
+    ora.set_state(z, z, z)
+    ref.set_state(z, z, z)
+    for k in range(4):
+        assert ora.step(5e-4) == ref.step(5e-4) == 0, k
+        U, V, _, _, _ = ref.state()
+        assert _close(ora.U, U, 1e-12) and _close(ora.V, V, 1e-11), k
