@@ -616,3 +616,57 @@ def test_quasi_newton_integrators_match_reference(oracle_mod, method):
         assert ora.step(5e-4) == ref.step(5e-4) == 0, k
         U, V, _, _, _ = ref.state()
         assert _close(ora.U, U, 1e-12) and _close(ora.V, V, 1e-11), k
+
+
+def _compressed_plate():
+    prob = P.flat_plate(m=6, p=2, E=1.0, nu=0.3, t=0.01, pressure=0.0, bc="simply")
+    n, ncp = prob.n1, prob.ncp
+    ii, jj = np.arange(ncp) % n, np.arange(ncp) // n
+    bnd = (ii == 0) | (ii == n - 1) | (jj == 0) | (jj == n - 1)
+    fixed = np.zeros((3, ncp), dtype=bool)
+    fixed[2, bnd] = True
+    fixed[0, ii == 0] = True
+    fixed[1, 0] = True
+    prob.fixed = fixed.ravel()
+    prob.edge_loads = np.array([[1, -1e-6, 0.0, 0.0]])
+    return prob
+
+
+@pytest.mark.parametrize("variant,extra,switch,jacobian", [
+    ("Perturbation", dict(Perturbation=1e2), True, False),
+    ("TestIt", dict(SingularPointTestIt=2), False, False),
+    ("ComputeTolE", dict(SingularPointComputeTolE=1e-4), False, False),
+    ("SwitchInside", {}, True, False),
+    ("Jacobian", {}, True, True),
+    ("Bisection", dict(SingularPointComputeTolB=1e-2), True, False),
+    ("FailureSwitch", dict(SingularPointFailure=1, SingularPointComputeTolE=1e-14), True, False),
+])
+def test_singular_point_options_match_reference(oracle_mod, variant, extra, switch, jacobian):
+    """The options of computeSingularPoint at the plate's bifurcation (gsALMBase.hpp:41-46,
+    628-852): the perturbation tau of the extended system, the power iterations of the test, the
+    extended-system tolerance, switching inside the call, a fresh Jacobian, the bisection stage,
+    and SingularPointFailure 1 (switch even when the extended iterations do not converge); the
+    critical point and the next step on the buckled branch are the reference's."""
+    A = oracle_mod.OracleAssembler(_compressed_plate())
+    opts = dict(Length=2e-4, TolF=1e-9, TolU=1e-9, Scaling=0.0, MaxIter=20, BifurcationMethod=0,
+                SingularPointComputeTolB=0.0)
+    opts.update(extra)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    for k in range(15):
+        Ur, Lr = ref.solution()
+        Uo, Lo = ora.U.copy(), ora.L
+        assert ref.step() == ora.step() == 0, k
+        if ora.stability_change():
+            break
+    else:
+        pytest.fail("no stability change")
+    st = ref.compute_singular_point(Ur, Lr, switch, jacobian, True)
+    assert ora.compute_singular_point(Uo, Lo, switch, jacobian, True) == st
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12
+    assert ref.step() == ora.step() == 0
+    U, L = ref.solution()
+    assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12
