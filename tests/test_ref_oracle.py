@@ -670,3 +670,41 @@ def test_singular_point_options_match_reference(oracle_mod, variant, extra, swit
     assert ref.step() == ora.step() == 0
     U, L = ref.solution()
     assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12
+
+
+@_bounded
+@pytest.mark.parametrize("schedule", ["serial", "solve"])
+def test_apalm_branches_at_bifurcation_match_reference(oracle_mod, schedule):
+    """gsAPALM with SingularPoint on the compressed plate: the initiation job that crosses the
+    bifurcation computes the critical point, switches branch and queues the buckled branch as a
+    new start (gsAPALM.hpp:934-1011, BifLengthMultiplier for its first step); serialSolve, or
+    solve with the interval corrections, gives the same two branches as the restatement --
+    points, levels and curve times."""
+    import apalm as AP
+    A = oracle_mod.OracleAssembler(_compressed_plate())
+    alm_opts = dict(Length=2e-4, TolF=1e-9, TolU=1e-9, Scaling=0.0, MaxIter=20, BifurcationMethod=0,
+                    SingularPointComputeTolB=0.0)
+    ap_opts = dict(SubIntervals=2, MaxIt=40, SingularPoint=True, BranchLengthMultiplier=1.0, BifLengthMultiplier=0.1)
+    data_opts = dict(MaxLevel=1, Tolerance=1e-3)
+    ref_alm = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", alm_opts)
+    ref_alm.initialize()
+    ref = RS.APALM(ref_alm, ap_opts, data_opts)
+    ora_alm = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), alm_opts)
+    ora_alm.initialize()
+    ora = AP.APALM(ora_alm, dict(ap_opts, **data_opts))
+    ref.initialize()
+    ora.initialize()
+    if schedule == "serial":
+        ref.serial_solve(14)
+        ora.serial_solve(14)
+    else:
+        ref.solve(14)
+        ora.solve(14)
+    assert ref.branches() == len(ora.times) == 2
+    for b in range(2):
+        Us, Ls, ts, lvs = ref.flat(b)
+        assert len(ts) == len(ora.times[b]) > 10 and lvs == list(ora.levels[b])
+        np.testing.assert_allclose(ora.times[b], ts, rtol=1e-12, atol=1e-15)
+        for U, L, (Uo, Lo) in zip(Us, Ls, ora.solutions[b]):
+            assert abs(Lo - L) <= 1e-12 * max(abs(L), 1e-300)
+            assert _rel(Uo, U) < 1e-12 or np.abs(U).max() == np.abs(Uo).max() == 0
