@@ -708,3 +708,31 @@ def test_apalm_branches_at_bifurcation_match_reference(oracle_mod, schedule):
         for U, L, (Uo, Lo) in zip(Us, Ls, ora.solutions[b]):
             assert abs(Lo - L) <= 1e-12 * max(abs(L), 1e-300)
             assert _rel(Uo, U) < 1e-12 or np.abs(U).max() == np.abs(Uo).max() == 0
+
+
+@pytest.mark.parametrize("method", ["ConsistentCrisfield", "Riks"])
+def test_determinant_flags_other_methods_match_reference(oracle_mod, method):
+    """BifurcationMethod 0 along ConsistentCrisfield (through both limit points of the roof: two
+    stability changes) and Riks (up to the step where both stop NotConverged): every status,
+    stability flag and point is the reference's."""
+    load, length, steps = {"ConsistentCrisfield": (1.0, 0.004, 20), "Riks": (1e5, 0.002, 40)}[method]
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=2, load=load))
+    opts = dict(ALM_BASE, Length=length, MaxIter=60, BifurcationMethod=0)
+    ref = RS.ALM(RS.Operators.from_assembler(A), method, opts)
+    ref.initialize()
+    cls = {"ConsistentCrisfield": oracle_mod.ALMConsistentCrisfield, "Riks": oracle_mod.ALMRiks}[method]
+    ora = cls(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    changes = 0
+    for k in range(steps):
+        st = ref.step()
+        assert ora.step() == st, k
+        if st != 0:
+            break
+        info = ref.info()
+        assert int(info["stability"]) == ora.stability and bool(info["stability_change"]) == ora.stability_change(), k
+        changes += int(info["stability_change"])
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
+    assert changes == (2 if method == "ConsistentCrisfield" else 0)
+    assert (st == 0) == (method == "ConsistentCrisfield")
