@@ -199,7 +199,14 @@ def _geometry(root, ids):
             elif el.tag == "Geometry":
                 g = el
     if g is None:
-        raise ValueError("no geometry with id 0")
+        others = sorted(int(e.get("id")) for e in root.iter("Geometry") if e.get("id") is not None)
+        if len(others) > 1:
+            # a file of several patches without a MultiPatch naming them (gsReadFile reads them all)
+            raise NotImplementedError(f"{len(others)} patches (geometry ids {others}): the device path takes one patch")
+        if len(others) == 1:
+            g = next(e for e in root.iter("Geometry") if e.get("id") is not None)
+        else:
+            raise ValueError("no geometry in the file")
     typ = g.get("type")
     basis = g.find("Basis")
     weights = None

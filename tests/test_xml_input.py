@@ -1,6 +1,7 @@
 """XML problem input (gsstructuralanalysis_gb300/xmlio.py) on CPU: files in the reference's
 gsFileData layout, elevated and refined as the reference's XML solvers do, give exactly the
 problems built directly in gsstructuralanalysis_gb300.problems; unsupported content is rejected."""
+import glob
 import os
 
 import numpy as np
@@ -138,3 +139,26 @@ def test_reference_roof_geometry_file(oracle_mod):
         assert alm.step() == 0
         assert np.linalg.norm(alm.U - fix["U"][k]) <= 1e-10 * np.linalg.norm(fix["U"][k])
         assert abs(alm.L - fix["L"][k]) <= 1e-10 * abs(fix["L"][k])
+
+
+def test_reader_on_every_reference_surface_file():
+    """Every surface and planar geometry file the reference ships: the single-patch shells load
+    (B-spline or NURBS, the weights kept), and the rest are refused with their reason -- several
+    patches, or a planar (geoDim 2) geometry."""
+    root = os.path.join(os.environ.get("KLSA_REFERENCE_TREE", "/root/reference"), "filedata")
+    files = sorted(glob.glob(os.path.join(root, "surface", "*.xml")) + glob.glob(os.path.join(root, "planar", "*.xml")))
+    if not files:
+        pytest.skip("reference tree not present")
+    loaded, refused = [], []
+    for f in files:
+        try:
+            p, U1, U2, ctrl, w = X.read_geometry(f, 0, 0, with_weights=True)
+            assert ctrl.shape == ((len(U1) - p - 1) * (len(U2) - p - 1), 3)
+            assert w is None or len(w) == len(ctrl)
+            loaded.append(os.path.basename(f))
+        except NotImplementedError as e:
+            assert "patches" in str(e) or "planar" in str(e), (f, e)
+            refused.append(os.path.basename(f))
+    assert "scordelis_lo_roof_shallow.xml" in loaded and "quarter_sphere.xml" in loaded
+    assert "frustrum.xml" in refused
+    assert len(loaded) >= 8
