@@ -736,3 +736,21 @@ def test_determinant_flags_other_methods_match_reference(oracle_mod, method):
         assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
     assert changes == (2 if method == "ConsistentCrisfield" else 0)
     assert (st == 0) == (method == "ConsistentCrisfield")
+
+
+@pytest.mark.parametrize("solver", ["SimplicialLDLT", "CGDiagonal"])
+def test_static_newton_solve_linear_matches_reference(oracle_mod, solver):
+    """gsStaticNewton::solveLinear (gsStaticNewton.hpp:57-99, 195-213): K_L u = F with the named
+    solver, on the clamped plate and on the roof; then a zero pivot (E = 0) is SolverError for
+    the factorising solver."""
+    for prob in (P.flat_plate(m=4, p=2), P.cylindrical_panel(m=6, p=3, load=800.0)):
+        A = oracle_mod.OracleAssembler(prob)
+        ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(Solver=solver))
+        ora = oracle_mod.StaticNewton(A.linear(), A.force(), A.jacobian, A.residual, {})
+        assert ref.solve_linear() == 0
+        U = ora.solve_linear()                                  # the restatement returns u (_solveLinear)
+        tol = 1e-12 if solver == "SimplicialLDLT" else 1e-8      # CG to machine-epsilon residual
+        assert _rel(U, ref.solution()) < tol
+    A = oracle_mod.OracleAssembler(P.flat_plate(m=4, p=2, E=0.0))
+    ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(Solver="SimplicialLDLT"))
+    assert ref.solve_linear() == 3
