@@ -1,14 +1,14 @@
-"""The oracle's restatement (oracle/oracle.py) pinned against the reference's OWN solver code.
+"""The restatements (oracle/oracle.py, oracle/apalm.py, oracle/dynamics.py) pinned against the
+reference's OWN solver code.
 
 oracle/_ref/libref_solvers.so is gsStaticNewton, gsALMCrisfield, gsALMRiks, gsALMLoadControl,
-gsALMConsistentCrisfield, gsModalSolver, gsBucklingSolver and the six time integrators of
-gsDynamicSolvers compiled unchanged from the reference tree against the test-only
-linear-algebra stand-in (oracle/refshim/; its GMRES, used by gsDynamicImplicitEuler, solves the
-block operator exactly).  Both sides get
-the same FP64 KL-shell operators (oracle.OracleAssembler), so every difference would be a
-difference of solver logic.  The reference tree exists only where the library can be built;
-elsewhere these tests skip (the golden fixtures written from it, tests/golden/ref_solvers.npz,
-carry the pin to the GPU tests).
+gsALMConsistentCrisfield, gsAPALM (without MPI), gsModalSolver, gsBucklingSolver and the six
+time integrators of gsDynamicSolvers, compiled unchanged from the reference tree against the
+test-only linear-algebra stand-in (oracle/refshim/; its GMRES, used by gsDynamicImplicitEuler,
+solves the block operator exactly).  Both sides get the same FP64 KL-shell operators
+(oracle.OracleAssembler), so every difference would be a difference of solver logic.  The
+reference tree exists only where the library can be built; elsewhere these tests skip (the
+golden fixtures written from it, tests/golden/ref_solvers.npz, carry the pin to the GPU tests).
 """
 import numpy as np
 import pytest
