@@ -331,6 +331,8 @@ def test_device_problem_refuses_tied_dofs(lib, tmp_path):
     prob.weights = None                      # keep only the ties to refuse
     with pytest.raises(NotImplementedError, match="tied dofs"):
         G.Problem(prob)
+    with pytest.raises(NotImplementedError, match="tied dofs"):
+        G.BatchedProblem([prob])
 
 
 def test_device_problem_refuses_rational_patches(lib):
