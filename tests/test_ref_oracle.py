@@ -142,13 +142,16 @@ def test_crisfield_variants_match_reference(oracle_mod, variant):
         assert abs(ora.arcLength - ref.info()["length"]) <= 1e-12 * abs(ora.arcLength), k
 
 
-@pytest.mark.parametrize("method", ["Crisfield", "Riks"])
+@pytest.mark.parametrize("method", ["Crisfield", "Riks", "ConsistentCrisfield", "LoadControl"])
 def test_predictor_guess_matches_reference(oracle_mod, method):
-    """setInitialGuess -> predictorGuess (gsALMCrisfield.hpp:167-191, gsALMRiks.hpp:137-170)."""
+    """setInitialGuess -> predictorGuess (gsALMCrisfield.hpp:167-191, gsALMRiks.hpp:137-170,
+    gsALMConsistentCrisfield.hpp:150-175, gsALMLoadControl.hpp)."""
     prob = P.cylindrical_panel(m=6, p=2, load=1e5 if method == "Riks" else 1.0)
     A = oracle_mod.OracleAssembler(prob)
-    opts = dict(ALM_BASE, Length=0.004 if method == "Crisfield" else 0.003)
-    cls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks}[method]
+    opts = dict(ALM_BASE, Length={"Crisfield": 0.004, "Riks": 0.003, "ConsistentCrisfield": 0.004,
+                                  "LoadControl": 100.0}[method])
+    cls = {"Crisfield": oracle_mod.ALMCrisfield, "Riks": oracle_mod.ALMRiks,
+           "ConsistentCrisfield": oracle_mod.ALMConsistentCrisfield, "LoadControl": oracle_mod.ALMLoadControl}[method]
     ref = RS.ALM(RS.Operators.from_assembler(A), method, opts)
     ref.initialize()
     ora = cls(A.jacobian, A.al_residual, A.force(), opts)
