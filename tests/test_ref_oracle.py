@@ -757,3 +757,29 @@ def test_static_newton_solve_linear_matches_reference(oracle_mod, solver):
     A = oracle_mod.OracleAssembler(P.flat_plate(m=4, p=2, E=0.0))
     ref = RS.StaticNewton(RS.Operators.from_assembler(A), dict(Solver="SimplicialLDLT"))
     assert ref.solve_linear() == 3
+
+
+def test_failure_recovery_with_reduce_length_matches_reference(oracle_mod):
+    """The reference drivers' recovery: after a NotConverged step, reduceLength(0.5) and step
+    again from the last converged point (gsALMBase.hpp:118-123, 328-351).  Fourteen steps with the
+    default automatic Scaling, three of them failing: every status, iteration count, arc length
+    and point is the reference's."""
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=6, p=2, load=1.0))
+    opts = dict(ALM_BASE, Scaling=-1.0, MaxIter=40, Length=0.01)
+    ref = RS.ALM(RS.Operators.from_assembler(A), "Crisfield", opts)
+    ref.initialize()
+    ora = oracle_mod.ALMCrisfield(A.jacobian, A.al_residual, A.force(), opts)
+    ora.initialize()
+    failures = 0
+    for k in range(14):
+        st = ref.step()
+        assert ora.step() == st, k
+        assert int(ref.info()["iterations"]) == ora.num_iterations, k
+        U, L = ref.solution()
+        assert abs(ora.L - L) <= 1e-12 * abs(L) and _rel(ora.U, U) < 1e-12, k
+        if st != 0:
+            failures += 1
+            ref.reduce_length(0.5)
+            ora.reduce_length(0.5)
+        assert ora.arcLength == ref.info()["length"], k
+    assert failures == 3
