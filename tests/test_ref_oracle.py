@@ -783,3 +783,26 @@ def test_failure_recovery_with_reduce_length_matches_reference(oracle_mod):
             ora.reduce_length(0.5)
         assert ora.arcLength == ref.info()["length"], k
     assert failures == 3
+
+
+@pytest.mark.parametrize("nonlinear", [False, True])
+@pytest.mark.parametrize("method,params", [("Newmark", dict(alpha=0.3025, delta=0.6)), ("Bathe", dict(gamma=0.6)),
+                                           ("Wilson", dict(gamma=1.37)),
+                                           ("Bathe", dict(alpha=0.3025, delta=0.6, gamma=0.5))])
+def test_integrator_parameters_match_reference(oracle_mod, method, params, nonlinear):
+    """The integrators' own options away from their defaults (gsDynamicNewmark / Bathe / Wilson
+    defaultOptions): Newmark with numerical damping (alpha 0.3025, delta 0.6), Bathe's sub-step
+    gamma and its Newmark stage parameters, Wilson's theta (gamma); 4 steps on the damped shell,
+    U and V to 1e-12 of their maxima."""
+    import dynamics as D
+    A = oracle_mod.OracleAssembler(P.cylindrical_panel(m=4, p=2, load=400.0))
+    cb = D.shell_callbacks(A, nonlinear, 0.5, 1e-4, D.load_table([0.0, 2e-3], [0.2, 1.0]))
+    n = len(A.force())
+    ora, ref = _dyn_pair(cb, n, method, nonlinear, dict({"TolF": 1e-10, "TolU": 1e-10}, **params))
+    z = np.zeros(n)
+    ora.set_state(z, z, z)
+    ref.set_state(z, z, z)
+    for k in range(4):
+        assert ora.step(5e-4) == ref.step(5e-4) == 0, k
+        U, V, _, _, _ = ref.state()
+        assert _close(ora.U, U, 1e-12) and _close(ora.V, V, 1e-12), k
